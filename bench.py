@@ -1,0 +1,307 @@
+"""Headline benchmark: plain wavefront path tracing of the 5.2M-triangle
+scene (64 displaced icospheres of 81,920 triangles, ground quad, four quad
+lights, constant environment 0.05) at 1920x1080, 64 spp, max depth 16,
+Russian roulette from depth 4, NEE + MIS, per-pixel curand streams.
+
+One step = one PathTracer frame (w*h*spp samples).  `value` is Msamples/s
+with the scene resident in HBM; `e2e` is the same metric through the C ABI
+with the frame parameters handed over from host memory and the film read
+back to pinned host memory every step.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Multi-GPU runs (torchrun) render independent replicas: each rank renders
+the full frame, value = all ranks' samples / max rank time (weak scaling).
+`--impl reference` times the reference's path-tracing algorithm on the
+host cores (the oracle's CPU restatement) on a bounded crop.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msamples/s and p50/p99 job latency at equal relMSE vs plain tracer, 1 GB300"
+W, H, SPP, MAX_DEPTH, RR_DEPTH, SEED = 1920, 1080, 64, 16, 4, 1
+N_SPHERES, SUBDIV = 64, 6
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 8:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[4:8]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        finally:
+            try:
+                os.remove(self.path)
+            except OSError:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_scene(S):
+    arrays = S.procedural("spheres", seed=SEED, n_spheres=N_SPHERES, subdiv=SUBDIV)
+    arrays.set_aspect(W / H)
+    return arrays
+
+
+def cpu_baseline(arrays, steps=1, budget_s=20.0):
+    """The oracle's megakernel restatement on the host cores, on a crop of
+    the same frame (bounded to about `budget_s` seconds of CPU work)."""
+    from oracle import oracle as O
+    import srt_gb300 as S
+    threads = os.cpu_count() or 1
+    osc = O.OracleScene(arrays.desc())
+    t0 = time.perf_counter()
+    osc.build_bvh()
+    build_s = time.perf_counter() - t0
+    # calibrate on a small crop, then size the crop to the budget
+    cw = ch = 32
+    spp = 1
+    p = S.pt_params(spp, MAX_DEPTH, RR_DEPTH, 1, 1, SEED)
+    x0, y0 = (W - cw) // 2, (H - ch) // 2
+    t0 = time.perf_counter()
+    osc.render(W, H, p, crop=(x0, y0, cw, ch), threads=threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rate = cw * ch * spp / dt
+    target = rate * budget_s / max(1, steps)
+    side = int(max(32, min(512, (target / 4) ** 0.5)))
+    spp = 4
+    x0, y0 = (W - side) // 2, (H - side) // 2
+    p = S.pt_params(spp, MAX_DEPTH, RR_DEPTH, 1, 1, SEED)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        osc.render(W, H, p, crop=(x0, y0, side, side), threads=threads)
+        times.append(time.perf_counter() - t0)
+    value = side * side * spp * len(times) / sum(times) / 1e6
+    return {"value": round(value, 4), "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"centre crop {side}x{side} of the {W}x{H} frame, {spp} spp, depth {MAX_DEPTH}, "
+                      f"oracle CPU BVH (build {build_s:.1f}s, not timed), {threads} threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import srt_gb300 as S
+    arrays = build_scene(S)
+    steps = max(1, args.steps)
+    cb = cpu_baseline(arrays, steps=steps, budget_s=min(60.0, 12.0 * steps))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(None), "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(info):
+    d = {"workload": "5.2M-triangle synthetic scene (64 icospheres subdiv 6, value-noise displaced), "
+                     "plain wavefront PT FP32", "width": W, "height": H, "spp": SPP, "max_depth": MAX_DEPTH,
+         "rr_depth": RR_DEPTH, "nee": True, "mis": True, "rng": "curand XORWOW per pixel",
+         "l2": "scene larger than L2 (no flush between steps)"}
+    if info:
+        d["triangles"] = info["num_triangles"]
+        d["scene_mb"] = round(info["device_bytes"] / 2 ** 20, 1)
+        d["bvh_nodes"] = info["num_nodes"]
+        d["bvh_build_s"] = round(info["build_ms"] / 1000, 2)
+    return d
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+    import srt_gb300 as S
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    arrays = build_scene(S)
+    scene = S.Scene(arrays)
+    info = scene.info()
+    pt = S.PathTracer(scene, W, H)
+    film = torch.zeros((W * H, 4), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    params = S.pt_params(SPP, MAX_DEPTH, RR_DEPTH, 1, 1, SEED)
+
+    for i in range(args.warmup):
+        params.seed = SEED + 1000 + i
+        pt.render(film, params, stream)
+    barrier()
+
+    # ---- device-resident timed region ----------------------------------
+    launches = 0
+    with Clocks(local) as clk:
+        barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for i in range(args.steps):
+            params.seed = SEED + i
+            pt.render(film, params, stream)
+            launches += pt.stats()["kernel_launches"]
+        ev1.record()
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    samples = W * H * SPP * args.steps * world
+    value = samples / (ms / 1e3) / 1e6
+    clocks = clk.summary()
+
+    # ---- end to end through the C ABI with host buffers -----------------
+    host_film = torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True)
+    h2d = C_PARAM_BYTES = 32 + 48  # srt_pt_params + srt_camera_desc handed over per frame
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        params.seed = SEED + 500 + i
+        scene.set_camera(arrays.camera)
+        pt.render(film, params, stream)
+        host_film.copy_(film, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_value = samples / float(t.item()) / 1e6
+
+    # ---- one profiled frame: per-kernel times and traversal traffic -----
+    pt.set_profiling(True)
+    params.seed = SEED + 900
+    pt.render(film, params, stream)
+    st = pt.stats()
+    pt.set_profiling(False)
+    names = ["k_closest", "k_shade", "k_shadow", "k_regen", "k_advance"]
+    kms = dict(zip(names, st["kernel_ms"]))
+    top = max(kms, key=kms.get)
+    # algorithmic bytes: per ray the ray (24 B) in and the hit (16 B) out, plus
+    # the BVH nodes (128 B) and triangles (48 B) the traversal fetches
+    if top == "k_shadow":
+        rays, nodes, tris = st["shadow_rays"], st["shadow_nodes"], st["shadow_tris"]
+        per_ray = 44
+    else:
+        rays, nodes, tris = st["closest_rays"], st["closest_nodes"], st["closest_tris"]
+        per_ray = 40
+    alg_bytes = rays * per_ray + nodes * 128 + tris * 48
+    iters = max(1, st["iterations"])
+    achieved = alg_bytes / (kms[top] / 1e3) / 1e9 if kms[top] > 0 else 0.0
+    peak, peak_kind = peaks()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_dict(info),
+            "clocks": clocks,
+            "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": W * H * 16},
+            "gpu_launches": int(launches),
+            "mrays_per_s": round((st["closest_rays"] + st["shadow_rays"]) / (sum(st["kernel_ms"]) / 1e3) / 1e6, 1)
+            if sum(st["kernel_ms"]) > 0 else None,
+            "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": None, "launches": iters,
+                         "per_launch_ms": round(kms[top] / iters, 4),
+                         "alg_bytes_per_launch": int(alg_bytes / iters),
+                         "nodes_per_ray": round(nodes / max(rays, 1), 2),
+                         "tris_per_ray": round(tris / max(rays, 1), 2)},
+            "profile_frame": {"kernel_ms": {k: round(v, 2) for k, v in kms.items()},
+                              "closest_rays": st["closest_rays"], "shadow_rays": st["shadow_rays"],
+                              "iterations": st["iterations"]},
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(arrays, steps=1, budget_s=20.0)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,340 @@
+/*
+ * srt.h — C ABI of the GB300-native wavefront path tracer.
+ *
+ * Every entry point takes plain pointers and sizes.  Device pointers are
+ * passed as `void*` / `float*` and must point to memory on the current CUDA
+ * device; `stream` is a `cudaStream_t` passed as `void*` (NULL = legacy
+ * default stream).  No entry point calls exit() or traps: failures come back
+ * as an `srt_status` and the last message is readable via srt_last_error().
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the woAIxuexiSR/SRT source tree).
+ */
+#ifndef SRT_H
+#define SRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Replaces `cout << "ERROR::..."; exit(-1)` (src/passes/renderpass.h:59-62,
+ * src/main/main.cu:9-13) and checkCudaErrors / OPTIX_CHECK exits
+ * (src/device_include/helper_optix.h:12-20). */
+typedef enum srt_status {
+    SRT_OK = 0,
+    SRT_ERR_ARG = 1,         /* invalid argument / inconsistent sizes          */
+    SRT_ERR_OOM = 2,         /* device or host allocation failed               */
+    SRT_ERR_CUDA = 3,        /* a CUDA runtime call failed                     */
+    SRT_ERR_TIMEOUT = 4,     /* a bounded device/host wait ran out             */
+    SRT_ERR_BUDGET = 5,      /* admission refused: HBM budget would be exceeded */
+    SRT_ERR_STACK = 6,       /* traversal stack overflowed (result incomplete) */
+    SRT_ERR_NOT_FOUND = 7,   /* unknown render-pass / scene name               */
+    SRT_ERR_PARSE = 8,       /* malformed JSON configuration                   */
+    SRT_ERR_UNSUPPORTED = 9  /* feature outside this build (textures, ...)     */
+} srt_status;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* srt_last_error(void);
+/* Library version string. */
+const char* srt_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Scene description (host arrays)                                     */
+/* ------------------------------------------------------------------ */
+
+/* BxDF::Type, src/device_include/scene/bxdf.h:62 */
+typedef enum srt_bxdf_type {
+    SRT_BXDF_DIFFUSE = 0,
+    SRT_BXDF_DIFFUSE_TRANSMISSION = 1,
+    SRT_BXDF_DIELECTRIC = 2,
+    SRT_BXDF_DISNEY = 3
+} srt_bxdf_type;
+
+/* BxDF parameters, same names, order and defaults as
+ * src/device_include/scene/bxdf.h:64-76 (52 bytes). */
+typedef struct srt_bxdf {
+    int32_t type;
+    float ior, metallic, subsurface, roughness, specular, specularTint,
+          anisotropic, sheen, sheenTint, clearcoat, clearcoatGloss, specTrans;
+} srt_bxdf;
+
+/* Material, src/scene/material.h:8-19 (texture ids unsupported). */
+typedef struct srt_material {
+    srt_bxdf bxdf;
+    float base_color[3];
+    float emission_color[3];
+    float intensity;          /* > 0 makes every instance of it an area light */
+} srt_material;
+
+/* TriangleMesh, src/scene/mesh.h:63-93.  Vertices/normals are float3
+ * packed (3 floats each); indices are uint3 packed.  Tangents and
+ * texture coordinates are not supported (no textures in this build). */
+typedef struct srt_mesh {
+    const float* vertices;     /* 3 * num_vertices                    */
+    const uint32_t* indices;   /* 3 * num_faces                       */
+    const float* normals;      /* 3 * num_vertices, or NULL           */
+    int32_t num_vertices;
+    int32_t num_faces;
+    int32_t material_id;       /* index into srt_scene_desc.materials */
+} srt_mesh;
+
+/* Scene::add_instance(transform, mesh), src/scene/scene.cu:194-202.
+ * transform: row-major 3x4 (the top 3 rows of the reference's 4x4). */
+typedef struct srt_instance {
+    int32_t mesh_id;
+    float transform[12];
+} srt_instance;
+
+/* Camera::Type, src/device_include/scene/camera.h:96 */
+typedef enum srt_camera_type {
+    SRT_CAMERA_PERSPECTIVE = 0,
+    SRT_CAMERA_ORTHOGRAPHIC = 1,
+    SRT_CAMERA_THINLENS = 2,
+    SRT_CAMERA_ENVIRONMENT = 3
+} srt_camera_type;
+
+/* The "camera" JSON block of Renderer::load_scene, src/renderer/renderer.cu:125-140:
+ * LookAt(position, target, up), radius = |position - target|, vertical fov
+ * in degrees, aspect = width / height. */
+typedef struct srt_camera_desc {
+    int32_t type;
+    float position[3];
+    float target[3];
+    float up[3];
+    float fov;
+    float aspect;
+    float aperture;           /* thin lens only (camera.h:101) */
+    float focal;              /* thin lens only                */
+} srt_camera_desc;
+
+/* Scene::build_gscene inputs, src/scene/scene.cu:214-418; env_color is the
+ * constant EnvironmentLight (src/device_include/scene/light.h:204-234). */
+typedef struct srt_scene_desc {
+    const srt_mesh* meshes;
+    int32_t num_meshes;
+    const srt_instance* instances;
+    int32_t num_instances;
+    const srt_material* materials;
+    int32_t num_materials;
+    srt_camera_desc camera;
+    float env_color[3];
+} srt_scene_desc;
+
+typedef struct srt_scene srt_scene;
+
+typedef struct srt_scene_info {
+    int64_t num_triangles;
+    int64_t num_nodes;           /* 128-byte 8-wide BVH nodes              */
+    int64_t num_lights;          /* area-light instances                   */
+    int64_t device_bytes;        /* resident HBM held by the scene         */
+    int32_t bvh_depth;           /* deepest node level                     */
+    float build_ms;              /* host BVH build + upload time           */
+    float light_weight_sum;      /* Σ intensity·area, scene.cu:388-391     */
+} srt_scene_info;
+
+/* Scene::build_gscene + OptixRayTracer GAS/IAS build
+ * (src/scene/scene.cu:214-418, src/optix/optix_ray_tracer.cu:213-359):
+ * flattens instances, builds the binned-SAH 8-wide BVH, the light CDFs,
+ * and uploads everything to the current device. */
+srt_status srt_scene_create(const srt_scene_desc* desc, srt_scene** out);
+/* Camera change without rebuilding geometry (camera.h:165-170). */
+srt_status srt_scene_set_camera(srt_scene* scene, const srt_camera_desc* camera);
+srt_status srt_scene_get_info(const srt_scene* scene, srt_scene_info* info);
+/* Maps a global primitive id (instance order, then face order) to
+ * (instance, face): the OptiX pair (instance, optixGetPrimitiveIndex()). */
+srt_status srt_scene_prim_to_instance(const srt_scene* scene, int64_t prim,
+                                      int32_t* instance, int32_t* face);
+void srt_scene_destroy(srt_scene* scene);
+
+/* ------------------------------------------------------------------ */
+/* Ray queries (replace optixTrace of path_tracer.cu:75-78, :124-127)  */
+/* ------------------------------------------------------------------ */
+
+/* rays:  n x 8 floats  (ox, oy, oz, tmin, dx, dy, dz, tmax), device.
+ * hits:  n x 4 floats  (t, u, v, prim as int32 bits; prim = -1 on miss), device.
+ * u, v are the barycentrics of vertex 1 and 2 (optixGetTriangleBarycentrics). */
+srt_status srt_trace_closest(const srt_scene* scene, const float* rays, int64_t n,
+                             float* hits, void* stream);
+/* visible: n int32 (1 = unoccluded in (tmin, tmax), 0 = occluded), device. */
+srt_status srt_trace_shadow(const srt_scene* scene, const float* rays, int64_t n,
+                            int32_t* visible, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Path tracing pass (src/passes/integrator/path_tracer.{h,cu})         */
+/* ------------------------------------------------------------------ */
+
+/* Random-number modes. */
+enum {
+    /* per-pixel curand XORWOW stream curand_init(seed + idx, 0, 0),
+     * u = 1 - curand_uniform (src/device_include/math/random.h:9-31);
+     * one path per pixel in flight, consumption order of path_tracer.cu:50-169 */
+    SRT_RNG_CURAND = 0,
+    /* counter-based hash of (seed, pixel, sample, dimension): stateless, lets
+     * several samples of one pixel be in flight at once */
+    SRT_RNG_HASH = 1
+};
+
+/* Flags for srt_pt_params.flags. */
+enum {
+    /* Light / triangle CDF remap done correctly ((u - cdf[i-1]) / pdf_i).
+     * Default (0) reproduces the reference's `int lower = cdf[idx-1]`
+     * truncation (light.h:65, gmesh.h:49). */
+    SRT_PT_FIXED_CDF_REMAP = 1
+};
+
+/* PathTracer JSON params + frame seed (path_tracer.h:15-19, 30-39;
+ * integrator_params.h:9-24). */
+typedef struct srt_pt_params {
+    int32_t samples_per_pixel;   /* default 1  */
+    int32_t max_depth;           /* default 16 */
+    int32_t rr_depth;            /* default 4  */
+    int32_t use_nee;             /* default 1  */
+    int32_t use_mis;             /* default 1  */
+    int32_t seed;                /* PathTracerParams::seed (path_tracer.cu:15) */
+    int32_t rng_mode;            /* SRT_RNG_*  */
+    int32_t flags;               /* SRT_PT_*   */
+} srt_pt_params;
+
+/* Counters of the last render (exact integers). */
+typedef struct srt_pt_stats {
+    int64_t samples;             /* samples finished = w*h*spp                   */
+    int64_t closest_rays;        /* rays through the closest-hit kernel          */
+    int64_t shadow_rays;         /* rays through the shadow kernel               */
+    int64_t iterations;          /* wavefront iterations (closest+shade+shadow)  */
+    int64_t stack_overflows;     /* traversal stack overflows (must be 0)        */
+    float render_ms;             /* wall time of srt_pt_render (host clock)      */
+    int64_t kernel_launches;     /* kernels this library launched for the frame  */
+    /* Filled only while profiling is on (srt_pt_set_profiling): summed device
+     * time of each kernel of the iteration (closest, shade, shadow, regen,
+     * advance) from CUDA events recorded between them, and the traversal
+     * work: 128-byte nodes visited and triangles tested. */
+    float kernel_ms[5];
+    int64_t closest_nodes, closest_tris, shadow_nodes, shadow_tris;
+} srt_pt_stats;
+
+typedef struct srt_pt srt_pt;
+
+/* PathTracer::init (path_tracer.cu:5-11): allocates the path queues for a
+ * width x height film against `scene`. */
+srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t height, srt_pt** out);
+/* PathTracer::render (path_tracer.cu:13-33): writes film[i] = (L/spp, 1)
+ * for every pixel i = iy*width + ix.  `film` is a device float4[w*h].
+ * Stream-ordered; returns after the frame has been enqueued and its
+ * completion polled (the reference synchronises at the same point). */
+srt_status srt_pt_render(srt_pt* pt, float* film, const srt_pt_params* params, void* stream);
+srt_status srt_pt_get_stats(const srt_pt* pt, srt_pt_stats* stats);
+/* Profiling switch (PROFILE() scopes of src/utils/profiler.h:219 applied per
+ * kernel): when on, the iteration graph carries event records between the
+ * kernels, the host reads them after every graph launch, and the traversal
+ * kernels count their node visits.  Results land in srt_pt_stats. */
+srt_status srt_pt_set_profiling(srt_pt* pt, int32_t enable);
+void srt_pt_destroy(srt_pt* pt);
+
+/* curand tape: out[p * ndraws + k] = k-th draw of the pixel-p stream of
+ * SRT_RNG_CURAND for frame seed `seed` (device float[npix*ndraws]). */
+srt_status srt_rng_tape(int32_t seed, int64_t npix, int32_t ndraws, float* out, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* BxDF batch (src/device_include/scene/gmaterial.h:59-103 over bxdf.h) */
+/* ------------------------------------------------------------------ */
+
+/* One shading point: world-space normal n (Onb(n), onb.h:11-16), outgoing
+ * wo, surface color, material parameters, two uniforms for sample().
+ * SoA device arrays, n points each:
+ *   normal[3n] wo[3n] color[3n] params[12n] (ior, metallic, subsurface, roughness,
+ *   specular, specularTint, anisotropic, sheen, sheenTint, clearcoat,
+ *   clearcoatGloss, specTrans per point) rnd[2n]
+ * Outputs (device): wi[3n], f[3n], pdf[n], delta[n] (int32). */
+typedef struct srt_bxdf_batch {
+    int64_t n;
+    int32_t type;               /* srt_bxdf_type, same for all points */
+    const float* normal;
+    const float* wo;
+    const float* color;
+    const float* params;
+    const float* rnd;
+    float* wi;
+    float* f;
+    float* pdf;
+    int32_t* delta;
+} srt_bxdf_batch;
+
+/* GMaterial::sample (gmaterial.h:74-89) for every point. */
+srt_status srt_bxdf_sample(const srt_bxdf_batch* batch, void* stream);
+/* GMaterial::eval / sample_pdf (gmaterial.h:59-72, 91-103) at the given
+ * wi (read from batch->wi): writes f and pdf. */
+srt_status srt_bxdf_eval(const srt_bxdf_batch* batch, void* stream);
+/* Fills the Disney batch inputs in device memory from PCG32(seed=i, seq=0)
+ * streams, point i in [first, first + n) (draw order: normal 2, wo 2,
+ * color 3, 9 params, roughness 1, rnd 2 of 4). */
+srt_status srt_bxdf_generate(int64_t first, const srt_bxdf_batch* batch, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Film passes (src/passes/postprocess/*.cu, src/utils/metrics.h)       */
+/* ------------------------------------------------------------------ */
+
+/* Accumulate::render (accumulate.cu:10-29): acc = acc*(1-w) + film*w,
+ * w = 1/(frame_count+1); film = acc.  float4[n] device arrays. */
+srt_status srt_film_accumulate(float* film, float* acc, int64_t n, int32_t frame_count, void* stream);
+
+/* ToneMapping::Type, tonemapping.h:10 */
+enum { SRT_TONE_NONE = 0, SRT_TONE_CLAMP = 1, SRT_TONE_REINHARD = 2,
+       SRT_TONE_UNCHARTED2 = 3, SRT_TONE_ACES = 4 };
+/* ToneMapping::render (tonemapping.cu:5-70), in place. */
+srt_status srt_film_tonemap(float* film, int64_t n, int32_t type, float exposure,
+                            int32_t use_gamma, void* stream);
+
+/* Metrics::Type, metrics.h:11 */
+enum { SRT_METRIC_MSE = 0, SRT_METRIC_MAPE = 1, SRT_METRIC_SMAPE = 2, SRT_METRIC_RELMSE = 3 };
+/* Metrics::cal_image / Measure::render (metrics.h:53-70, measure.cu:35-49):
+ * per-pixel error, drop the largest `discard` percent, mean of the rest.
+ * `scratch` is a device buffer of at least srt_film_metric_scratch_bytes(n)
+ * bytes owned by the caller; *out (host) receives the trimmed mean. */
+size_t srt_film_metric_scratch_bytes(int64_t n);
+srt_status srt_film_metric(const float* x, const float* ref, int64_t n, int32_t type,
+                           float discard, void* scratch, float* out, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Procedural scenes (inputs of the Cornell and 5.2M-triangle workloads) */
+/* ------------------------------------------------------------------ */
+
+typedef struct srt_procedural srt_procedural;
+/* name: "cornell" | "spheres".  spheres: n_spheres icospheres of
+ * `subdiv` subdivisions (81,920 faces at 6).  Host-side arrays only. */
+srt_status srt_procedural_create(const char* name, uint64_t seed, int32_t n_spheres,
+                                 int32_t subdiv, srt_procedural** out);
+/* Borrowed view of the generated scene (valid until destroy). */
+srt_status srt_procedural_desc(const srt_procedural* p, srt_scene_desc* desc);
+void srt_procedural_destroy(srt_procedural* p);
+
+/* ------------------------------------------------------------------ */
+/* Render-pass plugin API (src/passes/renderpass.h:10-80)               */
+/* ------------------------------------------------------------------ */
+
+/* JSON config with "render", "passes", "scene" (example/example.json).
+ * Passes registered: PathTracer, Wavefront, Accumulate, ToneMapping.
+ * scene.model: "procedural:cornell" | "procedural:spheres[:n[:subdiv[:seed]]]". */
+typedef struct srt_renderer srt_renderer;
+/* create_renderer + load_scene + load_passes (src/main/main.cu:19-41,
+ * src/renderer/renderer.cu:3-17, 42-174). */
+srt_status srt_renderer_create(const char* json_config, srt_renderer** out);
+/* ImageRenderer::run without the file save (renderer.cu:176-191): runs
+ * every pass once on the film; `frames` repeats it. */
+srt_status srt_renderer_run(srt_renderer* r, int32_t frames);
+srt_status srt_renderer_size(const srt_renderer* r, int32_t* width, int32_t* height);
+/* Copies the film (float4[w*h]) to host memory. */
+srt_status srt_renderer_read_film(const srt_renderer* r, float* host_rgba);
+/* Writes the film as a little-endian PFM (RGB float) to `path`. */
+srt_status srt_renderer_save_pfm(const srt_renderer* r, const char* path);
+void srt_renderer_destroy(srt_renderer* r);
+/* Names of the registered passes, ';'-separated (print_registered_pass). */
+const char* srt_registered_passes(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SRT_H */

@@ -1,0 +1,158 @@
+"""ctypes mirror of include/srt.h (struct layouts and entry points).
+
+The library is loaded from the package directory; a missing library is an
+error (there is no fallback implementation).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsrt_gb300.so")
+
+SRT_OK = 0
+STATUS_NAMES = {
+    0: "SRT_OK", 1: "SRT_ERR_ARG", 2: "SRT_ERR_OOM", 3: "SRT_ERR_CUDA", 4: "SRT_ERR_TIMEOUT",
+    5: "SRT_ERR_BUDGET", 6: "SRT_ERR_STACK", 7: "SRT_ERR_NOT_FOUND", 8: "SRT_ERR_PARSE",
+    9: "SRT_ERR_UNSUPPORTED",
+}
+
+BXDF_DIFFUSE, BXDF_DIFFUSE_TRANSMISSION, BXDF_DIELECTRIC, BXDF_DISNEY = 0, 1, 2, 3
+CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC = 0, 1
+RNG_CURAND, RNG_HASH = 0, 1
+PT_FIXED_CDF_REMAP = 1
+TONE_NONE, TONE_CLAMP, TONE_REINHARD, TONE_UNCHARTED2, TONE_ACES = 0, 1, 2, 3, 4
+METRIC_MSE, METRIC_MAPE, METRIC_SMAPE, METRIC_RELMSE = 0, 1, 2, 3
+
+f32p = C.POINTER(C.c_float)
+u32p = C.POINTER(C.c_uint32)
+i32p = C.POINTER(C.c_int32)
+
+
+class Bxdf(C.Structure):
+    _fields_ = [("type", C.c_int32)] + [(n, C.c_float) for n in (
+        "ior", "metallic", "subsurface", "roughness", "specular", "specularTint", "anisotropic",
+        "sheen", "sheenTint", "clearcoat", "clearcoatGloss", "specTrans")]
+
+
+class Material(C.Structure):
+    _fields_ = [("bxdf", Bxdf), ("base_color", C.c_float * 3), ("emission_color", C.c_float * 3),
+                ("intensity", C.c_float)]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("vertices", f32p), ("indices", u32p), ("normals", f32p), ("num_vertices", C.c_int32),
+                ("num_faces", C.c_int32), ("material_id", C.c_int32)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("mesh_id", C.c_int32), ("transform", C.c_float * 12)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("position", C.c_float * 3), ("target", C.c_float * 3),
+                ("up", C.c_float * 3), ("fov", C.c_float), ("aspect", C.c_float),
+                ("aperture", C.c_float), ("focal", C.c_float)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("meshes", C.POINTER(Mesh)), ("num_meshes", C.c_int32),
+                ("instances", C.POINTER(Instance)), ("num_instances", C.c_int32),
+                ("materials", C.POINTER(Material)), ("num_materials", C.c_int32),
+                ("camera", CameraDesc), ("env_color", C.c_float * 3)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_int64), ("num_nodes", C.c_int64), ("num_lights", C.c_int64),
+                ("device_bytes", C.c_int64), ("bvh_depth", C.c_int32), ("build_ms", C.c_float),
+                ("light_weight_sum", C.c_float)]
+
+
+class PtParams(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "samples_per_pixel", "max_depth", "rr_depth", "use_nee", "use_mis", "seed", "rng_mode", "flags")]
+
+
+class PtStats(C.Structure):
+    _fields_ = [("samples", C.c_int64), ("closest_rays", C.c_int64), ("shadow_rays", C.c_int64),
+                ("iterations", C.c_int64), ("stack_overflows", C.c_int64), ("render_ms", C.c_float),
+                ("kernel_launches", C.c_int64), ("kernel_ms", C.c_float * 5), ("closest_nodes", C.c_int64),
+                ("closest_tris", C.c_int64), ("shadow_nodes", C.c_int64), ("shadow_tris", C.c_int64)]
+
+
+class BxdfBatch(C.Structure):
+    _fields_ = [("n", C.c_int64), ("type", C.c_int32), ("normal", C.c_void_p), ("wo", C.c_void_p),
+                ("color", C.c_void_p), ("params", C.c_void_p), ("rnd", C.c_void_p), ("wi", C.c_void_p),
+                ("f", C.c_void_p), ("pdf", C.c_void_p), ("delta", C.c_void_p)]
+
+
+# (name, restype, argtypes)
+_PROTOS = [
+    ("srt_last_error", C.c_char_p, []),
+    ("srt_version", C.c_char_p, []),
+    ("srt_scene_create", C.c_int, [C.POINTER(SceneDesc), C.POINTER(C.c_void_p)]),
+    ("srt_scene_set_camera", C.c_int, [C.c_void_p, C.POINTER(CameraDesc)]),
+    ("srt_scene_get_info", C.c_int, [C.c_void_p, C.POINTER(SceneInfo)]),
+    ("srt_scene_prim_to_instance", C.c_int, [C.c_void_p, C.c_int64, i32p, i32p]),
+    ("srt_scene_destroy", None, [C.c_void_p]),
+    ("srt_trace_closest", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("srt_trace_shadow", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("srt_pt_create", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("srt_pt_render", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PtParams), C.c_void_p]),
+    ("srt_pt_get_stats", C.c_int, [C.c_void_p, C.POINTER(PtStats)]),
+    ("srt_pt_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
+    ("srt_pt_destroy", None, [C.c_void_p]),
+    ("srt_rng_tape", C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]),
+    ("srt_bxdf_sample", C.c_int, [C.POINTER(BxdfBatch), C.c_void_p]),
+    ("srt_bxdf_eval", C.c_int, [C.POINTER(BxdfBatch), C.c_void_p]),
+    ("srt_bxdf_generate", C.c_int, [C.c_int64, C.POINTER(BxdfBatch), C.c_void_p]),
+    ("srt_film_accumulate", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
+    ("srt_film_tonemap", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_float, C.c_int32, C.c_void_p]),
+    ("srt_film_metric_scratch_bytes", C.c_size_t, [C.c_int64]),
+    ("srt_film_metric", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_float, C.c_void_p,
+                                  f32p, C.c_void_p]),
+    ("srt_procedural_create", C.c_int, [C.c_char_p, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("srt_procedural_desc", C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
+    ("srt_procedural_destroy", None, [C.c_void_p]),
+    ("srt_renderer_create", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("srt_renderer_run", C.c_int, [C.c_void_p, C.c_int32]),
+    ("srt_renderer_size", C.c_int, [C.c_void_p, i32p, i32p]),
+    ("srt_renderer_read_film", C.c_int, [C.c_void_p, f32p]),
+    ("srt_renderer_save_pfm", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("srt_renderer_destroy", None, [C.c_void_p]),
+    ("srt_registered_passes", C.c_char_p, []),
+]
+
+_lib = None
+
+
+class SrtError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def lib():
+    """The loaded library; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: the CUDA library must be built "
+                              "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in _PROTOS:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def declared_symbols():
+    return [p[0] for p in _PROTOS]
+
+
+def check(status: int):
+    if status != SRT_OK:
+        raise SrtError(status, lib().srt_last_error().decode())

@@ -1,0 +1,267 @@
+// trace.cuh — closest-hit and any-hit traversal of the 8-wide quantised BVH
+// (replaces optixTrace with OPTIX_RAY_FLAG_DISABLE_ANYHIT, path_tracer.cu:75-78
+// and :124-127).
+//
+// Traversal keeps one "node group" (child_base, internal-slot mask, hit
+// bits in octant order) in registers and pushes at most one group per
+// visited node onto a short per-thread stack held in shared memory, so the
+// stack depth is bounded by the tree depth (Ylitie, Karras, Laine, HPG 2017).
+// Triangles hit by a node's leaf children are tested right after the node.
+// The triangle test is the watertight test of Woop, Benthin and Wald
+// (JCGT 2013); u, v are the barycentrics of vertex 1 and 2, as
+// optixGetTriangleBarycentrics returns them.
+#pragma once
+
+#include "device_types.h"
+#include "vmath.h"
+
+namespace srt {
+
+constexpr int kStackEntries = 32;
+
+struct Hit {
+    float t, u, v;
+    int32_t tri;  // BVH-order triangle, -1 on miss
+};
+
+struct RayPre {
+    float3 o;
+    float3 idir;
+    int kx, ky, kz;
+    float sx, sy, sz;
+    uint32_t oct;
+};
+
+__device__ __forceinline__ float comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+__device__ __forceinline__ RayPre make_ray(float3 o, float3 d)
+{
+    RayPre r;
+    r.o = o;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    if (ay > ax) kz = 1;
+    if (az > fmaxf(ax, ay)) kz = 2;
+    int kx = (kz == 2) ? 0 : kz + 1;
+    int ky = (kx == 2) ? 0 : kx + 1;
+    float dz = comp(d, kz);
+    if (dz < 0.0f) {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.sx = comp(d, kx) / dz;
+    r.sy = comp(d, ky) / dz;
+    r.sz = 1.0f / dz;
+    const float tiny = 1e-20f;
+    float3 dd = make_float3(fabsf(d.x) < tiny ? copysignf(tiny, d.x) : d.x,
+                            fabsf(d.y) < tiny ? copysignf(tiny, d.y) : d.y,
+                            fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z);
+    r.idir = make_float3(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z);
+    r.oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    return r;
+}
+
+// Watertight ray/triangle test; on a hit in (tmin, tmax) returns t and the
+// barycentrics of v1, v2.
+__device__ __forceinline__ bool hit_triangle(const RayPre& r, float3 v0, float3 v1, float3 v2, float tmin,
+                                             float tmax, float& t, float& b1, float& b2)
+{
+    float3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
+    float az = comp(A, r.kz), bz = comp(B, r.kz), cz = comp(C, r.kz);
+    float Ax = comp(A, r.kx) - r.sx * az, Ay = comp(A, r.ky) - r.sy * az;
+    float Bx = comp(B, r.kx) - r.sx * bz, By = comp(B, r.ky) - r.sy * bz;
+    float Cx = comp(C, r.kx) - r.sx * cz, Cy = comp(C, r.ky) - r.sy * cz;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = U + V + W;
+    if (det == 0.0f) return false;
+    float T = U * (r.sz * az) + V * (r.sz * bz) + W * (r.sz * cz);
+    float inv = 1.0f / det;
+    float tt = T * inv;
+    if (!(tt > tmin && tt < tmax)) return false;
+    t = tt;
+    b1 = V * inv;
+    b2 = W * inv;
+    return true;
+}
+
+__device__ __forceinline__ float u16f(uint32_t w, int hi)
+{
+    uint32_t q = hi ? (w >> 16) : (w & 0xffffu);
+    return __uint_as_float(0x4B000000u | q) - 8388608.0f;
+}
+__device__ __forceinline__ uint32_t word4(uint4 v, int j)
+{
+    return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+// Stack of node groups in shared memory: entry e of thread `lane_id` is at
+// stack[e * stride + lane_id] (stride = threads per block: conflict-free).
+struct Stack {
+    uint2* base;
+    int stride;
+    int sp;
+    __device__ __forceinline__ void push(uint2 g, int& overflow)
+    {
+        if (sp < kStackEntries) {
+            base[sp * stride] = g;
+            ++sp;
+        } else {
+            overflow = 1;
+        }
+    }
+    __device__ __forceinline__ uint2 pop()
+    {
+        --sp;
+        return base[sp * stride];
+    }
+};
+
+// Tests the eight children of node `ni`; returns the internal-child group
+// and the leaf-triangle mask (bit b -> triangle tri_base + b).
+__device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, uint32_t ni, const RayPre& r,
+                                           float tmin, float tmax, uint2& group, uint32_t& tmask,
+                                           uint32_t& tri_base)
+{
+    const uint4* np = reinterpret_cast<const uint4*>(nodes + ni);
+    uint4 w0 = __ldg(np + 0);
+    uint4 w1 = __ldg(np + 1);
+    uint4 qlx = __ldg(np + 2), qly = __ldg(np + 3), qlz = __ldg(np + 4);
+    uint4 qhx = __ldg(np + 5), qhy = __ldg(np + 6), qhz = __ldg(np + 7);
+    int ex = (int)(int8_t)(w0.w & 0xffu);
+    int ey = (int)(int8_t)((w0.w >> 8) & 0xffu);
+    int ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
+    uint32_t imask = w0.w >> 24;
+    float sx = __int_as_float((ex + 127) << 23), sy = __int_as_float((ey + 127) << 23),
+          sz = __int_as_float((ez + 127) << 23);
+    float Ax = sx * r.idir.x, Ay = sy * r.idir.y, Az = sz * r.idir.z;
+    float Bx = (__uint_as_float(w0.x) - r.o.x) * r.idir.x;
+    float By = (__uint_as_float(w0.y) - r.o.y) * r.idir.y;
+    float Bz = (__uint_as_float(w0.z) - r.o.z) * r.idir.z;
+    uint32_t ihits = 0;
+    uint32_t tm = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * (s & 3))) & 0xffu;
+        int j = s >> 1, hi = s & 1;
+        float tx0 = fmaf(u16f(word4(qlx, j), hi), Ax, Bx), tx1 = fmaf(u16f(word4(qhx, j), hi), Ax, Bx);
+        float ty0 = fmaf(u16f(word4(qly, j), hi), Ay, By), ty1 = fmaf(u16f(word4(qhy, j), hi), Ay, By);
+        float tz0 = fmaf(u16f(word4(qlz, j), hi), Az, Bz), tz1 = fmaf(u16f(word4(qhz, j), hi), Az, Bz);
+        float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+        float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+        bool hit = meta != 0u && tn <= tf * 1.00000024f;
+        if (hit) {
+            if (meta & 0x80u) {
+                ihits |= 1u << (s ^ r.oct);
+            } else {
+                tm |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+            }
+        }
+    }
+    group = make_uint2(w1.x, imask | (ihits << 8));
+    tmask = tm;
+    tri_base = w1.y;
+}
+
+__device__ __forceinline__ uint32_t group_next_node(uint2& g, uint32_t oct)
+{
+    uint32_t hits = g.y >> 8;
+    uint32_t k = __ffs(hits) - 1;
+    hits &= hits - 1;
+    uint32_t slot = k ^ oct;
+    uint32_t imask = g.y & 0xffu;
+    uint32_t rank = __popc(imask & ((1u << slot) - 1u));
+    g.y = imask | (hits << 8);
+    return g.x + rank;
+}
+
+// Per-ray work counters (profiling builds of the kernels only).
+struct TraceCount {
+    uint32_t nodes = 0, tris = 0;
+};
+
+// Closest hit in (tmin, tmax).  `stack` is this thread's shared stack.
+template <bool kCount = false>
+__device__ __forceinline__ Hit trace_closest(const SceneView& S, float3 o, float3 d, float tmin, float tmax,
+                                             Stack& st, int& overflow, TraceCount* cnt = nullptr)
+{
+    Hit h;
+    h.t = tmax;
+    h.u = h.v = 0.0f;
+    h.tri = -1;
+    RayPre r = make_ray(o, d);
+    st.sp = 0;
+    uint2 group = make_uint2(0u, 1u | ((1u << r.oct) << 8));  // root = child rank 0 of slot 0
+    for (;;) {
+        if ((group.y >> 8) == 0u) {
+            if (st.sp == 0) break;
+            group = st.pop();
+            continue;
+        }
+        uint32_t ni = group_next_node(group, r.oct);
+        if ((group.y >> 8) != 0u) st.push(group, overflow);
+        uint32_t tmask, tri_base;
+        visit_node(S.nodes, ni, r, tmin, h.t, group, tmask, tri_base);
+        if (kCount) {
+            cnt->nodes += 1;
+            cnt->tris += __popc(tmask);
+        }
+        while (tmask) {
+            uint32_t b = __ffs(tmask) - 1;
+            tmask &= tmask - 1;
+            uint32_t ti = tri_base + b;
+            const float4* tp = S.tris + 3 * (size_t)ti;
+            float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
+            float t, u, v;
+            if (hit_triangle(r, f3(a), f3(bb), f3(c), tmin, h.t, t, u, v)) {
+                h.t = t;
+                h.u = u;
+                h.v = v;
+                h.tri = (int32_t)ti;
+            }
+        }
+    }
+    return h;
+}
+
+// Any hit in (tmin, tmax): true when occluded.
+template <bool kCount = false>
+__device__ __forceinline__ bool trace_any(const SceneView& S, float3 o, float3 d, float tmin, float tmax,
+                                          Stack& st, int& overflow, TraceCount* cnt = nullptr)
+{
+    RayPre r = make_ray(o, d);
+    st.sp = 0;
+    uint2 group = make_uint2(0u, 1u | ((1u << r.oct) << 8));
+    for (;;) {
+        if ((group.y >> 8) == 0u) {
+            if (st.sp == 0) break;
+            group = st.pop();
+            continue;
+        }
+        uint32_t ni = group_next_node(group, r.oct);
+        if ((group.y >> 8) != 0u) st.push(group, overflow);
+        uint32_t tmask, tri_base;
+        visit_node(S.nodes, ni, r, tmin, tmax, group, tmask, tri_base);
+        if (kCount) {
+            cnt->nodes += 1;
+            cnt->tris += __popc(tmask);
+        }
+        while (tmask) {
+            uint32_t b = __ffs(tmask) - 1;
+            tmask &= tmask - 1;
+            const float4* tp = S.tris + 3 * (size_t)(tri_base + b);
+            float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
+            float t, u, v;
+            if (hit_triangle(r, f3(a), f3(bb), f3(c), tmin, tmax, t, u, v)) return true;
+        }
+    }
+    return false;
+}
+
+}  // namespace srt

@@ -1,0 +1,111 @@
+// trace_kernels.cu — batch ray queries against a resident scene
+// (srt_trace_closest / srt_trace_shadow).  Warps fetch 32 rays at a time
+// from a global counter so long rays do not hold a whole block.
+#include "scene.h"
+#include "trace.cuh"
+
+using namespace srt;
+
+namespace {
+
+constexpr int kTraceThreads = 128;
+
+__device__ __forceinline__ int64_t fetch_batch(unsigned long long* counter)
+{
+    unsigned long long base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(counter, 32ull);
+    return (int64_t)__shfl_sync(0xffffffffu, base, 0);
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_trace_closest(SceneView S, const float4* __restrict__ rays,
+                                                                 int64_t n, float4* __restrict__ hits,
+                                                                 unsigned long long* counter, int* overflow_flag)
+{
+    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
+    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
+    int overflow = 0;
+    for (;;) {
+        int64_t base = fetch_batch(counter);
+        if (base >= n) break;
+        int64_t i = base + (threadIdx.x & 31);
+        if (i < n) {
+            float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+            Hit h = trace_closest(S, f3(a), f3(b), a.w, b.w, st, overflow);
+            int32_t prim = h.tri >= 0 ? __ldg(S.tri_prim + h.tri) : -1;
+            hits[i] = make_float4(h.tri >= 0 ? h.t : b.w, h.u, h.v, __int_as_float(prim));
+        }
+    }
+    if (overflow) atomicAdd(overflow_flag, 1);
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(SceneView S, const float4* __restrict__ rays,
+                                                                int64_t n, int32_t* __restrict__ visible,
+                                                                unsigned long long* counter, int* overflow_flag)
+{
+    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
+    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
+    int overflow = 0;
+    for (;;) {
+        int64_t base = fetch_batch(counter);
+        if (base >= n) break;
+        int64_t i = base + (threadIdx.x & 31);
+        if (i < n) {
+            float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+            visible[i] = trace_any(S, f3(a), f3(b), a.w, b.w, st, overflow) ? 0 : 1;
+        }
+    }
+    if (overflow) atomicAdd(overflow_flag, 1);
+}
+
+struct QueryScratch {
+    unsigned long long counter;
+    int overflow;
+    int pad;
+};
+
+srt_status run_query(const srt_scene* s, const float* rays, int64_t n, void* out, bool shadow, void* stream)
+{
+    clear_error();
+    if (!s || (n > 0 && (!rays || !out))) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (n < 0) return set_error(SRT_ERR_ARG, "negative ray count");
+    if (reinterpret_cast<uintptr_t>(rays) % 16 != 0) return set_error(SRT_ERR_ARG, "rays must be 16-byte aligned");
+    if (!shadow && reinterpret_cast<uintptr_t>(out) % 16 != 0)
+        return set_error(SRT_ERR_ARG, "hits must be 16-byte aligned");
+    if (n == 0) return SRT_OK;
+    cudaStream_t st = as_stream(stream);
+    QueryScratch* scratch = nullptr;
+    SRT_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(QueryScratch), st));
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(QueryScratch), st);
+    int blocks = device_sm_count() * 8;
+    if (e == cudaSuccess) {
+        if (shadow)
+            k_trace_shadow<<<blocks, kTraceThreads, 0, st>>>(s->view, reinterpret_cast<const float4*>(rays), n,
+                                                              reinterpret_cast<int32_t*>(out), &scratch->counter,
+                                                              &scratch->overflow);
+        else
+            k_trace_closest<<<blocks, kTraceThreads, 0, st>>>(s->view, reinterpret_cast<const float4*>(rays), n,
+                                                               reinterpret_cast<float4*>(out), &scratch->counter,
+                                                               &scratch->overflow);
+        e = cudaGetLastError();
+    }
+    int overflow = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&overflow, &scratch->overflow, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(scratch, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, shadow ? "srt_trace_shadow" : "srt_trace_closest");
+    if (overflow) return set_error(SRT_ERR_STACK, "traversal stack overflow");
+    return SRT_OK;
+}
+
+}  // namespace
+
+extern "C" srt_status srt_trace_closest(const srt_scene* s, const float* rays, int64_t n, float* hits, void* stream)
+{
+    return run_query(s, rays, n, hits, false, stream);
+}
+
+extern "C" srt_status srt_trace_shadow(const srt_scene* s, const float* rays, int64_t n, int32_t* visible,
+                                       void* stream)
+{
+    return run_query(s, rays, n, visible, true, stream);
+}

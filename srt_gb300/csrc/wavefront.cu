@@ -1,0 +1,899 @@
+// wavefront.cu — kernels and host driver of the streaming wavefront tracer.
+//
+//   k_start    raygen for every pixel of a newly admitted job (SoA queue)
+//   k_closest  closest-hit traversal of the current queue -> hit records
+//   k_shade    miss / emitter-hit MIS / NEE + MIS / BSDF sample / Russian
+//              roulette; survivors compacted into the next queue with one
+//              atomic per warp; NEE rays into the shadow queue
+//   k_shadow   any-hit traversal; unoccluded contributions added to the pixel
+//   k_regen    NaN/Inf sample filter, film accumulation, next-sample raygen
+//   k_advance  one thread: swaps the queue counters, keeps statistics
+//
+// The per-path arithmetic follows the megakernel raygen program
+// src/shader/integrator/path_tracer.cu:50-169 statement by statement.
+#include <curand_kernel.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+
+#include "bxdf.h"
+#include "scene.h"
+#include "trace.cuh"
+#include "wavefront.cuh"
+
+namespace srt {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kTraceThreads = 128;
+constexpr uint32_t kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// RNG: the reference's per-pixel curand XORWOW stream (random.h:14-31).
+// Only the generator words (d, v[5]) are carried; the Box-Muller fields are
+// unused by curand_uniform.
+// ---------------------------------------------------------------------------
+struct Rng {
+    curandStateXORWOW s;
+    __device__ __forceinline__ void load(uint4 a, uint2 b)
+    {
+        s.v[0] = a.x;
+        s.v[1] = a.y;
+        s.v[2] = a.z;
+        s.v[3] = a.w;
+        s.v[4] = b.x;
+        s.d = b.y;
+        s.boxmuller_flag = 0;
+        s.boxmuller_flag_double = 0;
+        s.boxmuller_extra = 0.0f;
+        s.boxmuller_extra_double = 0.0;
+    }
+    __device__ __forceinline__ void store(uint4& a, uint2& b) const
+    {
+        a = make_uint4(s.v[0], s.v[1], s.v[2], s.v[3]);
+        b = make_uint2(s.v[4], s.d);
+    }
+    __device__ __forceinline__ float next() { return 1.0f - curand_uniform(&s); }
+};
+
+__device__ __forceinline__ unsigned long long pixel_seed(int32_t seed, int32_t idx)
+{
+    // `params.seed + idx` is an int sum widened to unsigned long long (path_tracer.cu:56)
+    int32_t si = (int32_t)((uint32_t)seed + (uint32_t)idx);
+    return (unsigned long long)(long long)si;
+}
+
+// ---------------------------------------------------------------------------
+// warp-aggregated queue append: one atomicAdd per warp, lanes get
+// consecutive slots in lane order.  All 32 lanes must call it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t warp_append(int32_t* counter, bool pred)
+{
+    uint32_t m = __ballot_sync(kFull, pred);
+    if (m == 0u) return -1;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    return pred ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+// Camera::get_ray, perspective / orthographic (camera.h:107-122).
+__device__ __forceinline__ void camera_ray(const CameraRec& c, float x, float y, float3& o, float3& d)
+{
+    float px = (x - 0.5f) * c.nw, py = (y - 0.5f) * c.nh;
+    if (c.type == SRT_CAMERA_ORTHOGRAPHIC) {
+        float3 lo = make_float3(px * c.radius, py * c.radius, 1.0f);
+        o = lo.x * c.x + lo.y * c.y + lo.z * c.z + c.pos;
+        d = 0.0f * c.x + 0.0f * c.y + 1.0f * c.z;
+    } else {
+        float3 ld = normalize(make_float3(px, py, 1.0f));
+        o = c.pos;
+        d = ld.x * c.x + ld.y * c.y + ld.z * c.z;
+    }
+}
+
+__device__ __forceinline__ int cdf_search(const float* __restrict__ cdf, int num, float x)
+{
+    int lf = 0, rg = num - 1;
+    while (lf <= rg) {
+        int mid = (lf + rg) >> 1;
+        if (__ldg(cdf + mid) <= x)
+            lf = mid + 1;
+        else
+            rg = mid - 1;
+    }
+    return min(rg + 1, num - 1);
+}
+
+// The reference keeps cdf[idx-1] in an int (light.h:65, gmesh.h:49).
+__device__ __forceinline__ float cdf_remap(const float* __restrict__ cdf, int idx, float u, bool fixed)
+{
+    if (fixed) {
+        float lower = (idx == 0) ? 0.0f : __ldg(cdf + idx - 1);
+        return (u - lower) / (__ldg(cdf + idx) - lower);
+    }
+    int lower = (idx == 0) ? 0 : (int)__ldg(cdf + idx - 1);
+    return (u - (float)lower) / (__ldg(cdf + idx) - (float)lower);
+}
+
+struct LightSample {
+    float3 pos, normal, emission;
+    float pdf;
+};
+
+// Light::sample + GInstance::sample (light.h:61-76, gmesh.h:45-85).
+__device__ __forceinline__ LightSample sample_light(const SceneView& S, float u1, float u2, bool fixed)
+{
+    int li = cdf_search(S.light_cdf, S.num_lights, u1);
+    u1 = cdf_remap(S.light_cdf, li, u1, fixed);
+    LightRec L = S.lights[li];
+    const float* fcdf = S.face_cdf + L.face_begin;
+    int fi = cdf_search(fcdf, L.num_faces, u1);
+    u1 = cdf_remap(fcdf, fi, u1, fixed);
+    float sx = sqrtf(u1);
+    float bu = 1.0f - sx, bv = u2 * sx;  // uniform_sample_triangle (basic.h:139-143)
+    int32_t t = __ldg(S.light_tri + L.face_begin + fi);
+    const float4* tp = S.tris + 3 * (size_t)t;
+    float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+    float3 v0 = f3(a), v1 = f3(b), v2 = f3(c);
+    LightSample ls;
+    ls.pos = v0 * (1.0f - bu - bv) + v1 * bu + v2 * bv;
+    float3 n = normalize(cross(v1 - v0, v2 - v0));
+    int32_t inst = __float_as_int(a.w);
+    InstanceRec ir = S.insts[inst];
+    if (ir.has_normals) {
+        const float4* np = S.normals + 3 * (size_t)t;
+        float3 sn = f3(__ldg(np)) * (1.0f - bu - bv) + f3(__ldg(np + 1)) * bu + f3(__ldg(np + 2)) * bv;
+        if (dot(n, sn) < 0.0f) n = -n;
+    }
+    ls.normal = n;
+    float4 em = __ldg(&S.mats[ir.material].m[4]);
+    ls.emission = f3(em);
+    ls.pdf = L.pdf;
+    return ls;
+}
+
+__device__ __forceinline__ Bxdf unpack_bxdf(const MaterialRec* __restrict__ m, int id, float3& base, float4& em,
+                                            int& mflags)
+{
+    const float4* p = &m[id].m[0];
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
+    em = __ldg(p + 4);
+    base = f3(a);
+    mflags = __float_as_int(a.w);
+    return Bxdf{mflags & 0xff, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+}
+
+constexpr int kMatSpecular = 1 << 8;
+constexpr int kMatTransmissive = 1 << 9;
+constexpr int kMatEmissive = 1 << 10;
+
+__device__ __forceinline__ uint32_t pack_flags(int depth, bool specular, int job)
+{
+    return (uint32_t)depth | (specular ? 0x100u : 0u) | ((uint32_t)job << 16);
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// Seeds job `job`: RandomGenerator(seed + idx, 0), film = (0, 0, 0, 1),
+// sample-0 camera ray (two jitter draws) appended to queue q at *n.
+__global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ jobs, int job, PathQueue q,
+                                                    int32_t* n, int64_t capacity, int32_t* overflow)
+{
+    const JobRec& J = jobs[job];
+    const int npix = J.npix;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < npix; base += stride) {
+        int pix = base + (threadIdx.x & 31);
+        bool valid = pix < npix;
+        float3 o = f3(0.0f), d = f3(0.0f);
+        uint4 ra = make_uint4(0, 0, 0, 0);
+        uint2 rb = make_uint2(0, 0);
+        if (valid) {
+            Rng rng;
+            curand_init(pixel_seed(J.seed, pix), 0ull, 0ull, &rng.s);
+            int ix = pix % J.width, iy = pix / J.width;
+            float xx = ((float)ix + rng.next()) / (float)J.width;
+            float yy = ((float)iy + rng.next()) / (float)J.height;
+            camera_ray(J.cam, xx, yy, o, d);
+            rng.store(ra, rb);
+            J.film[pix] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+            J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            J.spp_done[pix] = 0;
+        }
+        int32_t slot = warp_append(n, valid);
+        if (valid) {
+            if (slot < capacity) {
+                q.o[slot] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
+                q.d[slot] = make_float4(d.x, d.y, d.z, 1.0f);
+                q.beta[slot] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pack_flags(0, true, job)));
+                q.ra[slot] = ra;
+                q.rb[slot] = rb;
+            } else {
+                atomicAdd(overflow, 1);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ int64_t fetch_batch(unsigned long long* counter)
+{
+    unsigned long long b = 0;
+    if ((threadIdx.x & 31) == 0) b = atomicAdd(counter, 32ull);
+    return (int64_t)__shfl_sync(kFull, b, 0);
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(kTraceThreads) k_closest(const JobRec* __restrict__ jobs, PathQueue q,
+                                                           float4* __restrict__ hits, Counters* ctr,
+                                                           int64_t capacity)
+{
+    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
+    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
+    // a counter past the capacity (overflow, reported by the host) never indexes past the queue
+    const int64_t n = min((int64_t)ctr->n_cur, capacity);
+    int overflow = 0;
+    TraceCount cnt;
+    for (;;) {
+        int64_t base = fetch_batch(&ctr->fetch_closest);
+        if (base >= n) break;
+        int64_t i = base + (threadIdx.x & 31);
+        if (i < n) {
+            float4 o = q.o[i], d = q.d[i];
+            int job = (int)(__float_as_uint(q.beta[i].w) >> 16);
+            Hit h = trace_closest<kCount>(jobs[job].scene, f3(o), f3(d), 1e-3f, 1e16f, st, overflow, &cnt);
+            hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+        }
+    }
+    if (overflow) atomicAdd(&ctr->overflow_stack, 1);
+    if (kCount && (cnt.nodes | cnt.tris)) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_nodes), (unsigned long long)cnt.nodes);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_tris), (unsigned long long)cnt.tris);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_shade(const JobRec* __restrict__ jobs, PathQueue q,
+                                                    const float4* __restrict__ hits, PathQueue qn, ShadowQueue sq,
+                                                    int2* __restrict__ done, Counters* ctr, int64_t capacity)
+{
+    const int n = (int)min((int64_t)ctr->n_cur, capacity);
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
+        const int i = base + (threadIdx.x & 31);
+        const bool valid = i < n;
+        bool push_next = false, push_shadow = false, terminate = false;
+        float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
+        float3 sh_o = f3(0.0f), sh_d = f3(0.0f), sh_c = f3(0.0f);
+        float sh_t = 0.0f, pdf_next = 0.0f;
+        uint32_t flags = 0;
+        int pix = 0, job = 0;
+        uint4 ra = make_uint4(0, 0, 0, 0);
+        uint2 rb = make_uint2(0, 0);
+        if (valid) {
+            float4 o4 = q.o[i], d4 = q.d[i], b4 = q.beta[i];
+            float4 h = hits[i];
+            ra = q.ra[i];
+            rb = q.rb[i];
+            flags = __float_as_uint(b4.w);
+            job = (int)(flags >> 16);
+            int depth = (int)(flags & 0xffu);
+            bool specular = (flags & 0x100u) != 0u;
+            pix = __float_as_int(o4.w);
+            ro = f3(o4);
+            rd = f3(d4);
+            beta = f3(b4);
+            const float scatter_pdf = d4.w;
+            const JobRec& J = jobs[job];
+            const SceneView& S = J.scene;
+            const int tri = __float_as_int(h.w);
+            terminate = true;
+            if (tri < 0) {
+                // miss: environment light (path_tracer.cu:81-85)
+                L_add = beta * S.env;
+            } else {
+                const float4* tp = S.tris + 3 * (size_t)tri;
+                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float3 v0 = f3(a), v1 = f3(b), v2 = f3(c);
+                InstanceRec ir = S.insts[__float_as_int(a.w)];
+                float3 base_color;
+                float4 em;
+                int mflags;
+                Bxdf bx = unpack_bxdf(S.mats, ir.material, base_color, em, mflags);
+                // get_hitinfo (hit_info.h:27-64)
+                float u = h.y, v = h.z;
+                float3 pos = v0 * (1.0f - u - v) + v1 * u + v2 * v;
+                float3 ng = normalize(cross(v1 - v0, v2 - v0));
+                float3 sn = ng;
+                if (ir.has_normals) {
+                    const float4* np = S.normals + 3 * (size_t)tri;
+                    sn = normalize(f3(__ldg(np)) * (1.0f - u - v) + f3(__ldg(np + 1)) * u + f3(__ldg(np + 2)) * v);
+                }
+                if (dot(ng, sn) < 0.0f) ng = -ng;
+                if (mflags & kMatEmissive) {
+                    // emitter hit with MIS (path_tracer.cu:88-106)
+                    float cos_i = dot(ng, -rd);
+                    if (cos_i > 1e-4f) {
+                        float mis = 1.0f;
+                        if (J.use_nee && !specular) {
+                            mis = 0.0f;
+                            if (J.use_mis) {
+                                float t2 = dot(pos - ro, pos - ro);
+                                float lpdf = S.lights[ir.light_id].pdf * t2 / cos_i;
+                                mis = scatter_pdf / (lpdf + scatter_pdf);
+                            }
+                        }
+                        L_add = beta * f3(em) * mis;
+                    }
+                } else {
+                    Rng rng;
+                    rng.load(ra, rb);
+                    float3 tan = (fabsf(sn.x) > fabsf(sn.y)) ? make_float3(0.f, 1.f, 0.f) : make_float3(1.f, 0.f, 0.f);
+                    Frame fr = Frame::from_normal_tangent(sn, tan);
+                    if (dot(ng, -rd) < 0.0f) ng = -ng;
+                    const bool transmissive = (mflags & kMatTransmissive) != 0;
+                    const float3 wo = -rd;
+                    // NEE with MIS (path_tracer.cu:113-142)
+                    if (J.use_nee && !(mflags & kMatSpecular)) {
+                        float lu = rng.next();
+                        float lv = rng.next();
+                        LightSample ls = sample_light(S, lu, lv, (J.flags & SRT_PT_FIXED_CDF_REMAP) != 0);
+                        float3 sd = normalize(ls.pos - pos);
+                        float cos_o = dot(ng, sd);
+                        float cos_l = dot(ls.normal, -sd);
+                        float t = length(ls.pos - pos);
+                        if (cos_l > 1e-4f && ls.pdf > 1e-4f && t > 1e-3f && (cos_o > 0.0f || transmissive)) {
+                            float lpdf = ls.pdf * t * t / cos_l;
+                            float mis = 1.0f;
+                            if (J.use_mis) {
+                                float mpdf = material_pdf(bx, fr, sd, wo, base_color);
+                                mis = lpdf / (lpdf + mpdf);
+                            }
+                            float3 fv = material_eval(bx, fr, sd, wo, base_color);
+                            sh_c = beta * fv * fabsf(cos_o) * ls.emission * mis / lpdf;
+                            sh_o = pos;
+                            sh_d = sd;
+                            sh_t = t - 1e-3f;
+                            push_shadow = true;
+                        }
+                    }
+                    // BSDF sample (path_tracer.cu:145-153)
+                    float bu = rng.next();
+                    float bv = rng.next();
+                    BxdfSample ms = material_sample(bx, fr, wo, make_float2(bu, bv), base_color);
+                    if (ms.pdf > 1e-4f && !(dot(ms.wi, ng) < 0.0f && !transmissive)) {
+                        beta *= ms.f / ms.pdf;
+                        if (!ms.delta) beta *= fabsf(dot(ms.wi, ng));
+                        bool alive = true;
+                        // Russian roulette (path_tracer.cu:156-161)
+                        if (depth >= J.rr_depth) {
+                            float p = fmaxf(fmaxf(beta.x, fmaxf(beta.y, beta.z)), 0.05f);
+                            if (rng.next() > p)
+                                alive = false;
+                            else
+                                beta /= p;
+                        }
+                        if (alive && depth + 1 < J.max_depth) {
+                            terminate = false;
+                            push_next = true;
+                            ro = pos;
+                            rd = ms.wi;
+                            pdf_next = ms.pdf;
+                            flags = pack_flags(depth + 1, (mflags & kMatSpecular) != 0, job);
+                        }
+                    }
+                    rng.store(ra, rb);
+                }
+            }
+        }
+        // emitter / miss radiance of this vertex
+        if (valid && (L_add.x != 0.0f || L_add.y != 0.0f || L_add.z != 0.0f || !finite3(L_add))) {
+            float4* lp = jobs[job].lpath + pix;
+            float4 l = *lp;
+            *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, 0.0f);
+        }
+        int32_t slot = warp_append(&ctr->n_next, push_next);
+        if (push_next) {
+            if (slot < capacity) {
+                qn.o[slot] = make_float4(ro.x, ro.y, ro.z, __int_as_float(pix));
+                qn.d[slot] = make_float4(rd.x, rd.y, rd.z, pdf_next);
+                qn.beta[slot] = make_float4(beta.x, beta.y, beta.z, __uint_as_float(flags));
+                qn.ra[slot] = ra;
+                qn.rb[slot] = rb;
+            } else {
+                atomicAdd(&ctr->overflow_queue, 1);
+            }
+        }
+        slot = warp_append(&ctr->n_shadow, push_shadow);
+        if (push_shadow) {
+            if (slot < capacity) {
+                sq.o[slot] = make_float4(sh_o.x, sh_o.y, sh_o.z, __int_as_float(pix));
+                sq.d[slot] = make_float4(sh_d.x, sh_d.y, sh_d.z, sh_t);
+                sq.c[slot] = make_float4(sh_c.x, sh_c.y, sh_c.z, __int_as_float(job));
+            } else {
+                atomicAdd(&ctr->overflow_queue, 1);
+            }
+        }
+        bool fin = valid && terminate;
+        slot = warp_append(&ctr->n_done, fin);
+        if (fin) {
+            JobRec const& J = jobs[job];
+            J.rng_a[pix] = ra;
+            J.rng_b[pix] = rb;
+            if (slot < capacity)
+                done[slot] = make_int2(job, pix);
+            else
+                atomicAdd(&ctr->overflow_queue, 1);
+        }
+    }
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(kTraceThreads) k_shadow(const JobRec* __restrict__ jobs, ShadowQueue sq,
+                                                          Counters* ctr, int64_t capacity)
+{
+    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
+    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
+    const int64_t n = min((int64_t)ctr->n_shadow, capacity);
+    int overflow = 0;
+    TraceCount cnt;
+    for (;;) {
+        int64_t base = fetch_batch(&ctr->fetch_shadow);
+        if (base >= n) break;
+        int64_t i = base + (threadIdx.x & 31);
+        if (i < n) {
+            float4 o = sq.o[i], d = sq.d[i], c = sq.c[i];
+            const JobRec& J = jobs[__float_as_int(c.w)];
+            if (!trace_any<kCount>(J.scene, f3(o), f3(d), 1e-3f, d.w, st, overflow, &cnt)) {
+                // one path per pixel in flight: plain read-modify-write
+                float4* lp = J.lpath + __float_as_int(o.w);
+                float4 l = *lp;
+                *lp = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.0f);
+            }
+        }
+    }
+    if (overflow) atomicAdd(&ctr->overflow_stack, 1);
+    if (kCount && (cnt.nodes | cnt.tris)) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_nodes), (unsigned long long)cnt.nodes);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_tris), (unsigned long long)cnt.tris);
+    }
+}
+
+// Ends the samples of the done pixels (path_tracer.cu:164-165) and starts
+// their next sample (path_tracer.cu:64-68).
+__global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ jobs, const int2* __restrict__ done,
+                                                    PathQueue qn, Counters* ctr, int64_t capacity)
+{
+    const int n = (int)min((int64_t)ctr->n_done, capacity);
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
+        const int i = base + (threadIdx.x & 31);
+        bool again = false;
+        int job = 0, pix = 0;
+        float3 o = f3(0.0f), d = f3(0.0f);
+        uint4 ra = make_uint4(0, 0, 0, 0);
+        uint2 rb = make_uint2(0, 0);
+        if (i < n) {
+            int2 e = done[i];
+            job = e.x;
+            pix = e.y;
+            const JobRec& J = jobs[job];
+            float4 l = J.lpath[pix];
+            if (isfinite(l.x) && isfinite(l.y) && isfinite(l.z)) {
+                float4 f = J.film[pix];
+                float s = (float)J.spp;
+                J.film[pix] = make_float4(f.x + l.x / s, f.y + l.y / s, f.z + l.z / s, 1.0f);
+            }
+            J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            int k = J.spp_done[pix] + 1;
+            J.spp_done[pix] = k;
+            if (k < J.spp) {
+                Rng rng;
+                rng.load(J.rng_a[pix], J.rng_b[pix]);
+                int ix = pix % J.width, iy = pix / J.width;
+                float xx = ((float)ix + rng.next()) / (float)J.width;
+                float yy = ((float)iy + rng.next()) / (float)J.height;
+                camera_ray(J.cam, xx, yy, o, d);
+                rng.store(ra, rb);
+                again = true;
+            } else {
+                atomicAdd(J.pixels_done, 1);
+            }
+        }
+        int32_t slot = warp_append(&ctr->n_next, again);
+        if (again) {
+            if (slot < capacity) {
+                qn.o[slot] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
+                qn.d[slot] = make_float4(d.x, d.y, d.z, 1.0f);
+                qn.beta[slot] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pack_flags(0, true, job)));
+                qn.ra[slot] = ra;
+                qn.rb[slot] = rb;
+            } else {
+                atomicAdd(&ctr->overflow_queue, 1);
+            }
+        }
+    }
+}
+
+__global__ void k_advance(Counters* c)
+{
+    c->closest_total += c->n_cur;
+    c->shadow_total += c->n_shadow;
+    c->iterations += 1;
+    c->started += c->n_done;
+    c->n_cur = c->n_next;
+    c->n_next = 0;
+    c->n_shadow = 0;
+    c->n_done = 0;
+    c->fetch_closest = 0;
+    c->fetch_shadow = 0;
+}
+
+__global__ void k_rng_tape(int32_t seed, int64_t npix, int32_t ndraws, float* out)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    Rng rng;
+    curand_init(pixel_seed(seed, (int32_t)p), 0ull, 0ull, &rng.s);
+    for (int k = 0; k < ndraws; ++k) out[p * ndraws + k] = rng.next();
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Engine (host)
+// ---------------------------------------------------------------------------
+
+Engine::~Engine()
+{
+    if (graph_) cudaGraphExecDestroy(graph_);
+    if (graph_prof_) cudaGraphExecDestroy(graph_prof_);
+    for (auto& a : ev_)
+        for (auto& b : a)
+            for (auto& e : b)
+                if (e) cudaEventDestroy(e);
+    if (graph_stream_) cudaStreamDestroy(graph_stream_);
+    if (host_counters_) cudaFreeHost(host_counters_);
+}
+
+srt_status Engine::init(int64_t capacity, int max_jobs)
+{
+    if (capacity <= 0 || capacity > (int64_t)0x7ffffff0 || max_jobs <= 0 || max_jobs > 65535)
+        return set_error(SRT_ERR_ARG, "engine capacity out of range");
+    capacity_ = capacity;
+    max_jobs_ = max_jobs;
+    const size_t C = (size_t)capacity;
+    size_t per_queue = align_up(C * 16) * 3 + align_up(C * 16) + align_up(C * 8);
+    size_t total = 2 * per_queue + align_up(C * 16) * 3 /*shadow*/ + align_up(C * 16) /*hits*/ +
+                   align_up(C * 8) /*done*/ + align_up(sizeof(Counters)) + align_up(sizeof(JobRec) * max_jobs) +
+                   align_up(4 * (size_t)max_jobs);
+    SRT_TRY(buf_.alloc(total, "wavefront queues"));
+    bytes_ = total;
+    char* p = buf_.as<char>();
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += align_up(bytes);
+        return r;
+    };
+    for (int k = 0; k < 2; ++k) {
+        q_[k].o = (float4*)take(C * 16);
+        q_[k].d = (float4*)take(C * 16);
+        q_[k].beta = (float4*)take(C * 16);
+        q_[k].ra = (uint4*)take(C * 16);
+        q_[k].rb = (uint2*)take(C * 8);
+    }
+    sq_.o = (float4*)take(C * 16);
+    sq_.d = (float4*)take(C * 16);
+    sq_.c = (float4*)take(C * 16);
+    hits_ = (float4*)take(C * 16);
+    done_ = (int2*)take(C * 8);
+    counters_ = (Counters*)take(sizeof(Counters));
+    jobs_ = (JobRec*)take(sizeof(JobRec) * max_jobs);
+    pixels_done_ = (int32_t*)take(4 * (size_t)max_jobs);
+    SRT_CUDA_TRY(cudaMemset(counters_, 0, sizeof(Counters)));
+    SRT_CUDA_TRY(cudaMemset(pixels_done_, 0, 4 * (size_t)max_jobs));
+    SRT_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&host_counters_), sizeof(Counters)));
+    SRT_CUDA_TRY(cudaStreamCreateWithFlags(&graph_stream_, cudaStreamNonBlocking));
+    int sms = device_sm_count();
+    grid_persist_ = sms * 8;  // 128-thread traversal blocks, dynamic ray fetch
+    grid_stride_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kThreads - 1) / kThreads, sms * 8));
+    return SRT_OK;
+}
+
+srt_status Engine::set_job(int job, const JobRec& rec, cudaStream_t st)
+{
+    if (job < 0 || job >= max_jobs_) return set_error(SRT_ERR_ARG, "job slot out of range");
+    SRT_CUDA_TRY(cudaMemcpyAsync(jobs_ + job, &rec, sizeof(JobRec), cudaMemcpyHostToDevice, st));
+    SRT_CUDA_TRY(cudaMemsetAsync(pixels_done_ + job, 0, 4, st));
+    return SRT_OK;
+}
+
+srt_status Engine::start_job(int job, const JobRec& rec, cudaStream_t st)
+{
+    int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((rec.npix + kThreads - 1) / kThreads,
+                                                             (int64_t)device_sm_count() * 16));
+    k_start<<<blocks, kThreads, 0, st>>>(jobs_, job, q_[0], &counters_->n_cur, capacity_,
+                                         &counters_->overflow_queue);
+    times_.launches += 1;
+    SRT_CUDA_TRY(cudaGetLastError());
+    return SRT_OK;
+}
+
+void Engine::launch_iteration(int parity, cudaStream_t st, bool prof)
+{
+    const PathQueue& cur = q_[parity];
+    const PathQueue& nxt = q_[parity ^ 1];
+    auto mark = [&](int k, int e) {
+        if (prof) cudaEventRecord(ev_[parity][k][e], st);
+    };
+    mark(0, 0);
+    if (prof)
+        k_closest<true><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+    else
+        k_closest<false><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+    mark(0, 1);
+    mark(1, 0);
+    k_shade<<<grid_stride_, kThreads, 0, st>>>(jobs_, cur, hits_, nxt, sq_, done_, counters_, capacity_);
+    mark(1, 1);
+    mark(2, 0);
+    if (prof)
+        k_shadow<true><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
+    else
+        k_shadow<false><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
+    mark(2, 1);
+    mark(3, 0);
+    k_regen<<<grid_stride_, kThreads, 0, st>>>(jobs_, done_, nxt, counters_, capacity_);
+    mark(3, 1);
+    mark(4, 0);
+    k_advance<<<1, 1, 0, st>>>(counters_);
+    mark(4, 1);
+}
+
+srt_status Engine::capture(bool prof)
+{
+    if (prof && !ev_[0][0][0]) {
+        for (auto& a : ev_)
+            for (auto& b : a)
+                for (auto& e : b) SRT_CUDA_TRY(cudaEventCreate(&e));
+    }
+    cudaGraph_t g = nullptr;
+    SRT_CUDA_TRY(cudaStreamBeginCapture(graph_stream_, cudaStreamCaptureModeThreadLocal));
+    launch_iteration(0, graph_stream_, prof);
+    launch_iteration(1, graph_stream_, prof);
+    cudaError_t e = cudaStreamEndCapture(graph_stream_, &g);
+    if (e != cudaSuccess) return cuda_error(e, "capture wavefront iteration");
+    cudaGraphExec_t& out = prof ? graph_prof_ : graph_;
+    e = cudaGraphInstantiate(&out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        out = nullptr;
+        return cuda_error(e, "instantiate wavefront graph");
+    }
+    return SRT_OK;
+}
+
+srt_status Engine::reset_counters(cudaStream_t st)
+{
+    SRT_CUDA_TRY(cudaMemsetAsync(counters_, 0, sizeof(Counters), st));
+    return SRT_OK;
+}
+
+srt_status Engine::read_counters(Counters& c, cudaStream_t st)
+{
+    SRT_CUDA_TRY(cudaMemcpyAsync(host_counters_, counters_, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    SRT_CUDA_TRY(cudaStreamSynchronize(st));
+    c = *host_counters_;
+    return SRT_OK;
+}
+
+srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, long long budget_iters)
+{
+    const bool prof = profile_;
+    if (prof && !graph_prof_) SRT_TRY(capture(true));
+    if (!prof && !graph_) SRT_TRY(capture(false));
+    cudaGraphExec_t graph = prof ? graph_prof_ : graph_;
+    cudaEvent_t ev = nullptr;
+    SRT_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    // order the internal stream after the caller's stream
+    cudaError_t e = cudaEventRecord(ev, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(graph_stream_, ev, 0);
+    long long iters = 0;
+    srt_status status = SRT_OK;
+    int per_check = 2;
+    while (e == cudaSuccess) {
+        if (prof) per_check = 1;  // events are re-recorded by every launch: read them each time
+        for (int k = 0; k < per_check && e == cudaSuccess; ++k) {
+            e = cudaGraphLaunch(graph, graph_stream_);
+            iters += 2;
+            times_.launches += 10;
+        }
+        if (e != cudaSuccess) break;
+        e = cudaMemcpyAsync(host_counters_, counters_, sizeof(Counters), cudaMemcpyDeviceToHost, graph_stream_);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(graph_stream_);
+        if (e != cudaSuccess) break;
+        if (prof) {
+            for (int par = 0; par < 2 && e == cudaSuccess; ++par)
+                for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+                    float ms = 0.0f;
+                    e = cudaEventElapsedTime(&ms, ev_[par][k][0], ev_[par][k][1]);
+                    times_.ms[k] += ms;
+                }
+            if (e != cudaSuccess) break;
+        }
+        const Counters& c = *host_counters_;
+        if (c.overflow_queue) {
+            status = set_error(SRT_ERR_ARG, "wavefront queue capacity exceeded");
+            break;
+        }
+        if (c.overflow_stack) {
+            status = set_error(SRT_ERR_STACK, "traversal stack overflow");
+            break;
+        }
+        if (until_idle && c.n_cur == 0) break;
+        if (budget_iters > 0 && iters >= budget_iters) break;
+        if (max_iters > 0 && iters > max_iters) {
+            status = set_error(SRT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+            break;
+        }
+        per_check = std::min(per_check * 2, 16);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev, graph_stream_);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev, 0);
+    cudaEventDestroy(ev);
+    if (e != cudaSuccess) return cuda_error(e, "wavefront run");
+    return status;
+}
+
+}  // namespace srt
+
+// ---------------------------------------------------------------------------
+// srt_pt: the PathTracer pass (src/passes/integrator/path_tracer.{h,cu})
+// ---------------------------------------------------------------------------
+using namespace srt;
+
+struct srt_pt {
+    srt_scene* scene = nullptr;
+    int width = 0, height = 0;
+    Engine engine;
+    DeviceBuffer job_buf;
+    float4* lpath = nullptr;
+    uint4* rng_a = nullptr;
+    uint2* rng_b = nullptr;
+    int32_t* spp_done = nullptr;
+    srt_pt_stats stats{};
+};
+
+extern "C" srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t height, srt_pt** out)
+{
+    clear_error();
+    if (!out) return set_error(SRT_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!scene) return set_error(SRT_ERR_ARG, "scene is NULL");
+    if (width <= 0 || height <= 0 || (int64_t)width * height > (int64_t)1 << 27)
+        return set_error(SRT_ERR_ARG, "film size out of range");
+    srt_pt* p = new (std::nothrow) srt_pt();
+    if (!p) return set_error(SRT_ERR_OOM, "host allocation failed");
+    p->scene = scene;
+    p->width = width;
+    p->height = height;
+    const size_t npix = (size_t)width * height;
+    srt_status st = p->engine.init((int64_t)npix, 1);
+    if (st == SRT_OK) st = p->job_buf.alloc(npix * (16 + 16 + 8 + 4) + 1024, "per-pixel path state");
+    if (st != SRT_OK) {
+        delete p;
+        return st;
+    }
+    char* b = p->job_buf.as<char>();
+    p->lpath = (float4*)b;
+    p->rng_a = (uint4*)(b + npix * 16);
+    p->rng_b = (uint2*)(b + npix * 32);
+    p->spp_done = (int32_t*)(b + npix * 40);
+    *out = p;
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_pt_render(srt_pt* p, float* film, const srt_pt_params* prm, void* stream)
+{
+    clear_error();
+    if (!p || !film || !prm) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (reinterpret_cast<uintptr_t>(film) % 16 != 0) return set_error(SRT_ERR_ARG, "film must be 16-byte aligned");
+    if (prm->samples_per_pixel < 0 || prm->max_depth < 0 || prm->max_depth > 255)
+        return set_error(SRT_ERR_ARG, "samples_per_pixel / max_depth out of range");
+    if (prm->rng_mode != SRT_RNG_CURAND)
+        return set_error(SRT_ERR_UNSUPPORTED, "only SRT_RNG_CURAND is available for srt_pt_render");
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t st = as_stream(stream);
+    const int npix = p->width * p->height;
+    srt_scene* sc = p->scene;
+    if (prm->samples_per_pixel == 0 || prm->max_depth == 0) {
+        // no path segment is traced: every pixel is (0, 0, 0, 1)
+        std::vector<float4> black((size_t)npix, make_float4(0.0f, 0.0f, 0.0f, 1.0f));
+        SRT_CUDA_TRY(cudaMemcpyAsync(film, black.data(), (size_t)npix * 16, cudaMemcpyHostToDevice, st));
+        SRT_CUDA_TRY(cudaStreamSynchronize(st));
+        p->stats = srt_pt_stats{};
+        p->stats.samples = (int64_t)npix * prm->samples_per_pixel;
+        return SRT_OK;
+    }
+    if (prm->use_nee && sc->view.num_lights == 0) {
+        // the reference would index an empty light CDF; NEE without lights adds nothing
+    }
+    JobRec J{};
+    J.scene = sc->view;
+    J.cam = sc->camera;
+    J.film = reinterpret_cast<float4*>(film);
+    J.lpath = p->lpath;
+    J.rng_a = p->rng_a;
+    J.rng_b = p->rng_b;
+    J.spp_done = p->spp_done;
+    J.pixels_done = p->engine.pixels_done_slot(0);
+    J.width = p->width;
+    J.height = p->height;
+    J.npix = npix;
+    J.spp = prm->samples_per_pixel;
+    J.max_depth = prm->max_depth;
+    J.rr_depth = prm->rr_depth;
+    J.use_nee = (prm->use_nee && sc->view.num_lights > 0) ? 1 : 0;
+    J.use_mis = prm->use_mis ? 1 : 0;
+    J.seed = prm->seed;
+    J.flags = prm->flags;
+    J.rng_mode = prm->rng_mode;
+    p->engine.times() = KernelTimes();
+    SRT_TRY(p->engine.reset_counters(st));
+    SRT_TRY(p->engine.set_job(0, J, st));
+    SRT_TRY(p->engine.start_job(0, J, st));
+    long long bound = (long long)prm->samples_per_pixel * (prm->max_depth + 1) + 16;
+    SRT_TRY(p->engine.run(st, 2 * bound, true, 0));
+    Counters c;
+    SRT_TRY(p->engine.read_counters(c, st));
+    auto t1 = std::chrono::steady_clock::now();
+    p->stats.samples = c.started;
+    p->stats.closest_rays = c.closest_total;
+    p->stats.shadow_rays = c.shadow_total;
+    p->stats.iterations = c.iterations;
+    p->stats.stack_overflows = c.overflow_stack;
+    p->stats.render_ms = (float)std::chrono::duration<double, std::milli>(t1 - t0).count();
+    const KernelTimes& kt = p->engine.times();
+    p->stats.kernel_launches = kt.launches;
+    for (int k = 0; k < 5; ++k) p->stats.kernel_ms[k] = (float)kt.ms[k];
+    p->stats.closest_nodes = c.c_nodes;
+    p->stats.closest_tris = c.c_tris;
+    p->stats.shadow_nodes = c.s_nodes;
+    p->stats.shadow_tris = c.s_tris;
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_pt_set_profiling(srt_pt* p, int32_t enable)
+{
+    clear_error();
+    if (!p) return set_error(SRT_ERR_ARG, "NULL argument");
+    p->engine.set_profiling(enable != 0);
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_pt_get_stats(const srt_pt* p, srt_pt_stats* s)
+{
+    clear_error();
+    if (!p || !s) return set_error(SRT_ERR_ARG, "NULL argument");
+    *s = p->stats;
+    return SRT_OK;
+}
+
+extern "C" void srt_pt_destroy(srt_pt* p) { delete p; }
+
+extern "C" srt_status srt_rng_tape(int32_t seed, int64_t npix, int32_t ndraws, float* out, void* stream)
+{
+    clear_error();
+    if (npix < 0 || ndraws < 0 || (npix > 0 && ndraws > 0 && !out)) return set_error(SRT_ERR_ARG, "bad arguments");
+    if (npix == 0 || ndraws == 0) return SRT_OK;
+    int blocks = (int)((npix + 255) / 256);
+    k_rng_tape<<<blocks, 256, 0, as_stream(stream)>>>(seed, npix, ndraws, out);
+    SRT_CUDA_TRY(cudaGetLastError());
+    return SRT_OK;
+}

@@ -1,0 +1,109 @@
+// wavefront.cuh — the streaming wavefront path tracer shared by the
+// PathTracer pass (srt_pt_*) and the render-serving loop.
+//
+// One iteration = closest-hit kernel -> shade kernel -> shadow kernel ->
+// regenerate kernel -> advance.  Paths of any number of jobs (scenes,
+// resolutions, spp) share the queues; each path carries its job id.  In
+// SRT_RNG_CURAND mode a pixel has at most one path in flight and its curand
+// stream continues across its samples exactly as the megakernel's per-pixel
+// loop (src/shader/integrator/path_tracer.cu:56-166) consumes it; a pixel
+// whose path ends gets its next sample's camera ray in the same iteration.
+#pragma once
+
+#include <vector>
+
+#include "common.h"
+#include "device_types.h"
+
+namespace srt {
+
+// Per-job record read by every kernel (one per admitted render).
+struct JobRec {
+    SceneView scene;
+    CameraRec cam;
+    float4* film;        // caller film, float4[w*h], row-major idx = iy*w + ix
+    float4* lpath;       // per-pixel radiance of the sample in flight
+    uint4* rng_a;        // per-pixel XORWOW state v[0..3]
+    uint2* rng_b;        // per-pixel XORWOW state (v[4], d)
+    int32_t* spp_done;   // per-pixel finished samples
+    int32_t* pixels_done;  // pixels that finished every sample (one int)
+    int32_t width, height, npix;
+    int32_t spp, max_depth, rr_depth, use_nee, use_mis, seed, flags, rng_mode;
+};
+
+struct PathQueue {
+    float4* o;     // origin, pixel (int bits)
+    float4* d;     // direction, scatter pdf
+    float4* beta;  // throughput, flags: depth bits 0-7, specular bit 8, job bits 16-31
+    uint4* ra;     // rng state
+    uint2* rb;
+};
+
+struct ShadowQueue {
+    float4* o;  // origin, pixel (int bits)
+    float4* d;  // direction, tmax
+    float4* c;  // contribution, job (int bits)
+};
+
+struct Counters {
+    int32_t n_cur, n_next, n_shadow, n_done;
+    unsigned long long fetch_closest, fetch_shadow;
+    long long closest_total, shadow_total, iterations, started;
+    long long c_nodes, c_tris, s_nodes, s_tris;  // traversal work (profiling kernels)
+    int32_t overflow_stack, overflow_queue;
+};
+
+// Per-kernel device time gathered in profiling mode.
+struct KernelTimes {
+    double ms[5] = {0, 0, 0, 0, 0};  // closest, shade, shadow, regen, advance
+    long long launches = 0;          // every kernel the engine launched
+};
+
+// Device state of one wavefront engine (queues sized for `capacity` paths).
+class Engine {
+public:
+    ~Engine();
+    srt_status init(int64_t capacity, int max_jobs);
+    int64_t capacity() const { return capacity_; }
+    size_t device_bytes() const { return bytes_; }
+
+    // Uploads a job record to slot `job` (stream-ordered).
+    srt_status set_job(int job, const JobRec& rec, cudaStream_t st);
+    // Seeds every pixel of `job`: film cleared, rng initialised, sample-0
+    // camera rays appended to the current queue.
+    srt_status start_job(int job, const JobRec& rec, cudaStream_t st);
+    // Runs graph-captured iteration pairs until no path is in flight,
+    // or (when `budget_iters` > 0) at most that many iterations.
+    srt_status run(cudaStream_t st, long long max_iters, bool until_idle, long long budget_iters);
+    srt_status reset_counters(cudaStream_t st);
+    srt_status read_counters(Counters& c, cudaStream_t st);
+    int32_t* pixels_done_slot(int job) const { return pixels_done_ + job; }
+    void set_profiling(bool on) { profile_ = on; }
+    bool profiling() const { return profile_; }
+    KernelTimes& times() { return times_; }
+
+private:
+    srt_status capture(bool profile);
+    void launch_iteration(int parity, cudaStream_t st, bool profile);
+
+    int64_t capacity_ = 0;
+    int max_jobs_ = 0;
+    size_t bytes_ = 0;
+    DeviceBuffer buf_;
+    PathQueue q_[2]{};
+    ShadowQueue sq_{};
+    float4* hits_ = nullptr;
+    int2* done_ = nullptr;
+    Counters* counters_ = nullptr;
+    JobRec* jobs_ = nullptr;
+    int32_t* pixels_done_ = nullptr;
+    Counters* host_counters_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr, graph_prof_ = nullptr;
+    cudaStream_t graph_stream_ = nullptr;
+    cudaEvent_t ev_[2][5][2] = {};
+    bool profile_ = false;
+    KernelTimes times_;
+    int grid_persist_ = 0, grid_stride_ = 0;
+};
+
+}  // namespace srt

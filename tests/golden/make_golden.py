@@ -1,0 +1,162 @@
+"""Writes the golden vectors that pin the CPU oracle to the reference.
+
+Run in a container that has the reference tree (it builds
+oracle/_ref/libsrtref.so from the reference's own device headers):
+
+    python tests/golden/make_golden.py
+
+Outputs (committed): tests/golden/bxdf.npz, camera.npz, scene.npz (the
+Cornell scene arrays plus light samples, hit attributes and a small
+render, all produced by the reference's classes compiled for the host).
+The Cornell scene arrays come from the library's procedural generator.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from srt_gb300 import _capi  # noqa: E402
+from srt_gb300.build import build_reference  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def _np(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def ref_sample(type_, normal, wo, color, params, rnd2):
+    R = O.ref()
+    n = len(normal)
+    wi = np.zeros((n, 3), np.float32)
+    f = np.zeros((n, 3), np.float32)
+    pdf = np.zeros(n, np.float32)
+    delta = np.zeros(n, np.int32)
+    R.ref_bxdf_sample(type_, n, _np(normal), _np(wo), _np(color), _np(params), _np(np.ascontiguousarray(rnd2)),
+                      _np(wi), _np(f), _np(pdf), _np(delta))
+    return wi, f, pdf, delta
+
+
+def ref_eval(type_, normal, wo, color, params, wi):
+    R = O.ref()
+    n = len(normal)
+    f = np.zeros((n, 3), np.float32)
+    pdf = np.zeros(n, np.float32)
+    R.ref_bxdf_eval_pdf(type_, n, _np(normal), _np(wo), _np(color), _np(params), _np(np.ascontiguousarray(wi)),
+                        _np(f), _np(pdf))
+    return f, pdf
+
+
+def bxdf_sets(n=4096):
+    normal, wo, color, params, rnd4 = O.bxdf_inputs(0, n)
+    rng = np.random.default_rng(7)
+    sets = {}
+    sets["disney"] = (_capi.BXDF_DISNEY, params)
+    p2 = params.copy()
+    p2[:, 11] = rng.random(n, dtype=np.float32)          # specTrans: refraction lobe
+    sets["disney_trans"] = (_capi.BXDF_DISNEY, p2)
+    sets["diffuse"] = (_capi.BXDF_DIFFUSE, params)
+    sets["diffuse_transmission"] = (_capi.BXDF_DIFFUSE_TRANSMISSION, params)
+    sets["dielectric"] = (_capi.BXDF_DIELECTRIC, params)
+    out = {"normal": normal, "wo": wo, "color": color, "rnd4": rnd4}
+    # independent directions for eval/pdf (both hemispheres)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    out["wi_rand"] = d
+    for name, (t, p) in sets.items():
+        p = np.ascontiguousarray(p, np.float32)
+        wi, f, pdf, delta = ref_sample(t, normal, wo, color, p, rnd4[:, :2].copy())
+        fe, pe = ref_eval(t, normal, wo, color, p, d)
+        out[f"{name}_type"] = np.int32(t)
+        out[f"{name}_params"] = p
+        out[f"{name}_wi"], out[f"{name}_f"], out[f"{name}_pdf"], out[f"{name}_delta"] = wi, f, pdf, delta
+        out[f"{name}_eval_f"], out[f"{name}_eval_pdf"] = fe, pe
+    np.savez_compressed(os.path.join(OUT, "bxdf.npz"), **out)
+
+
+def camera_set():
+    out = {}
+    rng = np.random.default_rng(11)
+    xy = rng.random((512, 2), dtype=np.float32)
+    for name, typ, aspect, fov in (("persp", 0, 1.0, 40.0), ("persp_wide", 0, 16 / 9, 60.0), ("ortho", 1, 1.5, 40.0)):
+        cam = _capi.CameraDesc()
+        cam.type = typ
+        cam.position[:] = [0.3, 0.2, 3.5]
+        cam.target[:] = [0.0, -0.1, 0.0]
+        cam.up[:] = [0.0, 1.0, 0.0]
+        cam.fov, cam.aspect, cam.focal = fov, aspect, 1.0
+        rays = np.zeros((512, 8), np.float32)
+        O.ref().ref_camera_rays(C.cast(C.pointer(cam), C.c_void_p), 512, _np(xy), _np(rays))
+        out[f"{name}_cam"] = np.array([typ, fov, aspect, 0.3, 0.2, 3.5, 0.0, -0.1, 0.0], np.float32)
+        out[f"{name}_rays"] = rays
+    out["xy"] = xy
+    np.savez_compressed(os.path.join(OUT, "camera.npz"), **out)
+
+
+def scene_arrays_to_npz(s):
+    out = {}
+    out["num_meshes"] = np.int32(len(s.meshes))
+    for i, m in enumerate(s.meshes):
+        out[f"mesh{i}_v"] = m["vertices"].astype(np.float32)
+        out[f"mesh{i}_f"] = m["indices"].astype(np.uint32)
+        out[f"mesh{i}_mat"] = np.int32(m["material"])
+    out["inst_mesh"] = np.array([i for i, _ in s.instances], np.int32)
+    out["inst_xf"] = np.array([x for _, x in s.instances], np.float32)
+    out["materials"] = np.frombuffer(b"".join(bytes(m) for m in s.materials), np.uint8)
+    out["camera"] = np.frombuffer(bytes(s.camera), np.uint8)
+    out["env"] = np.array(s.env, np.float32)
+    return out
+
+
+def scene_set():
+    import srt_gb300 as S
+    s = S.procedural("cornell")
+    desc = s.desc()
+    R = O.ref()
+    h = R.ref_scene_create(C.cast(C.pointer(desc), C.c_void_p))
+    out = scene_arrays_to_npz(s)
+    rng = np.random.default_rng(5)
+    u2 = rng.random((2048, 2), dtype=np.float32)
+    ls = np.zeros((2048, 10), np.float32)
+    R.ref_light_sample(h, 2048, _np(u2), _np(ls))
+    out["light_u2"], out["light_ref"] = u2, ls
+    ntri = sum(len(m["indices"]) for m in s.meshes)
+    prim = rng.integers(0, ntri, 1024).astype(np.int32)
+    uv = rng.random((1024, 2), dtype=np.float32)
+    uv = np.where(uv.sum(1, keepdims=True) > 1, 1 - uv, uv).astype(np.float32)
+    hi = np.zeros((1024, 15), np.float32)
+    R.ref_hitinfo(h, 1024, _np(prim), _np(np.ascontiguousarray(uv)), _np(hi))
+    out["hit_prim"], out["hit_uv"], out["hit_ref"] = prim, uv, hi
+    # small renders through the reference's classes (curand streams, brute force hits)
+    for tag, (w, hh, spp, md, rr, nee, mis, seed) in {
+        "r0": (16, 16, 8, 8, 3, 1, 1, 1234),
+        "r1": (12, 10, 4, 6, 2, 1, 0, 99),
+        "r2": (10, 12, 4, 5, 3, 0, 0, 2024),
+    }.items():
+        film = np.zeros((w * hh, 4), np.float32)
+        s.camera.aspect = w / hh
+        desc = s.desc()
+        R.ref_scene_destroy(h)
+        h = R.ref_scene_create(C.cast(C.pointer(desc), C.c_void_p))
+        R.ref_render(h, w, hh, 0, 0, w, hh, spp, md, rr, nee, mis, seed, _np(film))
+        out[f"{tag}_cfg"] = np.array([w, hh, spp, md, rr, nee, mis, seed], np.int32)
+        out[f"{tag}_film"] = film
+    R.ref_scene_destroy(h)
+    np.savez_compressed(os.path.join(OUT, "scene.npz"), **out)
+
+
+if __name__ == "__main__":
+    if build_reference() is None:
+        sys.exit("the reference tree is needed to write golden vectors")
+    O.build()
+    bxdf_sets()
+    camera_set()
+    scene_set()
+    print("golden vectors written to", OUT)
