@@ -298,6 +298,60 @@ srt_status srt_film_metric(const float* x, const float* ref, int64_t n, int32_t 
                            float discard, void* scratch, float* out, void* stream);
 
 /* ------------------------------------------------------------------ */
+/* Render serving: continuous batching over one wavefront engine        */
+/* ------------------------------------------------------------------ */
+
+/* The reference renders one scene per process, one pass after another
+ * (InteractiveRenderer::run, src/renderer/renderer.cu:199-228); the server
+ * keeps scenes, path queues and per-job state resident and packs the rays
+ * of every admitted job into shared wavefront queues. */
+typedef struct srt_server srt_server;
+
+typedef struct srt_server_config {
+    int64_t hbm_budget_bytes;     /* admission budget: engine + job state + films + scenes in use */
+    int64_t max_paths;            /* paths in flight across jobs (one per pixel of each running job) */
+    int32_t max_jobs;             /* concurrent job slots (<= 65535)                       */
+    int32_t iterations_per_step;  /* wavefront iterations run by one srt_server_step (even) */
+} srt_server_config;
+
+typedef struct srt_job_desc {
+    srt_scene* scene;             /* resident scene, owned by the caller                   */
+    int32_t width, height;
+    srt_pt_params params;         /* same meaning as for srt_pt_render                      */
+    float* film;                  /* caller's device float4[w*h], or NULL: server-owned     */
+} srt_job_desc;
+
+enum { SRT_JOB_QUEUED = 0, SRT_JOB_RUNNING = 1, SRT_JOB_DONE = 2, SRT_JOB_FAILED = 3 };
+
+typedef struct srt_job_info {
+    int32_t state;                /* SRT_JOB_*                                              */
+    int32_t frames_done;          /* progressive frames completed (every pixel has k samples) */
+    double submit_s, admit_s, first_frame_s, done_s;  /* server clock, seconds              */
+    int64_t device_bytes;         /* admitted HBM footprint of the job                      */
+} srt_job_info;
+
+srt_status srt_server_create(const srt_server_config* config, srt_server** out);
+/* Queues a job (admitted by srt_server_step when a slot, paths and the HBM
+ * budget allow).  A job that could never fit returns SRT_ERR_BUDGET. */
+srt_status srt_server_submit(srt_server* s, const srt_job_desc* job, int64_t* job_id);
+/* Admits queued jobs, runs iterations_per_step wavefront iterations over
+ * all running jobs, retires finished jobs and records frame times. */
+srt_status srt_server_step(srt_server* s, int32_t* running, int32_t* queued);
+/* Steps until no job is queued or running, or `timeout_s` passes
+ * (SRT_ERR_TIMEOUT). */
+srt_status srt_server_drain(srt_server* s, double timeout_s);
+srt_status srt_server_job_info(const srt_server* s, int64_t job_id, srt_job_info* info);
+/* Completion time (server clock) of each progressive frame; n = frames_done. */
+srt_status srt_server_frame_times(const srt_server* s, int64_t job_id, double* times, int32_t max, int32_t* n);
+/* Device film of a job (the caller's, or the server-owned one). */
+srt_status srt_server_film(const srt_server* s, int64_t job_id, float** film);
+/* Frees a finished job's server-owned film and forgets the job. */
+srt_status srt_server_release(srt_server* s, int64_t job_id);
+/* Server clock now, seconds. */
+double srt_server_now(const srt_server* s);
+void srt_server_destroy(srt_server* s);
+
+/* ------------------------------------------------------------------ */
 /* Procedural scenes (inputs of the Cornell and 5.2M-triangle workloads) */
 /* ------------------------------------------------------------------ */
 

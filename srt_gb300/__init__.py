@@ -271,3 +271,59 @@ class Renderer:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Render serving loop (srt_server_*): jobs share one wavefront engine."""
+
+    def __init__(self, hbm_budget_bytes=150 << 30, max_paths=1 << 23, max_jobs=64, iterations_per_step=8):
+        cfg = _capi.ServerConfig(hbm_budget_bytes, max_paths, max_jobs, iterations_per_step)
+        self.handle = C.c_void_p()
+        check(lib().srt_server_create(C.byref(cfg), C.byref(self.handle)))
+
+    def submit(self, scene: Scene, width, height, params, film=None):
+        d = _capi.JobDesc(scene.handle, width, height, params, None if film is None else film.data_ptr())
+        jid = C.c_int64()
+        check(lib().srt_server_submit(self.handle, C.byref(d), C.byref(jid)))
+        return jid.value
+
+    def step(self):
+        r, q = C.c_int32(), C.c_int32()
+        check(lib().srt_server_step(self.handle, C.byref(r), C.byref(q)))
+        return r.value, q.value
+
+    def drain(self, timeout_s=600.0):
+        check(lib().srt_server_drain(self.handle, timeout_s))
+
+    def info(self, jid):
+        i = _capi.JobInfo()
+        check(lib().srt_server_job_info(self.handle, jid, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in _capi.JobInfo._fields_}
+
+    def frame_times(self, jid, max_frames=4096):
+        buf = (C.c_double * max_frames)()
+        n = C.c_int32()
+        check(lib().srt_server_frame_times(self.handle, jid, buf, max_frames, C.byref(n)))
+        return list(buf[: min(n.value, max_frames)])
+
+    def film_ptr(self, jid):
+        p = C.c_void_p()
+        check(lib().srt_server_film(self.handle, jid, C.byref(p)))
+        return p.value
+
+    def release(self, jid):
+        check(lib().srt_server_release(self.handle, jid))
+
+    def now(self):
+        return lib().srt_server_now(self.handle)
+
+    def close(self):
+        if self.handle:
+            lib().srt_server_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -81,6 +81,25 @@ class PtStats(C.Structure):
                 ("closest_tris", C.c_int64), ("shadow_nodes", C.c_int64), ("shadow_tris", C.c_int64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_paths", C.c_int64), ("max_jobs", C.c_int32),
+                ("iterations_per_step", C.c_int32)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("params", PtParams),
+                ("film", C.c_void_p)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("frames_done", C.c_int32), ("submit_s", C.c_double),
+                ("admit_s", C.c_double), ("first_frame_s", C.c_double), ("done_s", C.c_double),
+                ("device_bytes", C.c_int64)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+
+
 class BxdfBatch(C.Structure):
     _fields_ = [("n", C.c_int64), ("type", C.c_int32), ("normal", C.c_void_p), ("wo", C.c_void_p),
                 ("color", C.c_void_p), ("params", C.c_void_p), ("rnd", C.c_void_p), ("wi", C.c_void_p),
@@ -112,6 +131,16 @@ _PROTOS = [
     ("srt_film_metric_scratch_bytes", C.c_size_t, [C.c_int64]),
     ("srt_film_metric", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_float, C.c_void_p,
                                   f32p, C.c_void_p]),
+    ("srt_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    ("srt_server_submit", C.c_int, [C.c_void_p, C.POINTER(JobDesc), C.POINTER(C.c_int64)]),
+    ("srt_server_step", C.c_int, [C.c_void_p, i32p, i32p]),
+    ("srt_server_drain", C.c_int, [C.c_void_p, C.c_double]),
+    ("srt_server_job_info", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(JobInfo)]),
+    ("srt_server_frame_times", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_int32, i32p]),
+    ("srt_server_film", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
+    ("srt_server_release", C.c_int, [C.c_void_p, C.c_int64]),
+    ("srt_server_now", C.c_double, [C.c_void_p]),
+    ("srt_server_destroy", None, [C.c_void_p]),
     ("srt_procedural_create", C.c_int, [C.c_char_p, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     ("srt_procedural_desc", C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
     ("srt_procedural_destroy", None, [C.c_void_p]),

@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -15,12 +16,15 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-OBJ = os.path.join(HERE, "_build")
+OBJ = os.path.join(HERE, "_build", platform.machine())
 LIB = os.path.join(HERE, "libsrt_gb300.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
+# -fmad=false: no implicit multiply-add contraction, so the device evaluates
+# the reference formulas with the same roundings as the FP32 oracle (explicit
+# fmaf calls in the BVH slab tests stay fused)
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 # host translation units: -ffp-contract=off keeps host float math identical
 # on x86-64 and aarch64 (scene flattening, CDFs, camera set-up)
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", os.path.join(CUDA, "include")]
@@ -59,8 +63,23 @@ def _compile(src, hdr_mtime, log):
     return obj, None
 
 
+_ELF_MACHINE = {"x86_64": 62, "aarch64": 183}
+
+
+def drop_foreign(path: str) -> None:
+    """Removes a shared object built for another CPU architecture."""
+    want = _ELF_MACHINE.get(platform.machine())
+    if want is None or not os.path.exists(path):
+        return
+    with open(path, "rb") as f:
+        head = f.read(20)
+    if len(head) == 20 and head[:4] == b"\x7fELF" and int.from_bytes(head[18:20], "little") != want:
+        os.remove(path)
+
+
 def build_library(verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
+    drop_foreign(LIB)
     hdr = _headers_mtime()
     srcs = _sources()
     log: list[str] = []
@@ -85,6 +104,8 @@ def build_library(verbose: bool = False) -> str:
 def build_oracle() -> str:
     """CPU oracle (test infrastructure): oracle/liboracle.so."""
     d = os.path.join(ROOT, "oracle")
+    for name in ("liboracle.so", "srt_oracle.o", "curand_host.o"):
+        drop_foreign(os.path.join(d, name))
     r = subprocess.run(["make", "-s", "-C", d], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")

@@ -2,7 +2,7 @@
 //
 // Semantics follow the reference's vector helpers where results must match:
 // lerp(a, b, t) = a + t * (b - a), clamp(f, lo, hi) = max(lo, min(f, hi)),
-// normalize(v) = v * rsqrt(dot(v, v)).
+// normalize(v) = v * (1 / sqrt(dot(v, v))).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -42,14 +42,8 @@ SRT_HD float3 cross(float3 a, float3 b)
 {
     return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-SRT_HD float rsqrt_(float x)
-{
-#if defined(__CUDA_ARCH__)
-    return rsqrtf(x);
-#else
-    return 1.0f / sqrtf(x);
-#endif
-}
+// correctly rounded 1/sqrt(x) (IEEE sqrt and division on host and device)
+SRT_HD float rsqrt_(float x) { return 1.0f / sqrtf(x); }
 SRT_HD float3 normalize(float3 v) { return v * rsqrt_(dot(v, v)); }
 SRT_HD float length(float3 v) { return sqrtf(dot(v, v)); }
 SRT_HD float lerp(float a, float b, float t) { return a + t * (b - a); }

@@ -15,7 +15,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 
 #include "bxdf.h"
 #include "scene.h"
@@ -492,6 +494,7 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
             J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             int k = J.spp_done[pix] + 1;
             J.spp_done[pix] = k;
+            if (J.frame_done) atomicAdd(J.frame_done + (k - 1), 1);
             if (k < J.spp) {
                 Rng rng;
                 rng.load(J.rng_a[pix], J.rng_b[pix]);
@@ -630,8 +633,10 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof)
 {
     const PathQueue& cur = q_[parity];
     const PathQueue& nxt = q_[parity ^ 1];
+    // inside stream capture a plain event record only orders streams; the
+    // External flag makes it a real timestamp node of the graph
     auto mark = [&](int k, int e) {
-        if (prof) cudaEventRecord(ev_[parity][k][e], st);
+        if (prof) cudaEventRecordWithFlags(ev_[parity][k][e], st, cudaEventRecordExternal);
     };
     mark(0, 0);
     if (prof)
@@ -696,29 +701,51 @@ srt_status Engine::read_counters(Counters& c, cudaStream_t st)
 srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, long long budget_iters)
 {
     const bool prof = profile_;
-    if (prof && !graph_prof_) SRT_TRY(capture(true));
-    if (!prof && !graph_) SRT_TRY(capture(false));
+    // SRT_NO_GRAPH=1 launches the iteration kernels directly (diagnostics)
+    static const bool no_graph = [] {
+        const char* v = std::getenv("SRT_NO_GRAPH");
+        return v && v[0] == '1';
+    }();
+    if (!no_graph && prof && !graph_prof_) SRT_TRY(capture(true));
+    if (!no_graph && !prof && !graph_) SRT_TRY(capture(false));
     cudaGraphExec_t graph = prof ? graph_prof_ : graph_;
     cudaEvent_t ev = nullptr;
     SRT_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    const char* what = "record caller-stream event";
     // order the internal stream after the caller's stream
     cudaError_t e = cudaEventRecord(ev, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(graph_stream_, ev, 0);
+    if (e == cudaSuccess) {
+        what = "wait on caller-stream event";
+        e = cudaStreamWaitEvent(graph_stream_, ev, 0);
+    }
     long long iters = 0;
     srt_status status = SRT_OK;
     int per_check = 2;
     while (e == cudaSuccess) {
         if (prof) per_check = 1;  // events are re-recorded by every launch: read them each time
+        what = "cudaGraphLaunch";
         for (int k = 0; k < per_check && e == cudaSuccess; ++k) {
-            e = cudaGraphLaunch(graph, graph_stream_);
+            if (no_graph) {
+                what = "direct iteration launch";
+                launch_iteration(0, graph_stream_, false);
+                launch_iteration(1, graph_stream_, false);
+                e = cudaGetLastError();
+            } else {
+                e = cudaGraphLaunch(graph, graph_stream_);
+            }
             iters += 2;
             times_.launches += 10;
         }
         if (e != cudaSuccess) break;
+        what = "copy counters";
         e = cudaMemcpyAsync(host_counters_, counters_, sizeof(Counters), cudaMemcpyDeviceToHost, graph_stream_);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(graph_stream_);
+        if (e == cudaSuccess) {
+            what = "synchronize iteration graph";
+            e = cudaStreamSynchronize(graph_stream_);
+        }
         if (e != cudaSuccess) break;
         if (prof) {
+            what = "cudaEventElapsedTime";
             for (int par = 0; par < 2 && e == cudaSuccess; ++par)
                 for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
                     float ms = 0.0f;
@@ -736,7 +763,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
             status = set_error(SRT_ERR_STACK, "traversal stack overflow");
             break;
         }
-        if (until_idle && c.n_cur == 0) break;
+        if (c.n_cur == 0) break;  // nothing in flight: only a new job can add work
         if (budget_iters > 0 && iters >= budget_iters) break;
         if (max_iters > 0 && iters > max_iters) {
             status = set_error(SRT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
@@ -744,10 +771,19 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         }
         per_check = std::min(per_check * 2, 16);
     }
-    if (e == cudaSuccess) e = cudaEventRecord(ev, graph_stream_);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev, 0);
+    if (e == cudaSuccess) {
+        what = "record graph-stream event";
+        e = cudaEventRecord(ev, graph_stream_);
+    }
+    if (e == cudaSuccess) {
+        what = "caller stream waits on graph stream";
+        e = cudaStreamWaitEvent(st, ev, 0);
+    }
     cudaEventDestroy(ev);
-    if (e != cudaSuccess) return cuda_error(e, "wavefront run");
+    if (e != cudaSuccess) {
+        std::string msg = std::string("wavefront run (") + what + ", iteration " + std::to_string(iters) + ")";
+        return cuda_error(e, msg.c_str());
+    }
     return status;
 }
 

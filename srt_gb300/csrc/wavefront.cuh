@@ -27,6 +27,7 @@ struct JobRec {
     uint2* rng_b;        // per-pixel XORWOW state (v[4], d)
     int32_t* spp_done;   // per-pixel finished samples
     int32_t* pixels_done;  // pixels that finished every sample (one int)
+    int32_t* frame_done;   // [spp]: pixels that finished sample k (progressive frames), or null
     int32_t width, height, npix;
     int32_t spp, max_depth, rr_depth, use_nee, use_mis, seed, flags, rng_mode;
 };
@@ -78,6 +79,7 @@ public:
     srt_status reset_counters(cudaStream_t st);
     srt_status read_counters(Counters& c, cudaStream_t st);
     int32_t* pixels_done_slot(int job) const { return pixels_done_ + job; }
+    const int32_t* pixels_done_all() const { return pixels_done_; }
     void set_profiling(bool on) { profile_ = on; }
     bool profiling() const { return profile_; }
     KernelTimes& times() { return times_; }

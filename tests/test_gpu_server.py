@@ -1,0 +1,133 @@
+"""Render serving (continuous batching) on the GPU.
+
+Every pixel of every job has its own curand stream and its samples are
+accumulated in order, so a job's film is bit-identical whether it runs
+alone or packed with other jobs into the shared wavefront queues.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import golden, scene_from_npz
+from srt_gb300 import pt_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _alone(S, scene, w, h, params, cuda):
+    import torch
+    pt = S.PathTracer(scene, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device=cuda)
+    pt.render(film, params)
+    torch.cuda.synchronize()
+    return film.cpu().numpy()
+
+
+class Films:
+    """Caller-owned device films handed to the server."""
+
+    def __init__(self, cuda):
+        self.cuda, self.films = cuda, {}
+
+    def new(self, n):
+        import torch
+        f = torch.full((n, 4), -1.0, dtype=torch.float32, device=self.cuda)
+        return f
+
+    def host(self, f):
+        import torch
+        torch.cuda.synchronize()
+        return f.cpu().numpy()
+
+
+def _scenes(S):
+    cornell = scene_from_npz(golden("scene"))
+    spheres = S.procedural("spheres", seed=5, n_spheres=6, subdiv=3)
+    return cornell, spheres
+
+
+def test_mixed_jobs_equal_alone(cuda):
+    import srt_gb300 as S
+    cornell, spheres = _scenes(S)
+    jobs = [  # (arrays, w, h, spp, depth, seed)
+        (cornell, 40, 30, 8, 8, 11),
+        (spheres, 64, 36, 4, 16, 12),
+        (cornell, 17, 23, 16, 5, 13),
+        (spheres, 32, 32, 1, 16, 14),
+        (cornell, 96, 64, 2, 8, 15),
+    ]
+    scenes, films = {}, []
+    F = Films(cuda)
+    srv = S.Server(hbm_budget_bytes=8 << 30, max_paths=1 << 16, max_jobs=8, iterations_per_step=4)
+    ids = []
+    for k, (arr, w, h, spp, md, seed) in enumerate(jobs):
+        arr.set_aspect(w / h)
+        key = (id(arr), w, h)
+        scenes[key] = S.Scene(arr)  # camera aspect of this job
+        film = F.new(w * h) if k % 2 == 0 else None  # even jobs: caller film, odd: server-owned
+        films.append(film)
+        ids.append(srv.submit(scenes[key], w, h, pt_params(spp, md, 3, 1, 1, seed), film=film))
+    srv.drain(300)
+    infos = [srv.info(j) for j in ids]
+    assert all(i["state"] == 2 for i in infos)
+    # continuous batching: jobs overlapped on the device
+    assert sum(1 for a in infos for b in infos if a is not b and a["admit_s"] < b["done_s"] and b["admit_s"] < a["done_s"]) > 0
+    import torch
+    for (arr, w, h, spp, md, seed), jid, info, film in zip(jobs, ids, infos, films):
+        if film is None:  # server-owned film: copy it out (accumulate with weight 1 into zeros)
+            ptr = srv.film_ptr(jid)
+            assert ptr
+            film = torch.zeros((w * h, 4), dtype=torch.float32, device=cuda)
+            S.check(S.lib().srt_film_accumulate(C.c_void_p(ptr), C.c_void_p(film.data_ptr()), w * h, 0, None))
+        got = F.host(film)
+        ref = _alone(S, scenes[(id(arr), w, h)], w, h, pt_params(spp, md, 3, 1, 1, seed), cuda)
+        np.testing.assert_array_equal(got, ref)
+        ft = srv.frame_times(jid)
+        assert len(ft) == spp and all(a <= b for a, b in zip(ft, ft[1:]))
+        assert info["submit_s"] <= info["admit_s"] <= info["first_frame_s"] <= info["done_s"]
+        srv.release(jid)
+
+
+def test_admission_waits_for_budget_and_slots(cuda):
+    import srt_gb300 as S
+    cornell, _ = _scenes(S)
+    cornell.set_aspect(1.0)
+    scene = S.Scene(cornell)
+    # room for one 64x64 job's paths at a time: the others queue and are admitted later
+    srv = S.Server(hbm_budget_bytes=4 << 30, max_paths=64 * 64, max_jobs=4, iterations_per_step=2)
+    F = Films(cuda)
+    fl = [F.new(64 * 64) for _ in range(3)]
+    ids = [srv.submit(scene, 64, 64, pt_params(4, 6, 3, 1, 1, 100 + k), film=fl[k]) for k in range(3)]
+    r, q = srv.step()
+    assert r == 1 and q == 2
+    srv.drain(300)
+    infos = [srv.info(j) for j in ids]
+    assert all(i["state"] == 2 for i in infos)
+    assert infos[1]["admit_s"] >= infos[0]["done_s"] and infos[2]["admit_s"] >= infos[1]["done_s"]
+    for k, jid in enumerate(ids):
+        got = F.host(fl[k])
+        ref = _alone(S, scene, 64, 64, pt_params(4, 6, 3, 1, 1, 100 + k), cuda)
+        np.testing.assert_array_equal(got, ref)
+    with pytest.raises(S.SrtError) as e:
+        srv.submit(scene, 128, 128, pt_params(1, 4, 3, 1, 1, 0))  # more paths than the engine holds
+    assert e.value.status == 5
+
+
+def test_jobs_arriving_while_others_run(cuda):
+    import srt_gb300 as S
+    cornell, spheres = _scenes(S)
+    cornell.set_aspect(1.0)
+    spheres.set_aspect(1.0)
+    sc1, sc2 = S.Scene(cornell), S.Scene(spheres)
+    srv = S.Server(hbm_budget_bytes=8 << 30, max_paths=1 << 16, max_jobs=16, iterations_per_step=2)
+    F = Films(cuda)
+    f1, f2 = F.new(48 * 48), F.new(48 * 48)
+    first = srv.submit(sc1, 48, 48, pt_params(32, 8, 3, 1, 1, 7), film=f1)
+    srv.step()
+    late = srv.submit(sc2, 48, 48, pt_params(4, 16, 4, 1, 1, 8), film=f2)
+    srv.drain(300)
+    a, b = srv.info(first), srv.info(late)
+    assert b["admit_s"] < a["done_s"]  # admitted while the first job was still on the GPU
+    np.testing.assert_array_equal(F.host(f2), _alone(S, sc2, 48, 48, pt_params(4, 16, 4, 1, 1, 8), cuda))
+    np.testing.assert_array_equal(F.host(f1), _alone(S, sc1, 48, 48, pt_params(32, 8, 3, 1, 1, 7), cuda))
