@@ -298,6 +298,35 @@ srt_status srt_film_metric(const float* x, const float* ref, int64_t n, int32_t 
                            float discard, void* scratch, float* out, void* stream);
 
 /* ------------------------------------------------------------------ */
+/* Radiance-cache network (the learned part)                           */
+/* ------------------------------------------------------------------ */
+
+/* Replaces the tiny-cuda-nn network of the NeuralRadiosity pass
+ * (src/passes/npr/neural_radiosity.cu:6-52: encoding + CutlassMLP, Adam,
+ * relative L2 loss): 96 -> 5 x 64 (ReLU) -> 16 (exp on 3), BF16 weights,
+ * FP32 accumulation on tensor cores.  One query record is 16 floats:
+ * position, roughness, shading normal, -, direction toward the previous
+ * vertex, -, albedo, -.  Outputs are float4 (RGB radiance, 0). */
+typedef struct srt_mlp srt_mlp;
+#define SRT_MLP_PARAMS 23552
+srt_status srt_mlp_create(uint64_t seed, srt_mlp** out);
+/* Scene box that normalises positions before the frequency encoding. */
+srt_status srt_mlp_set_box(srt_mlp* mlp, const float* lo, const float* hi);
+/* FP32 master weights, W_l[out][in] row-major for l = 0..5 (host arrays). */
+srt_status srt_mlp_get_params(const srt_mlp* mlp, float* params);
+srt_status srt_mlp_set_params(srt_mlp* mlp, const float* params);
+/* records: device float[n*16]; out: device float[n*4]. */
+srt_status srt_mlp_infer(const srt_mlp* mlp, const float* records, int64_t n, float* out, void* stream);
+/* One Adam step (beta 0.9 / 0.99) on the relative L2 loss against
+ * targets (device float[n*4], RGB used); *loss (host, may be NULL). */
+srt_status srt_mlp_train_step(srt_mlp* mlp, const float* records, const float* targets, int64_t n,
+                              float lr, float* loss, void* stream);
+/* Loss gradient w.r.t. the weights without updating them (host float[SRT_MLP_PARAMS]). */
+srt_status srt_mlp_gradient(srt_mlp* mlp, const float* records, const float* targets, int64_t n,
+                            float* grad, float* loss, void* stream);
+void srt_mlp_destroy(srt_mlp* mlp);
+
+/* ------------------------------------------------------------------ */
 /* Render serving: continuous batching over one wavefront engine        */
 /* ------------------------------------------------------------------ */
 

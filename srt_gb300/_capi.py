@@ -98,6 +98,7 @@ class JobInfo(C.Structure):
 
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+MLP_PARAMS = 23552
 
 
 class BxdfBatch(C.Structure):
@@ -131,6 +132,14 @@ _PROTOS = [
     ("srt_film_metric_scratch_bytes", C.c_size_t, [C.c_int64]),
     ("srt_film_metric", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_float, C.c_void_p,
                                   f32p, C.c_void_p]),
+    ("srt_mlp_create", C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("srt_mlp_set_box", C.c_int, [C.c_void_p, f32p, f32p]),
+    ("srt_mlp_get_params", C.c_int, [C.c_void_p, f32p]),
+    ("srt_mlp_set_params", C.c_int, [C.c_void_p, f32p]),
+    ("srt_mlp_infer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("srt_mlp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, f32p, C.c_void_p]),
+    ("srt_mlp_gradient", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, f32p, f32p, C.c_void_p]),
+    ("srt_mlp_destroy", None, [C.c_void_p]),
     ("srt_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     ("srt_server_submit", C.c_int, [C.c_void_p, C.POINTER(JobDesc), C.POINTER(C.c_int64)]),
     ("srt_server_step", C.c_int, [C.c_void_p, i32p, i32p]),
