@@ -380,6 +380,22 @@ srt_status srt_server_release(srt_server* s, int64_t job_id);
 double srt_server_now(const srt_server* s);
 void srt_server_destroy(srt_server* s);
 
+/* srt_film_metric without a scratch argument, for callers that cannot
+ * allocate device memory when they measure a film: a serving loop that has
+ * reserved its whole HBM budget up front, or code that must not let
+ * cudaMalloc / cudaFree synchronise the device while other work is in
+ * flight.  No counterpart in the reference (its Measure pass allocates a
+ * GPUMemory error buffer per call).  The scratch is a fixed array in device
+ * memory of up to 2,097,152 pixels (about 8 MB, held by every GPU that loads
+ * the library until the process exits); larger n returns SRT_ERR_ARG.  It
+ * allocates nothing.  The first call on a device looks the array's device
+ * address up once (set-up), so make that first call before any stream
+ * capture.  All calls on a device share the array: calls that overlap on
+ * the GPU (different streams or host threads) race and must be serialised
+ * by the caller. */
+srt_status srt_film_metric_noalloc(const float* x, const float* ref, int64_t n, int32_t type,
+                                   float discard, float* out, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* Procedural scenes (inputs of the Cornell and 5.2M-triangle workloads) */
 /* ------------------------------------------------------------------ */

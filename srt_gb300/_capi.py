@@ -150,6 +150,8 @@ _PROTOS = [
     ("srt_server_release", C.c_int, [C.c_void_p, C.c_int64]),
     ("srt_server_now", C.c_double, [C.c_void_p]),
     ("srt_server_destroy", None, [C.c_void_p]),
+    ("srt_film_metric_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_float, f32p,
+                                          C.c_void_p]),
     ("srt_procedural_create", C.c_int, [C.c_char_p, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     ("srt_procedural_desc", C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
     ("srt_procedural_destroy", None, [C.c_void_p]),

@@ -6,6 +6,8 @@
 // in the reference, measure.cu:46-49) it finds the exact cut value with a
 // three-pass radix select over the error bits (11 + 11 + 10 bits) and sums
 // everything below it.
+#include <mutex>
+
 #include "common.h"
 #include "vmath.h"
 
@@ -271,6 +273,86 @@ extern "C" srt_status srt_film_metric(const float* x, const float* ref, int64_t 
                                                          ((size_t)n * 4 + 255) / 256 * 256);
     int g = grid_for(n);
     k_metric_init<<<1, 256, 0, st>>>(sc, keep);
+    k_metric_errors<<<g, kThreads, 0, st>>>(reinterpret_cast<const float4*>(x), reinterpret_cast<const float4*>(ref),
+                                            n, type, err);
+    const int shifts[3] = {21, 10, 0}, widths[3] = {11, 11, 10};
+    for (int p = 0; p < 3; ++p) {
+        k_metric_hist<<<g, kThreads, 0, st>>>(err, n, sc, shifts[p], widths[p]);
+        k_metric_select<<<1, 1, 0, st>>>(sc, shifts[p], widths[p], p == 2 ? 1 : 0);
+    }
+    SRT_CUDA_TRY(cudaGetLastError());
+    float res = 0.0f;
+    SRT_CUDA_TRY(cudaMemcpyAsync(&res, &sc->s.result, sizeof(float), cudaMemcpyDeviceToHost, st));
+    SRT_CUDA_TRY(cudaStreamSynchronize(st));
+    *out = res;
+    return SRT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free Measure metric.  Some callers cannot allocate device
+// memory when they measure a film: a render-serving loop that reserved its
+// whole HBM budget up front, or a caller that must not let cudaMalloc /
+// cudaFree synchronise the device while other jobs' frames are in flight.
+// This variant keeps its scratch (the per-pixel errors and the radix-select
+// state) in a fixed array in device memory instead of the caller's buffer.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kStaticMetricPixels = (int64_t)1 << 21;  // 2,097,152 pixels (1920x1080 fits)
+constexpr size_t kStaticMetricErrBytes = ((size_t)kStaticMetricPixels * 4 + 255) / 256 * 256;
+
+// Every GPU that loads the library holds this array (about 8 MB) until the
+// process exits; all calls on a device share it.
+static __device__ __align__(256) unsigned char g_metric_scratch[kStaticMetricErrBytes + sizeof(MetricScratch)];
+
+// Device address of g_metric_scratch on the current device, looked up once
+// per device (the array's host-side name is only a stand-in, never a device
+// address).
+srt_status static_metric_scratch(void** out)
+{
+    static std::mutex mu;
+    static void* ptrs[128] = {};
+    int dev = 0;
+    SRT_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return set_error(SRT_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_metric_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_metric_scratch)");
+        ptrs[dev] = p;
+    }
+    *out = ptrs[dev];
+    return SRT_OK;
+}
+
+}  // namespace
+
+extern "C" srt_status srt_film_metric_noalloc(const float* x, const float* ref, int64_t n, int32_t type,
+                                              float discard, float* out, void* stream)
+{
+    clear_error();
+    if (!out) return set_error(SRT_ERR_ARG, "out is NULL");
+    if (n < 0 || type < SRT_METRIC_MSE || type > SRT_METRIC_RELMSE || !(discard >= 0.0f && discard <= 100.0f))
+        return set_error(SRT_ERR_ARG, "bad arguments");
+    if (n > kStaticMetricPixels)
+        return set_error(SRT_ERR_ARG, "srt_film_metric_noalloc: n = " + std::to_string(n) +
+                                          " exceeds its fixed scratch of 2097152 pixels; use srt_film_metric");
+    long long keep = (long long)((float)n * (1.0f - discard / 100.0f));
+    if (keep <= 0) {
+        *out = NAN;
+        return SRT_OK;
+    }
+    if (!x || !ref) return set_error(SRT_ERR_ARG, "NULL buffer");
+    if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(ref)) % 16)
+        return set_error(SRT_ERR_ARG, "films must be 16-byte aligned");
+    void* base = nullptr;
+    SRT_TRY(static_metric_scratch(&base));
+    cudaStream_t st = as_stream(stream);
+    float* err = reinterpret_cast<float*>(base);
+    MetricScratch* sc = reinterpret_cast<MetricScratch*>(reinterpret_cast<char*>(base) + kStaticMetricErrBytes);
+    int g = grid_for(n);
+    k_metric_init<<<1, 256, 0, st>>>(sc, keep);  // clears the histograms and the select state
     k_metric_errors<<<g, kThreads, 0, st>>>(reinterpret_cast<const float4*>(x), reinterpret_cast<const float4*>(ref),
                                             n, type, err);
     const int shifts[3] = {21, 10, 0}, widths[3] = {11, 11, 10};
