@@ -168,6 +168,25 @@ def config_dict(info):
     return d
 
 
+def profile_case():
+    """The benchmark scene (392 MB resident, larger than L2) at 1920x1080
+    with 1 spp, two frames: the first closest-hit launch traces one camera
+    ray per pixel (2.07M rays), a few hundred launches in all, for ncu."""
+    import torch
+    import srt_gb300 as S
+    arrays = build_scene(S)
+    scene = S.Scene(arrays)
+    pt = S.PathTracer(scene, W, H)
+    film = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
+    for seed in range(2):
+        pt.render(film, S.pt_params(1, MAX_DEPTH, RR_DEPTH, 1, 1, seed))
+    torch.cuda.synchronize()
+    st = pt.stats()
+    print(json.dumps({"profile_case": "1920x1080x1spp", "closest_rays": st["closest_rays"],
+                      "shadow_rays": st["shadow_rays"], "iterations": st["iterations"],
+                      "kernel_launches": st["kernel_launches"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -175,7 +194,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="short run of the same scene (1 spp, two frames) for ncu captures")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case()
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

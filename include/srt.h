@@ -326,6 +326,30 @@ srt_status srt_mlp_gradient(srt_mlp* mlp, const float* records, const float* tar
                             float* grad, float* loss, void* stream);
 void srt_mlp_destroy(srt_mlp* mlp);
 
+/* Radiance-cache rendering of one frame with the PathTracer pass (the
+ * NeuralRadiosity pass's query-at-the-second-vertex estimator,
+ * src/shader/npr/nr_rhs.cu:50-157, with the network trained online on the
+ * tracer's own full paths instead of offline). */
+typedef struct srt_cache_params {
+    int32_t train_paths;      /* full-length training paths per frame (65536)          */
+    int32_t train_steps;      /* Adam steps per frame over the gathered vertices (4)  */
+    float learning_rate;      /* 1e-2                                                  */
+    float region_threshold;   /* relative bias that disables a cell (plain fallback)   */
+    int32_t region_res;       /* grid cells per axis over the network's scene box (16) */
+    int32_t train;            /* 0: frozen network (inference only)                    */
+} srt_cache_params;
+
+typedef struct srt_cache_stats {
+    int64_t queries;          /* paths ended by a network query                        */
+    int64_t fallback_queries; /* second vertices in disabled cells (traced plainly)     */
+    int64_t train_vertices;   /* training vertices gathered this frame                 */
+    float loss;               /* mean relative L2 loss of this frame's Adam steps      */
+    int32_t disabled_cells;   /* cells whose measured bias exceeds the threshold        */
+} srt_cache_stats;
+
+srt_status srt_pt_render_cached(srt_pt* pt, float* film, const srt_pt_params* params, srt_mlp* mlp,
+                                const srt_cache_params* cache, srt_cache_stats* stats, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* Render serving: continuous batching over one wavefront engine        */
 /* ------------------------------------------------------------------ */
@@ -348,6 +372,7 @@ typedef struct srt_job_desc {
     int32_t width, height;
     srt_pt_params params;         /* same meaning as for srt_pt_render                      */
     float* film;                  /* caller's device float4[w*h], or NULL: server-owned     */
+    struct srt_mlp* cache;        /* trained radiance cache of this scene (frozen), or NULL */
 } srt_job_desc;
 
 enum { SRT_JOB_QUEUED = 0, SRT_JOB_RUNNING = 1, SRT_JOB_DONE = 2, SRT_JOB_FAILED = 3 };

@@ -281,8 +281,9 @@ class Server:
         self.handle = C.c_void_p()
         check(lib().srt_server_create(C.byref(cfg), C.byref(self.handle)))
 
-    def submit(self, scene: Scene, width, height, params, film=None):
-        d = _capi.JobDesc(scene.handle, width, height, params, None if film is None else film.data_ptr())
+    def submit(self, scene: Scene, width, height, params, film=None, cache=None):
+        d = _capi.JobDesc(scene.handle, width, height, params, None if film is None else film.data_ptr(),
+                          cache)
         jid = C.c_int64()
         check(lib().srt_server_submit(self.handle, C.byref(d), C.byref(jid)))
         return jid.value

@@ -88,7 +88,7 @@ class ServerConfig(C.Structure):
 
 class JobDesc(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("params", PtParams),
-                ("film", C.c_void_p)]
+                ("film", C.c_void_p), ("cache", C.c_void_p)]
 
 
 class JobInfo(C.Structure):
@@ -99,6 +99,16 @@ class JobInfo(C.Structure):
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 MLP_PARAMS = 23552
+
+
+class CacheParams(C.Structure):
+    _fields_ = [("train_paths", C.c_int32), ("train_steps", C.c_int32), ("learning_rate", C.c_float),
+                ("region_threshold", C.c_float), ("region_res", C.c_int32), ("train", C.c_int32)]
+
+
+class CacheStats(C.Structure):
+    _fields_ = [("queries", C.c_int64), ("fallback_queries", C.c_int64), ("train_vertices", C.c_int64),
+                ("loss", C.c_float), ("disabled_cells", C.c_int32)]
 
 
 class BxdfBatch(C.Structure):
@@ -140,6 +150,8 @@ _PROTOS = [
     ("srt_mlp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, f32p, C.c_void_p]),
     ("srt_mlp_gradient", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, f32p, f32p, C.c_void_p]),
     ("srt_mlp_destroy", None, [C.c_void_p]),
+    ("srt_pt_render_cached", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PtParams), C.c_void_p,
+                                       C.POINTER(CacheParams), C.POINTER(CacheStats), C.c_void_p]),
     ("srt_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     ("srt_server_submit", C.c_int, [C.c_void_p, C.POINTER(JobDesc), C.POINTER(C.c_int64)]),
     ("srt_server_step", C.c_int, [C.c_void_p, i32p, i32p]),

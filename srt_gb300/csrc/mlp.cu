@@ -19,6 +19,7 @@
 
 #include "common.h"
 #include "mlp.cuh"
+#include "wavefront.cuh"
 
 namespace srt {
 
@@ -460,6 +461,49 @@ __global__ void k_to_bf16(const float* __restrict__ wf, __nv_bfloat16* __restric
     if (i < n) wb[i] = __float2bfloat16(wf[i]);
 }
 
+// Radiance-cache queries of one job per blockIdx.y: network output times the
+// path throughput is added to the pixel's in-flight radiance (one path per
+// pixel in flight, so a plain read-modify-write).
+__global__ void __launch_bounds__(kMlpThreads) k_cache_query(const JobRec* __restrict__ jobs)
+{
+    const JobRec& J = jobs[blockIdx.y];
+    const CacheRec& C = J.cache;
+    if (!C.w) return;  // uniform over the block
+    const int64_t n = min((int64_t)C.q_count[0], (int64_t)J.npix);
+    if (n == 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __nv_bfloat16* ws = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+    load_weights(C.w, ws, nullptr);
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int warp = threadIdx.x >> 5;
+    const int64_t tiles = (n + 15) / 16;
+    for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < tiles; tile += (int64_t)gridDim.x * 4) {
+        int64_t r0 = tile * 16 + g, r1 = r0 + 8;
+        bool v0 = r0 < n, v1 = r1 < n;
+        float4 q0[4], q1[4];
+        load_record(C.q_rec, r0, v0, q0);
+        load_record(C.q_rec, r1, v1, q1);
+        uint32_t a0[6][4];
+        input_fragments(q0, q1, v0, v1, C.box, a0);
+        float z[2][4];
+        uint32_t masks[5];
+        forward_tile<false>(ws, a0, z, masks, nullptr);
+        float3 o0, o1;
+        output_rgb(z, o0, o1);
+        if (t == 0) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (!(k ? v1 : v0)) continue;
+                float4 b = C.q_beta[k ? r1 : r0];
+                float3 o = k ? o1 : o0;
+                float4* lp = J.lpath + __float_as_int(b.w);
+                float4 l = *lp;
+                *lp = make_float4(l.x + b.x * o.x, l.y + b.y * o.y, l.z + b.z * o.z, 0.0f);
+            }
+        }
+    }
+}
+
 size_t infer_smem() { return (size_t)kWSmem * 2; }
 size_t train_smem() { return (size_t)(kWSmem + kWtSmem) * 2; }
 
@@ -468,21 +512,6 @@ size_t train_smem() { return (size_t)(kWSmem + kWtSmem) * 2; }
 }  // namespace srt
 
 using namespace srt;
-
-struct srt_mlp {
-    DeviceBuffer params;   // fp32 master | bf16 copy | adam m | adam v | grad | loss
-    float* wf = nullptr;
-    __nv_bfloat16* wb = nullptr;
-    float* m = nullptr;
-    float* v = nullptr;
-    float* grad = nullptr;
-    float* loss = nullptr;
-    DeviceBuffer scratch;  // act | dz for the largest batch seen
-    int64_t scratch_rows = 0;
-    MlpBox box{};
-    int64_t step = 0;
-    float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
-};
 
 namespace {
 
@@ -500,6 +529,7 @@ srt_status configure_smem()
     static bool done = false;
     if (done) return SRT_OK;
     SRT_CUDA_TRY(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
+    SRT_CUDA_TRY(cudaFuncSetAttribute(k_cache_query, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
     SRT_CUDA_TRY(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
     done = true;
     return SRT_OK;
@@ -550,6 +580,13 @@ srt_status mlp_train_launch(srt_mlp* p, const float4* rec, const float4* target,
 }
 
 MlpView mlp_view(const srt_mlp* p) { return MlpView{p->wb, p->box}; }
+
+void launch_cache_queries(const JobRec* jobs, int max_jobs, cudaStream_t st)
+{
+    configure_smem();
+    dim3 grid((unsigned)device_sm_count(), (unsigned)max_jobs);
+    k_cache_query<<<grid, kMlpThreads, infer_smem(), st>>>(jobs);
+}
 
 }  // namespace srt
 

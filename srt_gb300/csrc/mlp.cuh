@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "common.h"
+
 namespace srt {
 
 constexpr int kMlpIn = 96;
@@ -50,4 +52,26 @@ struct MlpView {
     MlpBox box;
 };
 
+}  // namespace srt
+
+// Network state: FP32 master weights, BF16 copy, Adam moments, gradient.
+struct srt_mlp {
+    srt::DeviceBuffer params;  // fp32 master | adam m | adam v | grad | loss | bf16 copy
+    float* wf = nullptr;
+    __nv_bfloat16* wb = nullptr;
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grad = nullptr;
+    float* loss = nullptr;
+    srt::DeviceBuffer scratch;  // per-row layer inputs and gradients for training
+    int64_t scratch_rows = 0;
+    srt::MlpBox box{};
+    int64_t step = 0;
+    float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+};
+
+namespace srt {
+srt_status mlp_infer_launch(const srt_mlp* p, const float4* rec, int64_t n, float4* out, cudaStream_t st);
+srt_status mlp_train_launch(srt_mlp* p, const float4* rec, const float4* target, int64_t n, float lr, bool update,
+                            cudaStream_t st);
 }  // namespace srt

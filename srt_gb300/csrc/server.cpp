@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "common.h"
+#include "mlp.cuh"
 #include "scene.h"
 #include "wavefront.cuh"
 
@@ -34,13 +35,18 @@ struct Job {
     bool own_film = false;
     double submit_s = 0, admit_s = -1, first_frame_s = -1, done_s = -1;
     std::vector<double> frame_times;
+    size_t frames_off = 0;  // byte offset of the frame counters in state_buf
 };
 
-size_t state_bytes(int64_t npix, int spp)
+size_t frames_bytes(int spp) { return ((size_t)std::max(spp, 1) * 4 + 255) & ~(size_t)255; }
+
+size_t state_bytes(int64_t npix, int spp, bool cache)
 {
-    // lpath 16 + rng_a 16 + rng_b 8 + spp_done 4 per pixel, frame counters
-    size_t b = (size_t)npix * 44 + (size_t)std::max(spp, 1) * 4;
-    return (b + 255) & ~(size_t)255;
+    // lpath 16 + rng_a 16 + rng_b 8 + spp_done 4 per pixel (rounded), frame counters,
+    // and for a cached job its query records (64 B), throughputs (16 B) and counters
+    size_t b = (((size_t)npix * 44 + 255) & ~(size_t)255) + frames_bytes(spp);
+    if (cache) b += (size_t)npix * 80 + 256;
+    return b;
 }
 
 }  // namespace
@@ -76,7 +82,8 @@ struct srt_server {
     srt_status admit(Job& j, int slot)
     {
         const int spp = j.desc.params.samples_per_pixel;
-        size_t sb = state_bytes(j.npix, spp);
+        const bool cached = j.desc.cache != nullptr;
+        size_t sb = state_bytes(j.npix, spp, cached);
         cudaError_t e = cudaMallocAsync(&j.state_buf, sb, stream);
         if (e != cudaSuccess) return cuda_error(e, "job state allocation");
         if (!j.desc.film) {
@@ -92,8 +99,10 @@ struct srt_server {
         }
         char* b = reinterpret_cast<char*>(j.state_buf);
         const size_t n = (size_t)j.npix;
-        int32_t* frame_done = reinterpret_cast<int32_t*>(b + n * 44);
-        SRT_CUDA_TRY(cudaMemsetAsync(frame_done, 0, (size_t)std::max(spp, 1) * 4, stream));
+        const size_t px_bytes = ((size_t)n * 44 + 255) & ~(size_t)255;
+        int32_t* frame_done = reinterpret_cast<int32_t*>(b + px_bytes);
+        SRT_CUDA_TRY(cudaMemsetAsync(frame_done, 0, frames_bytes(spp), stream));
+        j.frames_off = px_bytes;
         JobRec J{};
         const srt_scene* sc = j.desc.scene;
         J.scene = sc->view;
@@ -117,6 +126,22 @@ struct srt_server {
         J.seed = j.desc.params.seed;
         J.flags = j.desc.params.flags;
         J.rng_mode = j.desc.params.rng_mode;
+        if (cached) {
+            // frozen network: every pixel ends at its second vertex with a query
+            char* cb = b + px_bytes + frames_bytes(spp);
+            CacheRec& C = J.cache;
+            C.w = j.desc.cache->wb;
+            C.box = j.desc.cache->box;
+            C.q_rec = reinterpret_cast<float4*>(cb);
+            C.q_beta = reinterpret_cast<float4*>(cb + n * 64);
+            C.q_count = reinterpret_cast<int32_t*>(cb + n * 80);
+            SRT_CUDA_TRY(cudaMemsetAsync(C.q_count, 0, 64, stream));
+            C.region_off = nullptr;
+            C.region_res = 1;
+            C.train_stride = j.npix + 1;  // no training pixels
+            C.train_phase = -1;
+            engine.enable_cache();
+        }
         SRT_TRY(engine.set_job(slot, J, stream));
         SRT_TRY(engine.start_job(slot, J, stream));
         j.slot = slot;
@@ -137,7 +162,7 @@ struct srt_server {
         j.state_buf = nullptr;
         slots[j.slot] = 0;
         paths_used -= j.npix;
-        bytes_used -= (int64_t)state_bytes(j.npix, j.desc.params.samples_per_pixel);
+        bytes_used -= (int64_t)state_bytes(j.npix, j.desc.params.samples_per_pixel, j.desc.cache != nullptr);
         if (--scene_refs[j.desc.scene] == 0) {
             scene_refs.erase(j.desc.scene);
             bytes_used -= scene_bytes(j.desc.scene);
@@ -181,7 +206,9 @@ extern "C" srt_status srt_server_submit(srt_server* s, const srt_job_desc* d, in
     j->id = s->next_id++;
     j->desc = *d;
     j->npix = d->width * d->height;
-    j->bytes = (int64_t)state_bytes(j->npix, p.samples_per_pixel) + (d->film ? 0 : (int64_t)j->npix * 16);
+    j->bytes = (int64_t)state_bytes(j->npix, p.samples_per_pixel, d->cache != nullptr) +
+               (d->film ? 0 : (int64_t)j->npix * 16);
+    if (d->cache && p.max_depth < 2) return set_error(SRT_ERR_ARG, "cached jobs need max_depth >= 2");
     j->submit_s = s->now();
     int64_t fixed = (int64_t)s->engine.device_bytes();
     if (j->npix > s->cfg.max_paths || fixed + j->bytes + d->scene->info.device_bytes > s->cfg.hbm_budget_bytes)
@@ -241,7 +268,7 @@ extern "C" srt_status srt_server_step(srt_server* s, int32_t* running, int32_t* 
         for (int64_t id : s->slots) {
             if (!id) continue;
             Job& j = *s->jobs[id];
-            const char* b = reinterpret_cast<const char*>(j.state_buf) + (size_t)j.npix * 44;
+            const char* b = reinterpret_cast<const char*>(j.state_buf) + j.frames_off;
             SRT_CUDA_TRY(cudaMemcpyAsync(s->h_frames + off, b, 4 * (size_t)j.desc.params.samples_per_pixel,
                                          cudaMemcpyDeviceToHost, s->stream));
             off += (size_t)j.desc.params.samples_per_pixel;

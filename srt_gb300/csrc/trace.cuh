@@ -17,7 +17,12 @@
 
 namespace srt {
 
-constexpr int kStackEntries = 32;
+constexpr int kStackEntries = 24;  // node groups; at most one per tree level
+
+// resident 128-thread traversal blocks per SM the compiler budgets registers for
+#ifndef SRT_TRACE_MIN_BLOCKS
+#define SRT_TRACE_MIN_BLOCKS 6
+#endif
 
 struct Hit {
     float t, u, v;
@@ -228,6 +233,115 @@ __device__ __forceinline__ Hit trace_closest(const SceneView& S, float3 o, float
         }
     }
     return h;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent traversal with lane refill.  A warp keeps 32 rays in flight;
+// each lane advances its own ray by a bounded number of node visits per
+// round, and as soon as at least kRefill lanes have finished, the warp
+// fetches that many new rays with one atomic (Aila & Laine, "Understanding
+// the efficiency of ray traversal on GPUs", HPG 2009), so lanes do not idle
+// until the slowest ray of a fixed batch ends.
+// ---------------------------------------------------------------------------
+constexpr int kRefill = 8;
+constexpr int kStepBudget = 4;  // node visits per lane between refill checks
+
+struct TravState {
+    RayPre r;
+    float tmin, tmax;  // tmax shrinks with closest hits
+    uint2 group;
+    uint32_t tmask, tri_base;
+    float u, v;
+    int32_t tri;
+    const WideNode* nodes;
+    const float4* tris;
+};
+
+__device__ __forceinline__ void trav_init(TravState& s, const WideNode* nodes, const float4* tris, float3 o, float3 d,
+                                          float tmin, float tmax, Stack& st)
+{
+    s.r = make_ray(o, d);
+    s.tmin = tmin;
+    s.tmax = tmax;
+    s.group = make_uint2(0u, 1u | ((1u << s.r.oct) << 8));
+    s.tmask = 0;
+    s.tri_base = 0;
+    s.u = s.v = 0.0f;
+    s.tri = -1;
+    s.nodes = nodes;
+    s.tris = tris;
+    st.sp = 0;
+}
+
+// Advances one ray; returns true when its traversal is complete (for any-hit
+// rays: on the first hit, with s.tri set).
+template <bool kAny, bool kCount>
+__device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overflow, TraceCount& cnt)
+{
+    for (int it = 0; it < kStepBudget; ++it) {
+        while (s.tmask) {
+            uint32_t b = __ffs(s.tmask) - 1;
+            s.tmask &= s.tmask - 1;
+            uint32_t ti = s.tri_base + b;
+            const float4* tp = s.tris + 3 * (size_t)ti;
+            float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
+            float t, u, v;
+            if (hit_triangle(s.r, f3(a), f3(bb), f3(c), s.tmin, s.tmax, t, u, v)) {
+                s.u = u;
+                s.v = v;
+                s.tri = (int32_t)ti;
+                if (kAny) return true;
+                s.tmax = t;
+            }
+        }
+        if ((s.group.y >> 8) == 0u) {
+            if (st.sp == 0) return true;
+            s.group = st.pop();
+        }
+        uint32_t ni = group_next_node(s.group, s.r.oct);
+        if ((s.group.y >> 8) != 0u) st.push(s.group, overflow);
+        visit_node(s.nodes, ni, s.r, s.tmin, s.tmax, s.group, s.tmask, s.tri_base);
+        if (kCount) {
+            cnt.nodes += 1;
+            cnt.tris += __popc(s.tmask);
+        }
+    }
+    return false;
+}
+
+// Drives a warp over rays [0, n) taken from *fetch.  load(i, state, stack)
+// starts ray i (calls trav_init); store(i, state) writes its result.
+template <bool kAny, bool kCount, class Load, class Store>
+__device__ __forceinline__ void trace_persistent(int64_t n, unsigned long long* fetch, Stack& st, int& overflow,
+                                                 TraceCount& cnt, Load load, Store store)
+{
+    const uint32_t full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int64_t ray = -1;
+    TravState s;
+    bool drained = false;
+    for (;;) {
+        uint32_t idle = __ballot_sync(full, ray < 0);
+        if (!drained && (int)__popc(idle) >= kRefill) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(fetch, (unsigned long long)__popc(idle));
+            base = __shfl_sync(full, base, 0);
+            if (base + __popc(idle) >= (unsigned long long)n) drained = true;
+            if (ray < 0) {
+                int64_t idx = (int64_t)base + __popc(idle & ((1u << lane) - 1u));
+                if (idx < n) {
+                    ray = idx;
+                    load(idx, s, st);
+                }
+            }
+            idle = __ballot_sync(full, ray < 0);
+        }
+        if (idle == full && drained) break;
+        if (ray >= 0 && trav_advance<kAny, kCount>(s, st, overflow, cnt)) {
+            store(ray, s);
+            ray = -1;
+        }
+    }
 }
 
 // Any hit in (tmin, tmax): true when occluded.

@@ -10,50 +10,42 @@ namespace {
 
 constexpr int kTraceThreads = 128;
 
-__device__ __forceinline__ int64_t fetch_batch(unsigned long long* counter)
-{
-    unsigned long long base = 0;
-    if ((threadIdx.x & 31) == 0) base = atomicAdd(counter, 32ull);
-    return (int64_t)__shfl_sync(0xffffffffu, base, 0);
-}
-
-__global__ void __launch_bounds__(kTraceThreads) k_trace_closest(SceneView S, const float4* __restrict__ rays,
-                                                                 int64_t n, float4* __restrict__ hits,
-                                                                 unsigned long long* counter, int* overflow_flag)
+__global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace_closest(SceneView S, const float4* __restrict__ rays,
+                                                                    int64_t n, float4* __restrict__ hits,
+                                                                    unsigned long long* counter, int* overflow_flag)
 {
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
     Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
     int overflow = 0;
-    for (;;) {
-        int64_t base = fetch_batch(counter);
-        if (base >= n) break;
-        int64_t i = base + (threadIdx.x & 31);
-        if (i < n) {
+    TraceCount cnt;
+    trace_persistent<false, false>(
+        n, counter, st, overflow, cnt,
+        [&](int64_t i, TravState& s, Stack& stk) {
             float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
-            Hit h = trace_closest(S, f3(a), f3(b), a.w, b.w, st, overflow);
-            int32_t prim = h.tri >= 0 ? __ldg(S.tri_prim + h.tri) : -1;
-            hits[i] = make_float4(h.tri >= 0 ? h.t : b.w, h.u, h.v, __int_as_float(prim));
-        }
-    }
+            trav_init(s, S.nodes, S.tris, f3(a), f3(b), a.w, b.w, stk);
+        },
+        [&](int64_t i, const TravState& s) {
+            int32_t prim = s.tri >= 0 ? __ldg(S.tri_prim + s.tri) : -1;
+            hits[i] = make_float4(s.tmax, s.u, s.v, __int_as_float(prim));
+        });
     if (overflow) atomicAdd(overflow_flag, 1);
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(SceneView S, const float4* __restrict__ rays,
-                                                                int64_t n, int32_t* __restrict__ visible,
-                                                                unsigned long long* counter, int* overflow_flag)
+__global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace_shadow(SceneView S, const float4* __restrict__ rays,
+                                                                   int64_t n, int32_t* __restrict__ visible,
+                                                                   unsigned long long* counter, int* overflow_flag)
 {
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
     Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
     int overflow = 0;
-    for (;;) {
-        int64_t base = fetch_batch(counter);
-        if (base >= n) break;
-        int64_t i = base + (threadIdx.x & 31);
-        if (i < n) {
+    TraceCount cnt;
+    trace_persistent<true, false>(
+        n, counter, st, overflow, cnt,
+        [&](int64_t i, TravState& s, Stack& stk) {
             float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
-            visible[i] = trace_any(S, f3(a), f3(b), a.w, b.w, st, overflow) ? 0 : 1;
-        }
-    }
+            trav_init(s, S.nodes, S.tris, f3(a), f3(b), a.w, b.w, stk);
+        },
+        [&](int64_t i, const TravState& s) { visible[i] = s.tri >= 0 ? 0 : 1; });
     if (overflow) atomicAdd(overflow_flag, 1);
 }
 

@@ -83,6 +83,30 @@ __device__ __forceinline__ int32_t warp_append(int32_t* counter, bool pred)
     return pred ? base + __popc(m & ((1u << lane) - 1u)) : -1;
 }
 
+// Append where lanes may target different counters (one per job): lanes
+// with the same counter share one atomic.  All 32 lanes must call it.
+__device__ __forceinline__ int32_t warp_append_multi(int32_t* counter, bool pred)
+{
+    uint32_t active = __ballot_sync(kFull, pred);
+    if (!pred) return -1;
+    uint32_t peers = __match_any_sync(active, (unsigned long long)counter);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(peers) - 1;
+    int32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ int region_cell(const CacheRec& c, float3 p)
+{
+    int r = c.region_res;
+    int x = min(max((int)((p.x - c.box.lo.x) * c.box.inv_extent.x * r), 0), r - 1);
+    int y = min(max((int)((p.y - c.box.lo.y) * c.box.inv_extent.y * r), 0), r - 1);
+    int z = min(max((int)((p.z - c.box.lo.z) * c.box.inv_extent.z * r), 0), r - 1);
+    return (z * r + y) * r + x;
+}
+
 // Camera::get_ray, perspective / orthographic (camera.h:107-122).
 __device__ __forceinline__ void camera_ray(const CameraRec& c, float x, float y, float3& o, float3& d)
 {
@@ -208,6 +232,8 @@ __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ j
             J.film[pix] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
             J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             J.spp_done[pix] = 0;
+            if (J.cache.w && (pix % J.cache.train_stride) == J.cache.train_phase)
+                J.cache.t_len[pix / J.cache.train_stride] = 0;
         }
         int32_t slot = warp_append(n, valid);
         if (valid) {
@@ -232,9 +258,9 @@ __device__ __forceinline__ int64_t fetch_batch(unsigned long long* counter)
 }
 
 template <bool kCount>
-__global__ void __launch_bounds__(kTraceThreads) k_closest(const JobRec* __restrict__ jobs, PathQueue q,
-                                                           float4* __restrict__ hits, Counters* ctr,
-                                                           int64_t capacity)
+__global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest(const JobRec* __restrict__ jobs, PathQueue q,
+                                                              float4* __restrict__ hits, Counters* ctr,
+                                                              int64_t capacity)
 {
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
     Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
@@ -242,17 +268,14 @@ __global__ void __launch_bounds__(kTraceThreads) k_closest(const JobRec* __restr
     const int64_t n = min((int64_t)ctr->n_cur, capacity);
     int overflow = 0;
     TraceCount cnt;
-    for (;;) {
-        int64_t base = fetch_batch(&ctr->fetch_closest);
-        if (base >= n) break;
-        int64_t i = base + (threadIdx.x & 31);
-        if (i < n) {
+    trace_persistent<false, kCount>(
+        n, &ctr->fetch_closest, st, overflow, cnt,
+        [&](int64_t i, TravState& s, Stack& stk) {
             float4 o = q.o[i], d = q.d[i];
-            int job = (int)(__float_as_uint(q.beta[i].w) >> 16);
-            Hit h = trace_closest<kCount>(jobs[job].scene, f3(o), f3(d), 1e-3f, 1e16f, st, overflow, &cnt);
-            hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
-        }
-    }
+            const SceneView& S = jobs[__float_as_uint(q.beta[i].w) >> 16].scene;
+            trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, 1e16f, stk);
+        },
+        [&](int64_t i, const TravState& s) { hits[i] = make_float4(s.tmax, s.u, s.v, __int_as_float(s.tri)); });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
     if (kCount && (cnt.nodes | cnt.tris)) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_nodes), (unsigned long long)cnt.nodes);
@@ -269,7 +292,8 @@ __global__ void __launch_bounds__(kThreads) k_shade(const JobRec* __restrict__ j
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
         const int i = base + (threadIdx.x & 31);
         const bool valid = i < n;
-        bool push_next = false, push_shadow = false, terminate = false;
+        bool push_next = false, push_shadow = false, terminate = false, push_query = false;
+        float4 qrec[4];
         float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
         float3 sh_o = f3(0.0f), sh_d = f3(0.0f), sh_c = f3(0.0f);
         float sh_t = 0.0f, pdf_next = 0.0f;
@@ -333,13 +357,40 @@ __global__ void __launch_bounds__(kThreads) k_shade(const JobRec* __restrict__ j
                         L_add = beta * f3(em) * mis;
                     }
                 } else {
+                    if (dot(ng, -rd) < 0.0f) ng = -ng;
+                    const float3 wo = -rd;
+                    // radiance cache: non-training pixels end at the second vertex
+                    const CacheRec& Cc = J.cache;
+                    const bool cache_job = Cc.w != nullptr;
+                    const bool train_pix = cache_job && (pix % Cc.train_stride) == Cc.train_phase;
+                    if (cache_job && !train_pix && depth == 1) {
+                        push_query = !Cc.region_off || !Cc.region_off[region_cell(Cc, pos)];
+                        if (!push_query) atomicAdd(Cc.q_count + 1, 1);
+                    }
+                    if (push_query) {
+                        qrec[0] = make_float4(pos.x, pos.y, pos.z, bx.type == BXDF_DISNEY ? bx.roughness : 1.0f);
+                        qrec[1] = make_float4(ng.x, ng.y, ng.z, 0.0f);
+                        qrec[2] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+                        qrec[3] = make_float4(base_color.x, base_color.y, base_color.z, 0.0f);
+                    } else {
+                    if (train_pix && depth >= 1 && depth <= kTrainVertices && J.spp_done[pix] == 0) {
+                        // training vertex: features, arriving throughput, radiance gathered so far
+                        int slot = (pix / Cc.train_stride) * kTrainVertices + depth - 1;
+                        float4* tr = Cc.t_rec + 4 * (size_t)slot;
+                        tr[0] = make_float4(pos.x, pos.y, pos.z, bx.type == BXDF_DISNEY ? bx.roughness : 1.0f);
+                        tr[1] = make_float4(ng.x, ng.y, ng.z, 0.0f);
+                        tr[2] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+                        tr[3] = make_float4(base_color.x, base_color.y, base_color.z, 0.0f);
+                        float4 lnow = J.lpath[pix];
+                        Cc.t_aux[2 * (size_t)slot] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+                        Cc.t_aux[2 * (size_t)slot + 1] = make_float4(lnow.x, lnow.y, lnow.z, 0.0f);
+                        Cc.t_len[pix / Cc.train_stride] = depth;
+                    }
                     Rng rng;
                     rng.load(ra, rb);
                     float3 tan = (fabsf(sn.x) > fabsf(sn.y)) ? make_float3(0.f, 1.f, 0.f) : make_float3(1.f, 0.f, 0.f);
                     Frame fr = Frame::from_normal_tangent(sn, tan);
-                    if (dot(ng, -rd) < 0.0f) ng = -ng;
                     const bool transmissive = (mflags & kMatTransmissive) != 0;
-                    const float3 wo = -rd;
                     // NEE with MIS (path_tracer.cu:113-142)
                     if (J.use_nee && !(mflags & kMatSpecular)) {
                         float lu = rng.next();
@@ -390,8 +441,20 @@ __global__ void __launch_bounds__(kThreads) k_shade(const JobRec* __restrict__ j
                         }
                     }
                     rng.store(ra, rb);
+                    }
                 }
             }
+        }
+        // network query of a cached path (its radiance is added by k_cache)
+        int32_t qslot = warp_append_multi(jobs[job].cache.q_count, valid && push_query);
+        if (push_query) {
+            const CacheRec& Cc = jobs[job].cache;
+            float4* qr = Cc.q_rec + 4 * (size_t)qslot;
+            qr[0] = qrec[0];
+            qr[1] = qrec[1];
+            qr[2] = qrec[2];
+            qr[3] = qrec[3];
+            Cc.q_beta[qslot] = make_float4(beta.x, beta.y, beta.z, __int_as_float(pix));
         }
         // emitter / miss radiance of this vertex
         if (valid && (L_add.x != 0.0f || L_add.y != 0.0f || L_add.z != 0.0f || !finite3(L_add))) {
@@ -436,29 +499,30 @@ __global__ void __launch_bounds__(kThreads) k_shade(const JobRec* __restrict__ j
 }
 
 template <bool kCount>
-__global__ void __launch_bounds__(kTraceThreads) k_shadow(const JobRec* __restrict__ jobs, ShadowQueue sq,
-                                                          Counters* ctr, int64_t capacity)
+__global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_shadow(const JobRec* __restrict__ jobs, ShadowQueue sq,
+                                                             Counters* ctr, int64_t capacity)
 {
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
     Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
     const int64_t n = min((int64_t)ctr->n_shadow, capacity);
     int overflow = 0;
     TraceCount cnt;
-    for (;;) {
-        int64_t base = fetch_batch(&ctr->fetch_shadow);
-        if (base >= n) break;
-        int64_t i = base + (threadIdx.x & 31);
-        if (i < n) {
-            float4 o = sq.o[i], d = sq.d[i], c = sq.c[i];
-            const JobRec& J = jobs[__float_as_int(c.w)];
-            if (!trace_any<kCount>(J.scene, f3(o), f3(d), 1e-3f, d.w, st, overflow, &cnt)) {
-                // one path per pixel in flight: plain read-modify-write
-                float4* lp = J.lpath + __float_as_int(o.w);
+    trace_persistent<true, kCount>(
+        n, &ctr->fetch_shadow, st, overflow, cnt,
+        [&](int64_t i, TravState& s, Stack& stk) {
+            float4 o = sq.o[i], d = sq.d[i];
+            const SceneView& S = jobs[__float_as_int(sq.c[i].w)].scene;
+            trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, d.w, stk);
+        },
+        [&](int64_t i, const TravState& s) {
+            if (s.tri < 0) {
+                // unoccluded; one path per pixel in flight: plain read-modify-write
+                float4 o = sq.o[i], c = sq.c[i];
+                float4* lp = jobs[__float_as_int(c.w)].lpath + __float_as_int(o.w);
                 float4 l = *lp;
                 *lp = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.0f);
             }
-        }
-    }
+        });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
     if (kCount && (cnt.nodes | cnt.tris)) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_nodes), (unsigned long long)cnt.nodes);
@@ -486,6 +550,24 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
             pix = e.y;
             const JobRec& J = jobs[job];
             float4 l = J.lpath[pix];
+            const CacheRec& Cc = J.cache;
+            if (Cc.w && (pix % Cc.train_stride) == Cc.train_phase && J.spp_done[pix] == 0) {
+                // targets of the recorded vertices: radiance gathered after the
+                // vertex divided by the throughput that arrived there
+                const int ts = pix / Cc.train_stride;
+                const int nv = Cc.t_len[ts];
+                const bool ok = isfinite(l.x) && isfinite(l.y) && isfinite(l.z);
+                for (int k = 0; k < nv; ++k) {
+                    float4* ax = Cc.t_aux + 2 * ((size_t)ts * kTrainVertices + k);
+                    float4 b = ax[0], before = ax[1];
+                    bool valid = ok && b.x > 1e-6f && b.y > 1e-6f && b.z > 1e-6f;
+                    float4 tgt = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (valid)
+                        tgt = make_float4(fmaxf(l.x - before.x, 0.0f) / b.x, fmaxf(l.y - before.y, 0.0f) / b.y,
+                                          fmaxf(l.z - before.z, 0.0f) / b.z, 1.0f);
+                    ax[1] = tgt;
+                }
+            }
             if (isfinite(l.x) && isfinite(l.y) && isfinite(l.z)) {
                 float4 f = J.film[pix];
                 float s = (float)J.spp;
@@ -523,8 +605,13 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
     }
 }
 
-__global__ void k_advance(Counters* c)
+__global__ void k_advance(Counters* c, const JobRec* __restrict__ jobs, int max_jobs)
 {
+    for (int j = 0; j < max_jobs; ++j)
+        if (jobs[j].cache.q_count) {
+            jobs[j].cache.q_count[4] += jobs[j].cache.q_count[0];  // queries of the frame
+            jobs[j].cache.q_count[0] = 0;
+        }
     c->closest_total += c->n_cur;
     c->shadow_total += c->n_shadow;
     c->iterations += 1;
@@ -601,6 +688,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     jobs_ = (JobRec*)take(sizeof(JobRec) * max_jobs);
     pixels_done_ = (int32_t*)take(4 * (size_t)max_jobs);
     SRT_CUDA_TRY(cudaMemset(counters_, 0, sizeof(Counters)));
+    SRT_CUDA_TRY(cudaMemset(jobs_, 0, sizeof(JobRec) * (size_t)max_jobs));  // unused slots read as plain, empty jobs
     SRT_CUDA_TRY(cudaMemset(pixels_done_, 0, 4 * (size_t)max_jobs));
     SRT_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&host_counters_), sizeof(Counters)));
     SRT_CUDA_TRY(cudaStreamCreateWithFlags(&graph_stream_, cudaStreamNonBlocking));
@@ -653,12 +741,20 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof)
     else
         k_shadow<false><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
     mark(2, 1);
+    if (cache_) launch_cache_queries(jobs_, max_jobs_, st);
     mark(3, 0);
     k_regen<<<grid_stride_, kThreads, 0, st>>>(jobs_, done_, nxt, counters_, capacity_);
     mark(3, 1);
     mark(4, 0);
-    k_advance<<<1, 1, 0, st>>>(counters_);
+    k_advance<<<1, 1, 0, st>>>(counters_, jobs_, max_jobs_);
     mark(4, 1);
+}
+
+void Engine::drop_graphs()
+{
+    if (graph_) cudaGraphExecDestroy(graph_);
+    if (graph_prof_) cudaGraphExecDestroy(graph_prof_);
+    graph_ = graph_prof_ = nullptr;
 }
 
 srt_status Engine::capture(bool prof)
@@ -793,18 +889,6 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
 // srt_pt: the PathTracer pass (src/passes/integrator/path_tracer.{h,cu})
 // ---------------------------------------------------------------------------
 using namespace srt;
-
-struct srt_pt {
-    srt_scene* scene = nullptr;
-    int width = 0, height = 0;
-    Engine engine;
-    DeviceBuffer job_buf;
-    float4* lpath = nullptr;
-    uint4* rng_a = nullptr;
-    uint2* rng_b = nullptr;
-    int32_t* spp_done = nullptr;
-    srt_pt_stats stats{};
-};
 
 extern "C" srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t height, srt_pt** out)
 {

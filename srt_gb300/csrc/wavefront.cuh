@@ -14,8 +14,28 @@
 
 #include "common.h"
 #include "device_types.h"
+#include "mlp.cuh"
 
 namespace srt {
+
+// Radiance-cache state of a job (all null: a plain job).  Non-training
+// pixels end their paths at the second vertex with a network query; one
+// pixel in `train_stride` (offset `train_phase`) traces a full path and
+// records up to 8 vertices whose targets are computed when it ends.
+struct CacheRec {
+    const __nv_bfloat16* w;   // network weights (bf16); null = plain job
+    MlpBox box;
+    float4* q_rec;            // [npix * 4] query records
+    float4* q_beta;           // [npix] throughput (rgb), pixel (int bits)
+    int32_t* q_count;         // queries this iteration; [1] fallback queries (total)
+    const uint8_t* region_off;  // [res^3]: 1 = cache disabled in the cell (plain fallback)
+    int32_t region_res;
+    int32_t train_stride, train_phase, n_train;
+    float4* t_rec;            // [n_train * 8 * 4] records of training vertices
+    float4* t_aux;            // [n_train * 8 * 2]: (beta, -), (radiance before -> target, valid)
+    int32_t* t_len;           // [n_train] recorded vertices
+};
+constexpr int kTrainVertices = 8;
 
 // Per-job record read by every kernel (one per admitted render).
 struct JobRec {
@@ -30,6 +50,7 @@ struct JobRec {
     int32_t* frame_done;   // [spp]: pixels that finished sample k (progressive frames), or null
     int32_t width, height, npix;
     int32_t spp, max_depth, rr_depth, use_nee, use_mis, seed, flags, rng_mode;
+    CacheRec cache;
 };
 
 struct PathQueue {
@@ -60,6 +81,9 @@ struct KernelTimes {
     long long launches = 0;          // every kernel the engine launched
 };
 
+// Launches the radiance-cache query kernel over every job's queries (mlp.cu).
+void launch_cache_queries(const JobRec* jobs, int max_jobs, cudaStream_t st);
+
 // Device state of one wavefront engine (queues sized for `capacity` paths).
 class Engine {
 public:
@@ -81,11 +105,20 @@ public:
     int32_t* pixels_done_slot(int job) const { return pixels_done_ + job; }
     const int32_t* pixels_done_all() const { return pixels_done_; }
     void set_profiling(bool on) { profile_ = on; }
+    // adds the radiance-cache query kernel to the iteration (re-captures the graph)
+    void enable_cache()
+    {
+        if (!cache_) {
+            cache_ = true;
+            drop_graphs();
+        }
+    }
     bool profiling() const { return profile_; }
     KernelTimes& times() { return times_; }
 
 private:
     srt_status capture(bool profile);
+    void drop_graphs();
     void launch_iteration(int parity, cudaStream_t st, bool profile);
 
     int64_t capacity_ = 0;
@@ -104,8 +137,27 @@ private:
     cudaStream_t graph_stream_ = nullptr;
     cudaEvent_t ev_[2][5][2] = {};
     bool profile_ = false;
+    bool cache_ = false;
     KernelTimes times_;
     int grid_persist_ = 0, grid_stride_ = 0;
 };
 
 }  // namespace srt
+
+// The PathTracer pass: one engine, one job (srt_pt_* in wavefront.cu; the
+// cached variant in cache.cu).
+struct srt_pt {
+    srt_scene* scene = nullptr;
+    int width = 0, height = 0;
+    srt::Engine engine;
+    srt::DeviceBuffer job_buf;
+    float4* lpath = nullptr;
+    uint4* rng_a = nullptr;
+    uint2* rng_b = nullptr;
+    int32_t* spp_done = nullptr;
+    srt_pt_stats stats{};
+    srt::DeviceBuffer cache_buf;  // radiance-cache buffers, sized on first cached render
+    int64_t cache_train = 0;
+    int cache_res = 0;
+    int64_t frame = 0;
+};
