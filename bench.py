@@ -99,6 +99,16 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def dist_max(x, world, device):
+    """Largest value over the ranks (the slowest rank's time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def build_scene(S):
     arrays = S.procedural("spheres", seed=SEED, n_spheres=N_SPHERES, subdiv=SUBDIV)
     arrays.set_aspect(W / H)
@@ -168,6 +178,88 @@ def config_dict(info):
     return d
 
 
+def relmse(S, x, ref):
+    """Reference relMSE (metrics.h:30-34, largest 0.1 % dropped) on the GPU."""
+    import torch
+    return S.film_metric(torch.from_numpy(x).cuda(), torch.from_numpy(ref).cuda(), S.METRIC_RELMSE, 0.1)
+
+
+def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_spp=64):
+    """Learned-cache workload: 1280x720, 1 spp per frame for `frames` frames
+    with online training on 2^16 paths per frame; relMSE of the accumulated
+    image against a 4096-spp plain render accumulated in FP64, and the wall
+    time the cached form needs to reach the plain tracer's 64-spp relMSE."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    arrays.set_aspect(w / h)
+    S.check(S.lib().srt_scene_set_camera(scene.handle, C.byref(arrays.camera)))
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    plain = S.PathTracer(scene, w, h)
+    # reference: 64 frames x 64 spp accumulated in FP64
+    acc = np.zeros((w * h, 4), np.float64)
+    for f in range(ref_frames):
+        plain.render(film, S.pt_params(ref_spp, MAX_DEPTH, RR_DEPTH, 1, 1, 50000 + f))
+        torch.cuda.synchronize()
+        acc += film.cpu().numpy()
+    ref = (acc / ref_frames).astype(np.float32)
+    # plain 64 spp: relMSE and wall time
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain.render(film, S.pt_params(64, MAX_DEPTH, RR_DEPTH, 1, 1, 777))
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    rel_plain = relmse(S, film.cpu().numpy(), ref)
+    # cached: progressive 1-spp frames, network trained online
+    verts = np.concatenate([m["vertices"] for m in arrays.meshes])
+    lo, hi = verts.min(0) - 0.05, verts.max(0) + 0.05
+    mlp = C.c_void_p()
+    S.check(S.lib().srt_mlp_create(1, C.byref(mlp)))
+    S.check(S.lib().srt_mlp_set_box(mlp, (C.c_float * 3)(*lo), (C.c_float * 3)(*hi)))
+    pt = S.PathTracer(scene, w, h)
+    cp = S._capi.CacheParams(1 << 16, 4, 1e-2, 0.5, 16, 1)
+    st = S._capi.CacheStats()
+    accd = torch.zeros((w * h, 4), dtype=torch.float64, device="cuda")
+    t_total, t_reach, curve = 0.0, None, []
+    queries = fallback = 0
+    for f in range(frames):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p = S.pt_params(1, MAX_DEPTH, RR_DEPTH, 1, 1, 9000 + f)
+        S.check(S.lib().srt_pt_render_cached(pt.handle, C.c_void_p(film.data_ptr()), C.byref(p), mlp,
+                                             C.byref(cp), C.byref(st), None))
+        accd += film.double()
+        torch.cuda.synchronize()
+        t_total += time.perf_counter() - t0
+        queries += st.queries
+        fallback += st.fallback_queries
+        if (f + 1) in (1, 2, 4, 8, 16, 32, 64, 128, 256) or (t_reach is None and (f + 1) % 8 == 0):
+            r = relmse(S, (accd / (f + 1)).float().cpu().numpy(), ref)
+            curve.append((f + 1, round(t_total, 4), r))
+            if t_reach is None and r <= rel_plain:
+                t_reach = t_total
+    S.lib().srt_mlp_destroy(mlp)
+    arrays.set_aspect(W / H)
+    S.check(S.lib().srt_scene_set_camera(scene.handle, C.byref(arrays.camera)))
+    return {"workload": f"{w}x{h}, 1 spp/frame x {frames} frames, online training on 2^16 paths/frame",
+            "reference": f"{ref_frames * ref_spp}-spp plain render accumulated in FP64",
+            "plain_64spp": {"relmse": rel_plain, "wall_s": round(t_plain, 4)},
+            "cached": {"relmse_final": curve[-1][2], "wall_s": round(t_total, 4), "frames": frames,
+                       "relmse_curve": curve,
+                       "fallback_fraction": round(fallback / max(1, queries + fallback), 4)},
+            "time_to_plain64_relmse_s": None if t_reach is None else round(t_reach, 4),
+            "speedup_vs_plain64": None if t_reach is None else round(t_plain / t_reach, 3)}
+
+
+def serving_eval(S, scene_big, rate=20.0, duration=10.0):
+    """Short serving run (Poisson arrivals at `rate` jobs/s for `duration` s)."""
+    from srt_gb300 import serve_bench as SB
+    scenes = SB.build_scenes(S, n_variants=1, cache_frames=30)
+    out = SB.run_rate(S, scenes, rate, duration)
+    out["mix"] = "res {256^2,512^2,1024^2,1920x1080} x spp {1,4,16,64} x {cornell, 5.2M spheres} x {plain, cached}"
+    return out
+
+
 def profile_case():
     """The benchmark scene (392 MB resident, larger than L2) at 1920x1080
     with 1 spp, two frames: the first closest-hit launch traces one camera
@@ -194,6 +286,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cache", action="store_true", help="skip the learned-cache workload")
+    ap.add_argument("--no-serving", action="store_true", help="skip the short serving run")
     ap.add_argument("--profile-case", action="store_true",
                     help="short run of the same scene (1 spp, two frames) for ncu captures")
     args = ap.parse_args()
@@ -249,10 +343,7 @@ def main():
         ev1.record()
         barrier()
     ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
+    ms = dist_max(ms, world, dev)
     samples = W * H * SPP * args.steps * world
     value = samples / (ms / 1e3) / 1e6
     clocks = clk.summary()
@@ -270,10 +361,7 @@ def main():
         torch.cuda.current_stream().synchronize()
     barrier()
     e2e_s = time.perf_counter() - t0
-    t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = samples / float(t.item()) / 1e6
+    e2e_value = samples / dist_max(e2e_s, world, dev) / 1e6
 
     # ---- one profiled frame: per-kernel times and traversal traffic -----
     pt.set_profiling(True)
@@ -320,6 +408,12 @@ def main():
                               "closest_rays": st["closest_rays"], "shadow_rays": st["shadow_rays"],
                               "iterations": st["iterations"]},
         }
+        if not args.no_cache:
+            line["cache"] = cache_eval(S, arrays, scene)
+        if not args.no_serving:
+            line["serving"] = serving_eval(S, scene)
+            line["p50_job_latency_s"] = line["serving"]["p50_job_s"]
+            line["p99_job_latency_s"] = line["serving"]["p99_job_s"]
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(arrays, steps=1, budget_s=20.0)
         print(json.dumps(line), flush=True)

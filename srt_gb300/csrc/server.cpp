@@ -154,10 +154,14 @@ struct srt_server {
         return SRT_OK;
     }
 
-    void retire(Job& j, double t)
+    srt_status retire(Job& j, double t)
     {
         j.state = SRT_JOB_DONE;
         j.done_s = t;
+        // Empty the slot's device record before its state is freed: the cache
+        // kernels walk every slot and would otherwise reach the freed (and
+        // soon reused) query counters and records of a cached job.
+        srt_status st = engine.set_job(j.slot, JobRec{}, stream);
         if (j.state_buf) cudaFreeAsync(j.state_buf, stream);
         j.state_buf = nullptr;
         slots[j.slot] = 0;
@@ -167,6 +171,7 @@ struct srt_server {
             scene_refs.erase(j.desc.scene);
             bytes_used -= scene_bytes(j.desc.scene);
         }
+        return st;
     }
 };
 
@@ -286,7 +291,7 @@ extern "C" srt_status srt_server_step(srt_server* s, int32_t* running, int32_t* 
                 j.frame_times.push_back(t);
             }
             off += (size_t)spp;
-            if (s->h_pixels_done[k] >= j.npix) s->retire(j, t);
+            if (s->h_pixels_done[k] >= j.npix) SRT_TRY(s->retire(j, t));
         }
     }
     if (running) {

@@ -48,7 +48,7 @@ def _reference(S, scene, cuda, frames=32, spp=128):
 
 def _cached_frame(S, pt, film, mlp, seed, train=1, stats=None):
     p = pt_params(1, 8, 3, 1, 1, seed)
-    cp = S._capi.CacheParams(4096, 4, 1e-2, 0.5, 8, train)
+    cp = S._capi.CacheParams(256, 4, 1e-2, 0.5, 8, train)  # one training pixel in 16
     st = S._capi.CacheStats()
     S.check(S.lib().srt_pt_render_cached(pt.handle, C.c_void_p(film.data_ptr()), C.byref(p), mlp, C.byref(cp),
                                          C.byref(st), None))

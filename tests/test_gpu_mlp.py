@@ -5,7 +5,7 @@ in FP32; the oracle evaluates the same network in FP64 on the BF16-rounded
 weights.  Tolerances follow from BF16's 8-bit mantissa: outputs within
 5 % (|log ratio| < 0.05) for 99 % of queries; weight gradients within 5 %
 (cosine > 0.999) of an FP64 evaluation that rounds where the kernels round,
-and cosine > 0.99 (0.8 for the first layer) against the exact FP64 gradient.
+and cosine > 0.99 against the exact FP64 gradient.
 """
 import ctypes as C
 
@@ -62,8 +62,8 @@ def test_inference_matches_fp64(cuda):
     ws = [M.bf16(w) for w in M.split(_params(S, h))]
     rec = _records(5000, 1)
     out = torch.zeros((5000, 4), dtype=torch.float32, device=cuda)
-    S.check(S.lib().srt_mlp_infer(h, C.c_void_p(torch.from_numpy(rec).to(cuda).data_ptr()), 5000,
-                                  C.c_void_p(out.data_ptr()), None))
+    rec_d = torch.from_numpy(rec).to(cuda)  # held until the kernel has run
+    S.check(S.lib().srt_mlp_infer(h, C.c_void_p(rec_d.data_ptr()), 5000, C.c_void_p(out.data_ptr()), None))
     torch.cuda.synchronize()
     got = out.cpu().numpy()[:, :3]
     want = M.predict(ws, M.encode(rec, LO, HI))
@@ -82,8 +82,10 @@ def test_gradient_matches_fp64(cuda):
     tgt = _target(rec)
     g = np.zeros(M.PARAMS, np.float32)
     loss = C.c_float()
-    S.check(S.lib().srt_mlp_gradient(h, C.c_void_p(torch.from_numpy(rec).to(cuda).data_ptr()),
-                                     C.c_void_p(torch.from_numpy(tgt).to(cuda).data_ptr()), n,
+    # device copies stay referenced across the call: a temporary's block would
+    # be handed to the next upload before the kernels read it
+    rec_d, tgt_d = torch.from_numpy(rec).to(cuda), torch.from_numpy(tgt).to(cuda)
+    S.check(S.lib().srt_mlp_gradient(h, C.c_void_p(rec_d.data_ptr()), C.c_void_p(tgt_d.data_ptr()), n,
                                      g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss), None))
     x = M.encode(rec, LO, HI)
     ol, og = M.loss_and_grad(ws, x, tgt)                       # exact FP64
@@ -99,10 +101,7 @@ def test_gradient_matches_fp64(cuda):
         cos, rel = cmp(gpu[l], eg[l])
         assert cos > 0.999 and rel < 0.05, ("bf16-emulating oracle", l, cos, rel)
         cos, rel = cmp(gpu[l], og[l])
-        # the first layer's gradient sums signed sin/cos features over the batch:
-        # BF16 rounding of inputs and dL/dz leaves a larger relative error after cancellation
-        need = 0.8 if l == 0 else 0.99
-        assert cos > need, ("exact oracle", l, cos, rel)
+        assert cos > 0.99, ("exact oracle", l, cos, rel)
     S.lib().srt_mlp_destroy(h)
 
 
@@ -116,16 +115,16 @@ def test_training_reduces_loss(cuda):
         rec = _records(n, 100 + step)
         tgt = _target(rec)
         loss = C.c_float()
-        S.check(S.lib().srt_mlp_train_step(h, C.c_void_p(torch.from_numpy(rec).to(cuda).data_ptr()),
-                                           C.c_void_p(torch.from_numpy(tgt).to(cuda).data_ptr()), n, 1e-2,
+        rec_d, tgt_d = torch.from_numpy(rec).to(cuda), torch.from_numpy(tgt).to(cuda)
+        S.check(S.lib().srt_mlp_train_step(h, C.c_void_p(rec_d.data_ptr()), C.c_void_p(tgt_d.data_ptr()), n, 1e-2,
                                            C.byref(loss), None))
         losses.append(loss.value)
     assert np.mean(losses[-20:]) < 0.2 * np.mean(losses[:5]), (losses[:5], losses[-5:])
     # held-out queries: the trained network predicts the function
     rec = _records(4000, 7)
     out = torch.zeros((4000, 4), dtype=torch.float32, device=cuda)
-    S.check(S.lib().srt_mlp_infer(h, C.c_void_p(torch.from_numpy(rec).to(cuda).data_ptr()), 4000,
-                                  C.c_void_p(out.data_ptr()), None))
+    rec_d = torch.from_numpy(rec).to(cuda)
+    S.check(S.lib().srt_mlp_infer(h, C.c_void_p(rec_d.data_ptr()), 4000, C.c_void_p(out.data_ptr()), None))
     torch.cuda.synchronize()
     rel = np.abs(out.cpu().numpy()[:, :3] - _target(rec)[:, :3]) / _target(rec)[:, :3]
     assert np.median(rel) < 0.1

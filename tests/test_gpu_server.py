@@ -131,3 +131,34 @@ def test_jobs_arriving_while_others_run(cuda):
     assert b["admit_s"] < a["done_s"]  # admitted while the first job was still on the GPU
     np.testing.assert_array_equal(F.host(f2), _alone(S, sc2, 48, 48, pt_params(4, 16, 4, 1, 1, 8), cuda))
     np.testing.assert_array_equal(F.host(f1), _alone(S, sc1, 48, 48, pt_params(32, 8, 3, 1, 1, 7), cuda))
+
+
+def test_slot_of_a_finished_cached_job_is_emptied(cuda):
+    """A cached job finishes and frees its state; jobs admitted after it
+    reuse that memory and the freed slot.  The cache kernels visit every
+    slot, so the finished job's record must no longer point at its state:
+    the later plain job's film stays bit-identical to a lone render and the
+    later cached job completes with finite pixels."""
+    import srt_gb300 as S
+    cornell, _ = _scenes(S)
+    cornell.set_aspect(1.0)
+    scene = S.Scene(cornell)
+    mlp = C.c_void_p()
+    S.check(S.lib().srt_mlp_create(3, C.byref(mlp)))
+    S.check(S.lib().srt_mlp_set_box(mlp, (C.c_float * 3)(-1.05, -1.05, -1.05), (C.c_float * 3)(1.05, 1.05, 1.05)))
+    srv = S.Server(hbm_budget_bytes=4 << 30, max_paths=1 << 14, max_jobs=2, iterations_per_step=2)
+    F = Films(cuda)
+    fa, fb, fc = F.new(64 * 64), F.new(64 * 64), F.new(64 * 64)
+    a = srv.submit(scene, 64, 64, pt_params(2, 8, 3, 1, 1, 21), film=fa, cache=mlp)
+    srv.drain(300)
+    assert srv.info(a)["state"] == 2
+    b = srv.submit(scene, 64, 64, pt_params(4, 8, 3, 1, 1, 22), film=fb)
+    c = srv.submit(scene, 64, 64, pt_params(3, 8, 3, 1, 1, 23), film=fc, cache=mlp)
+    srv.drain(300)
+    assert srv.info(b)["state"] == 2 and srv.info(c)["state"] == 2
+    np.testing.assert_array_equal(F.host(fb), _alone(S, scene, 64, 64, pt_params(4, 8, 3, 1, 1, 22), cuda))
+    for f in (fa, fc):
+        img = F.host(f)
+        assert np.all(np.isfinite(img)) and np.all(img[:, 3] == 1.0)
+    del srv
+    S.lib().srt_mlp_destroy(mlp)
