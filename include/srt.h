@@ -344,7 +344,10 @@ typedef struct srt_cache_stats {
     int64_t fallback_queries; /* second vertices in disabled cells (traced plainly)     */
     int64_t train_vertices;   /* training vertices gathered this frame                 */
     float loss;               /* mean relative L2 loss of this frame's Adam steps      */
-    int32_t disabled_cells;   /* cells whose measured bias exceeds the threshold        */
+    int32_t disabled_cells;   /* cells traced plainly next frame (unmeasured, or bias
+                                 shown above the threshold)                            */
+    float trace_ms;           /* host time of the frame's wavefront run                */
+    float train_ms;           /* host time of gathering, cell statistics and Adam steps */
 } srt_cache_stats;
 
 srt_status srt_pt_render_cached(srt_pt* pt, float* film, const srt_pt_params* params, srt_mlp* mlp,

@@ -108,7 +108,8 @@ class CacheParams(C.Structure):
 
 class CacheStats(C.Structure):
     _fields_ = [("queries", C.c_int64), ("fallback_queries", C.c_int64), ("train_vertices", C.c_int64),
-                ("loss", C.c_float), ("disabled_cells", C.c_int32)]
+                ("loss", C.c_float), ("disabled_cells", C.c_int32), ("trace_ms", C.c_float),
+                ("train_ms", C.c_float)]
 
 
 class BxdfBatch(C.Structure):

@@ -7,10 +7,12 @@
 // that reached it, is that vertex's training target (the estimator of the
 // NeuralRadiosity RHS pass, src/shader/npr/nr_rhs.cu:50-157, trained online
 // instead of offline).  After the frame the targets are gathered, the
-// network's relative bias is measured per cell of a coarse grid (cells
-// whose bias exceeds the threshold fall back to plain tracing for the next
-// frame) and the network takes a few Adam steps.
+// network's relative bias is measured per cell of a coarse grid (cells not
+// yet measured, or whose bias is shown to exceed the threshold, fall back
+// to plain tracing for the next frame) and the network takes a few Adam
+// steps.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -37,7 +39,10 @@ struct CacheBuffers {
     float4* b_rec;
     float4* b_tgt;
     float4* b_pred;
+    float* loss_hist;  // loss of each Adam step of the frame
 };
+
+constexpr int kMaxTrainSteps = 64;
 
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -64,6 +69,7 @@ CacheBuffers carve(char* base, int64_t npix, int64_t n_train, int res)
     b.b_rec = (float4*)take(nv * 64);
     b.b_tgt = (float4*)take(nv * 16);
     b.b_pred = (float4*)take(nv * 16);
+    b.loss_hist = (float*)take(kMaxTrainSteps * 4);
     return b;
 }
 
@@ -72,7 +78,8 @@ size_t carve_bytes(int64_t npix, int64_t n_train, int res)
     const size_t cells = (size_t)res * res * res;
     const size_t nv = (size_t)n_train * kTrainVertices;
     return a256((size_t)npix * 64) + a256((size_t)npix * 16) + a256(64) + a256(cells) + 2 * a256(cells * 16) +
-           a256(nv * 64) + a256(nv * 32) + a256((size_t)n_train * 4) + a256(nv * 64) + 2 * a256(nv * 16) + 256;
+           a256(nv * 64) + a256(nv * 32) + a256((size_t)n_train * 4) + a256(nv * 64) + 2 * a256(nv * 16) +
+           a256(kMaxTrainSteps * 4) + 256;
 }
 
 // valid training vertices -> contiguous (record, target) batch
@@ -99,19 +106,26 @@ __device__ __forceinline__ int cell_of(float4 p, MlpBox box, int r)
 
 __device__ __forceinline__ float lum(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
-// per-cell sums of predicted and target luminance over this frame's batch
+// per-cell sums of predicted luminance, target luminance, count and squared
+// target luminance over this frame's batch
 __global__ void k_region_sums(CacheBuffers b, const int32_t* count, MlpBox box, int res)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *count) return;
     int c = cell_of(b.b_rec[4 * (size_t)i], box, res);
+    float t = lum(b.b_tgt[i]);
     atomicAdd(&b.region_new[c].x, lum(b.b_pred[i]));
-    atomicAdd(&b.region_new[c].y, lum(b.b_tgt[i]));
+    atomicAdd(&b.region_new[c].y, t);
     atomicAdd(&b.region_new[c].z, 1.0f);
+    atomicAdd(&b.region_new[c].w, t * t);
 }
 
-// exponential moving averages per cell; a cell with enough samples whose
-// relative bias |pred - target| / target exceeds the threshold falls back
+// Exponential moving averages per cell.  A cell is served by the network
+// only once it holds 16 (weighted) samples and its measured relative bias
+// is not shown to exceed the threshold: |mean pred - mean target| minus two
+// standard errors of the target mean must stay below threshold * mean
+// target.  Unmeasured cells, including every cell before the first
+// training frame, are traced plainly.
 __global__ void k_region_update(CacheBuffers b, int cells, float threshold, float decay, int32_t* disabled)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -120,9 +134,15 @@ __global__ void k_region_update(CacheBuffers b, int cells, float threshold, floa
     s.x = decay * s.x + n.x;
     s.y = decay * s.y + n.y;
     s.z = decay * s.z + n.z;
+    s.w = decay * s.w + n.w;
     b.region_stat[c] = s;
     b.region_new[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool off = s.z > 16.0f && fabsf(s.x - s.y) > threshold * (s.y + 1e-3f * s.z);
+    bool off = true;
+    if (s.z >= 16.0f) {
+        float mp = s.x / s.z, mt = s.y / s.z;
+        float se = sqrtf(fmaxf(s.w / s.z - mt * mt, 0.0f) / s.z);
+        off = fabsf(mp - mt) - 2.0f * se > threshold * (mt + 1e-3f);
+    }
     b.region_off[c] = off ? 1 : 0;
     if (off) atomicAdd(disabled, 1);
 }
@@ -137,6 +157,7 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
     if (prm->samples_per_pixel <= 0 || prm->max_depth < 2 || prm->max_depth > 255 || prm->rng_mode != SRT_RNG_CURAND)
         return set_error(SRT_ERR_ARG, "cached rendering needs spp >= 1, 2 <= max_depth <= 255, curand streams");
     if (cp->train_paths <= 0 || cp->region_res <= 0 || cp->region_res > 64 || cp->train_steps < 0 ||
+        cp->train_steps > kMaxTrainSteps ||
         !(cp->learning_rate >= 0.0f))
         return set_error(SRT_ERR_ARG, "cache parameters out of range");
     if (reinterpret_cast<uintptr_t>(film) % 16) return set_error(SRT_ERR_ARG, "film must be 16-byte aligned");
@@ -151,6 +172,9 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
         SRT_CUDA_TRY(cudaMemset(p->cache_buf.get(), 0, p->cache_buf.bytes()));
         p->cache_train = n_train;
         p->cache_res = res;
+        // no cell has been measured: all trace plainly until the first training frame
+        CacheBuffers b0 = carve(p->cache_buf.as<char>(), npix, n_train, res);
+        SRT_CUDA_TRY(cudaMemset(b0.region_off, 1, (size_t)cells));
     }
     CacheBuffers b = carve(p->cache_buf.as<char>(), npix, n_train, res);
     srt_scene* sc = p->scene;
@@ -197,9 +221,11 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
     SRT_TRY(p->engine.set_job(0, J, st));
     SRT_TRY(p->engine.start_job(0, J, st));
     long long bound = (long long)prm->samples_per_pixel * (prm->max_depth + 1) + 16;
+    auto t0 = std::chrono::steady_clock::now();
     SRT_TRY(p->engine.run(st, 2 * bound, true, 0));
     Counters cnt;
     SRT_TRY(p->engine.read_counters(cnt, st));
+    auto t1 = std::chrono::steady_clock::now();
 
     srt_cache_stats out{};
     int32_t host_counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -219,18 +245,21 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
             SRT_CUDA_TRY(cudaGetLastError());
             const int steps = std::max(1, cp->train_steps);
             const int64_t slice = (nb + steps - 1) / steps;
-            float loss_sum = 0.0f;
             int used = 0;
             for (int s = 0; s < steps; ++s) {
                 int64_t b0 = s * slice, n = std::min(slice, nb - b0);
                 if (n <= 0) break;
                 SRT_TRY(mlp_train_launch(mlp, b.b_rec + 4 * b0, b.b_tgt + b0, n, cp->learning_rate, true, st));
-                float l = 0.0f;
-                SRT_CUDA_TRY(cudaMemcpyAsync(&l, mlp->loss, 4, cudaMemcpyDeviceToHost, st));
-                SRT_CUDA_TRY(cudaStreamSynchronize(st));
-                loss_sum += l;
+                SRT_CUDA_TRY(cudaMemcpyAsync(b.loss_hist + s, mlp->loss, 4, cudaMemcpyDeviceToDevice, st));
                 ++used;
             }
+            float losses[kMaxTrainSteps];
+            if (used) {
+                SRT_CUDA_TRY(cudaMemcpyAsync(losses, b.loss_hist, 4 * (size_t)used, cudaMemcpyDeviceToHost, st));
+                SRT_CUDA_TRY(cudaStreamSynchronize(st));
+            }
+            float loss_sum = 0.0f;
+            for (int s = 0; s < used; ++s) loss_sum += losses[s];
             out.loss = used ? loss_sum / (float)used : 0.0f;
             out.train_vertices = nb;
         }
@@ -240,6 +269,9 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
         SRT_CUDA_TRY(cudaMemcpyAsync(host_counts, b.q_count, 32, cudaMemcpyDeviceToHost, st));
     }
     SRT_CUDA_TRY(cudaStreamSynchronize(st));
+    auto t2 = std::chrono::steady_clock::now();
+    out.trace_ms = (float)std::chrono::duration<double, std::milli>(t1 - t0).count();
+    out.train_ms = (float)std::chrono::duration<double, std::milli>(t2 - t1).count();
     out.fallback_queries = host_counts[1];
     out.disabled_cells = host_counts[3];
     out.queries = host_counts[4];

@@ -21,7 +21,7 @@ constexpr int kStackEntries = 24;  // node groups; at most one per tree level
 
 // resident 128-thread traversal blocks per SM the compiler budgets registers for
 #ifndef SRT_TRACE_MIN_BLOCKS
-#define SRT_TRACE_MIN_BLOCKS 6
+#define SRT_TRACE_MIN_BLOCKS 7
 #endif
 
 struct Hit {
@@ -66,7 +66,9 @@ __device__ __forceinline__ RayPre make_ray(float3 o, float3 d)
                             fabsf(d.y) < tiny ? copysignf(tiny, d.y) : d.y,
                             fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z);
     r.idir = make_float3(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z);
-    r.oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    // octant = signs of idir (a -0 component counts as negative), so that the
+    // near slab plane of every child box is its low plane exactly when the bit is clear
+    r.oct = (r.idir.x < 0.0f ? 1u : 0u) | (r.idir.y < 0.0f ? 2u : 0u) | (r.idir.z < 0.0f ? 4u : 0u);
     return r;
 }
 
@@ -106,6 +108,21 @@ __device__ __forceinline__ uint32_t word4(uint4 v, int j)
     return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
 }
 
+// three-input minimum / maximum (one instruction on sm_100 and later; NaN
+// inputs are ignored as by fminf / fmaxf)
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // Stack of node groups in shared memory: entry e of thread `lane_id` is at
 // stack[e * stride + lane_id] (stride = threads per block: conflict-free).
 struct Stack {
@@ -137,8 +154,15 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     const uint4* np = reinterpret_cast<const uint4*>(nodes + ni);
     uint4 w0 = __ldg(np + 0);
     uint4 w1 = __ldg(np + 1);
-    uint4 qlx = __ldg(np + 2), qly = __ldg(np + 3), qlz = __ldg(np + 4);
-    uint4 qhx = __ldg(np + 5), qhy = __ldg(np + 6), qhz = __ldg(np + 7);
+    // low planes at lines 2..4, high planes at 5..7.  Along an axis where the
+    // ray's idir is negative the high plane is the near one: loading the
+    // planes in near/far order replaces the per-child min/max of the two slab
+    // distances (fmaf is monotonic in the quantised coordinate, so the
+    // selected value equals that min/max exactly).
+    const int ox = (int)(r.oct & 1u), oy = (int)((r.oct >> 1) & 1u), oz = (int)(r.oct >> 2);
+    uint4 nqx = __ldg(np + 2 + 3 * ox), fqx = __ldg(np + 5 - 3 * ox);
+    uint4 nqy = __ldg(np + 3 + 3 * oy), fqy = __ldg(np + 6 - 3 * oy);
+    uint4 nqz = __ldg(np + 4 + 3 * oz), fqz = __ldg(np + 7 - 3 * oz);
     int ex = (int)(int8_t)(w0.w & 0xffu);
     int ey = (int)(int8_t)((w0.w >> 8) & 0xffu);
     int ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
@@ -155,11 +179,11 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     for (int s = 0; s < 8; ++s) {
         uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * (s & 3))) & 0xffu;
         int j = s >> 1, hi = s & 1;
-        float tx0 = fmaf(u16f(word4(qlx, j), hi), Ax, Bx), tx1 = fmaf(u16f(word4(qhx, j), hi), Ax, Bx);
-        float ty0 = fmaf(u16f(word4(qly, j), hi), Ay, By), ty1 = fmaf(u16f(word4(qhy, j), hi), Ay, By);
-        float tz0 = fmaf(u16f(word4(qlz, j), hi), Az, Bz), tz1 = fmaf(u16f(word4(qhz, j), hi), Az, Bz);
-        float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-        float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+        float nx = fmaf(u16f(word4(nqx, j), hi), Ax, Bx), fx = fmaf(u16f(word4(fqx, j), hi), Ax, Bx);
+        float ny = fmaf(u16f(word4(nqy, j), hi), Ay, By), fy = fmaf(u16f(word4(fqy, j), hi), Ay, By);
+        float nz = fmaf(u16f(word4(nqz, j), hi), Az, Bz), fz = fmaf(u16f(word4(fqz, j), hi), Az, Bz);
+        float tn = fmax3(nx, ny, fmaxf(nz, tmin));
+        float tf = fmin3(fx, fy, fminf(fz, tmax));
         bool hit = meta != 0u && tn <= tf * 1.00000024f;
         if (hit) {
             if (meta & 0x80u) {
@@ -243,8 +267,14 @@ __device__ __forceinline__ Hit trace_closest(const SceneView& S, float3 o, float
 // the efficiency of ray traversal on GPUs", HPG 2009), so lanes do not idle
 // until the slowest ray of a fixed batch ends.
 // ---------------------------------------------------------------------------
-constexpr int kRefill = 8;
-constexpr int kStepBudget = 4;  // node visits per lane between refill checks
+#ifndef SRT_TRACE_REFILL
+#define SRT_TRACE_REFILL 8
+#endif
+#ifndef SRT_TRACE_STEPS
+#define SRT_TRACE_STEPS 4
+#endif
+constexpr int kRefill = SRT_TRACE_REFILL;     // idle lanes that trigger a fetch
+constexpr int kStepBudget = SRT_TRACE_STEPS;  // node visits per lane between refill checks
 
 struct TravState {
     RayPre r;

