@@ -178,6 +178,19 @@ def config_dict(info):
     return d
 
 
+def measured_traffic(kernel, rays_per_launch):
+    """DRAM bytes per launch of `kernel` scaled from one ncu capture: the
+    per-ray dram__bytes_read.sum + dram__bytes_write.sum of a captured launch
+    (profiles/<kernel>_dram.json, written from the capture) times the rays of
+    an average benchmark launch."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_dram.json")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as f:
+        d = json.load(f)
+    return int(d["dram_bytes_per_ray"] * rays_per_launch), d["capture"]
+
+
 def relmse(S, x, ref):
     """Reference relMSE (metrics.h:30-34, largest 0.1 % dropped) on the GPU."""
     import torch
@@ -261,22 +274,30 @@ def serving_eval(S, scene_big, rate=20.0, duration=10.0):
 
 
 def profile_case():
-    """The benchmark scene (392 MB resident, larger than L2) at 1920x1080
-    with 1 spp, two frames: the first closest-hit launch traces one camera
-    ray per pixel (2.07M rays), a few hundred launches in all, for ncu."""
+    """The benchmark scene (392 MB resident, larger than L2) at 1920x1080,
+    for ncu.  Frame A: 1 spp with max depth 2, so the first closest-hit
+    launch traces the 2,073,600 camera rays and the second the first-bounce
+    rays (their count is printed), the first shadow launch the NEE rays of
+    the primary hits.  Frame B: 1 spp at the benchmark's depth.  A few
+    hundred launches in all; run it with SRT_NO_GRAPH=1 so that ncu sees the
+    same kernels as separate launches."""
     import torch
     import srt_gb300 as S
     arrays = build_scene(S)
     scene = S.Scene(arrays)
     pt = S.PathTracer(scene, W, H)
     film = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
-    for seed in range(2):
-        pt.render(film, S.pt_params(1, MAX_DEPTH, RR_DEPTH, 1, 1, seed))
+    pt.render(film, S.pt_params(1, 2, RR_DEPTH, 1, 1, 0))
     torch.cuda.synchronize()
-    st = pt.stats()
-    print(json.dumps({"profile_case": "1920x1080x1spp", "closest_rays": st["closest_rays"],
-                      "shadow_rays": st["shadow_rays"], "iterations": st["iterations"],
-                      "kernel_launches": st["kernel_launches"]}))
+    a = pt.stats()
+    pt.render(film, S.pt_params(1, MAX_DEPTH, RR_DEPTH, 1, 1, 1))
+    torch.cuda.synchronize()
+    b = pt.stats()
+    print(json.dumps({"profile_case": "1920x1080x1spp",
+                      "frame_a": {"max_depth": 2, "camera_rays": W * H,
+                                  "bounce_rays": a["closest_rays"] - W * H, "shadow_rays": a["shadow_rays"]},
+                      "frame_b": {"max_depth": MAX_DEPTH, "closest_rays": b["closest_rays"],
+                                  "shadow_rays": b["shadow_rays"], "iterations": b["iterations"]}}))
 
 
 def main():
@@ -363,14 +384,19 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_value = samples / dist_max(e2e_s, world, dev) / 1e6
 
-    # ---- one profiled frame: per-kernel times and traversal traffic -----
-    pt.set_profiling(True)
+    # ---- two profiled frames of the same seed (identical rays): one with
+    # the counting traversal kernels for the work per ray, one with event
+    # timestamps around the production kernels for their durations -------
     params.seed = SEED + 900
+    pt.set_profiling(1)
     pt.render(film, params, stream)
     st = pt.stats()
-    pt.set_profiling(False)
+    pt.set_profiling(2)
+    pt.render(film, params, stream)
+    st_t = pt.stats()
+    pt.set_profiling(0)
     names = ["k_closest", "k_shade", "k_shadow", "k_regen", "k_advance"]
-    kms = dict(zip(names, st["kernel_ms"]))
+    kms = dict(zip(names, st_t["kernel_ms"]))
     top = max(kms, key=kms.get)
     # algorithmic bytes: per ray the ray (24 B) in and the hit (16 B) out, plus
     # the BVH nodes (128 B) and triangles (48 B) the traversal fetches
@@ -382,6 +408,7 @@ def main():
         per_ray = 40
     alg_bytes = rays * per_ray + nodes * 128 + tris * 48
     iters = max(1, st["iterations"])
+    traffic, traffic_src = measured_traffic(top, rays / iters)
     achieved = alg_bytes / (kms[top] / 1e3) / 1e9 if kms[top] > 0 else 0.0
     peak, peak_kind = peaks()
 
@@ -395,11 +422,10 @@ def main():
             "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": W * H * 16},
             "gpu_launches": int(launches),
-            "mrays_per_s": round((st["closest_rays"] + st["shadow_rays"]) / (sum(st["kernel_ms"]) / 1e3) / 1e6, 1)
-            if sum(st["kernel_ms"]) > 0 else None,
+            "mrays_per_s": round((st["closest_rays"] + st["shadow_rays"]) / (ms / args.steps / 1e3) / 1e6, 1),
             "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": None, "launches": iters,
+                         "traffic": traffic, "traffic_source": traffic_src, "launches": iters,
                          "per_launch_ms": round(kms[top] / iters, 4),
                          "alg_bytes_per_launch": int(alg_bytes / iters),
                          "nodes_per_ray": round(nodes / max(rays, 1), 2),

@@ -227,9 +227,12 @@ srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t height, srt_pt
 srt_status srt_pt_render(srt_pt* pt, float* film, const srt_pt_params* params, void* stream);
 srt_status srt_pt_get_stats(const srt_pt* pt, srt_pt_stats* stats);
 /* Profiling switch (PROFILE() scopes of src/utils/profiler.h:219 applied per
- * kernel): when on, the iteration graph carries event records between the
- * kernels, the host reads them after every graph launch, and the traversal
- * kernels count their node visits.  Results land in srt_pt_stats. */
+ * kernel).  enable = 1: the iteration graph carries event records between
+ * the kernels, the host reads them after every graph launch, and the
+ * traversal kernels are the variants that count their node visits and
+ * triangle tests.  enable = 2: event records only, around kernels identical
+ * to the unprofiled ones (their durations are the production kernels').
+ * 0 turns profiling off.  Results land in srt_pt_stats. */
 srt_status srt_pt_set_profiling(srt_pt* pt, int32_t enable);
 void srt_pt_destroy(srt_pt* pt);
 

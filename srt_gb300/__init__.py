@@ -174,8 +174,9 @@ class PathTracer:
         out["kernel_ms"] = list(s.kernel_ms)
         return out
 
-    def set_profiling(self, on: bool):
-        check(lib().srt_pt_set_profiling(self.handle, int(on)))
+    def set_profiling(self, mode):
+        """0 off; 1 (or True) timestamps + traversal work counters; 2 timestamps only."""
+        check(lib().srt_pt_set_profiling(self.handle, int(mode)))
 
     def close(self):
         if self.handle:

@@ -105,7 +105,16 @@ public:
     srt_status read_counters(Counters& c, cudaStream_t st);
     int32_t* pixels_done_slot(int job) const { return pixels_done_ + job; }
     const int32_t* pixels_done_all() const { return pixels_done_; }
-    void set_profiling(bool on) { profile_ = on; }
+    // mode 0: off; 1: timestamps between the kernels and traversal work
+    // counters (counting kernel variants); 2: timestamps only, the kernels
+    // identical to the unprofiled ones
+    void set_profiling(int mode)
+    {
+        const bool count = mode == 1;
+        if (count != count_) drop_graphs();
+        profile_ = mode != 0;
+        count_ = count;
+    }
     // adds the radiance-cache query kernel to the iteration (re-captures the graph)
     void enable_cache()
     {
@@ -140,9 +149,10 @@ private:
     cudaStream_t graph_stream_ = nullptr;
     cudaEvent_t ev_[2][5][2] = {};
     bool profile_ = false;
+    bool count_ = true;
     bool cache_ = false;
     KernelTimes times_;
-    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0;
+    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0, grid_shade_ = 0;
 };
 
 }  // namespace srt
