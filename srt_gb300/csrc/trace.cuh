@@ -17,7 +17,16 @@
 
 namespace srt {
 
-constexpr int kStackEntries = 24;  // node groups; at most one per tree level
+#ifndef SRT_STACK_ENTRIES
+#define SRT_STACK_ENTRIES 24
+#endif
+constexpr int kStackEntries = SRT_STACK_ENTRIES;  // node groups; at most one per tree level
+
+// Node prefetch while a lane tests its leaf triangles: 0 none, 1 the next
+// node into L1, 2 the next node into L1 and the other hit children into L2.
+#ifndef SRT_TRACE_PREFETCH
+#define SRT_TRACE_PREFETCH 0
+#endif
 
 // resident 128-thread traversal blocks per SM the compiler budgets registers for
 #ifndef SRT_TRACE_MIN_BLOCKS
@@ -198,6 +207,9 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     tri_base = w1.y;
 }
 
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 __device__ __forceinline__ uint32_t group_next_node(uint2& g, uint32_t oct)
 {
     uint32_t hits = g.y >> 8;
@@ -335,12 +347,21 @@ __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overf
             cnt.nodes += 1;
             cnt.tris += __popc(s.tmask);
         }
+        if (SRT_TRACE_PREFETCH && s.tmask && (s.group.y >> 8) != 0u) {
+            // the leaf tests of this node come first: start fetching the next node
+            uint2 g = s.group;
+            prefetch_l1(s.nodes + group_next_node(g, s.r.oct));
+            if (SRT_TRACE_PREFETCH == 2)
+                while ((g.y >> 8) != 0u) prefetch_l2(s.nodes + group_next_node(g, s.r.oct));
+        }
     }
     return false;
 }
 
 // Drives a warp over rays [0, n) taken from *fetch.  load(i, state, stack)
-// starts ray i (calls trav_init); store(i, state) writes its result.
+// starts ray i (calls trav_init); store(i, state, fin) is called by all 32
+// lanes after every round (so it may use warp-wide votes and appends), with
+// fin set in the lanes whose ray i just finished.
 template <bool kAny, bool kCount, class Load, class Store>
 __device__ __forceinline__ void trace_persistent(int64_t n, unsigned long long* fetch, Stack& st, int& overflow,
                                                  TraceCount& cnt, Load load, Store store)
@@ -367,10 +388,9 @@ __device__ __forceinline__ void trace_persistent(int64_t n, unsigned long long* 
             idle = __ballot_sync(full, ray < 0);
         }
         if (idle == full && drained) break;
-        if (ray >= 0 && trav_advance<kAny, kCount>(s, st, overflow, cnt)) {
-            store(ray, s);
-            ray = -1;
-        }
+        const bool fin = ray >= 0 && trav_advance<kAny, kCount>(s, st, overflow, cnt);
+        store(ray, s, fin);
+        if (fin) ray = -1;
     }
 }
 

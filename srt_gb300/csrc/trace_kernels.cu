@@ -24,7 +24,8 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace_c
             float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
             trav_init(s, S.nodes, S.tris, f3(a), f3(b), a.w, b.w, stk);
         },
-        [&](int64_t i, const TravState& s) {
+        [&](int64_t i, const TravState& s, bool fin) {
+            if (!fin) return;
             int32_t prim = s.tri >= 0 ? __ldg(S.tri_prim + s.tri) : -1;
             hits[i] = make_float4(s.tmax, s.u, s.v, __int_as_float(prim));
         });
@@ -45,7 +46,9 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace_s
             float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
             trav_init(s, S.nodes, S.tris, f3(a), f3(b), a.w, b.w, stk);
         },
-        [&](int64_t i, const TravState& s) { visible[i] = s.tri >= 0 ? 0 : 1; });
+        [&](int64_t i, const TravState& s, bool fin) {
+            if (fin) visible[i] = s.tri >= 0 ? 0 : 1;
+        });
     if (overflow) atomicAdd(overflow_flag, 1);
 }
 

@@ -252,7 +252,8 @@ __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ j
 
 template <bool kCount>
 __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest(const JobRec* __restrict__ jobs, PathQueue q,
-                                                              float4* __restrict__ hits, Counters* ctr,
+                                                              float4* __restrict__ hits,
+                                                              int32_t* __restrict__ order, Counters* ctr,
                                                               int64_t capacity)
 {
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
@@ -268,7 +269,16 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
             const SceneView& S = jobs[__float_as_uint(q.beta[i].w) >> 16].scene;
             trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, 1e16f, stk);
         },
-        [&](int64_t i, const TravState& s) { hits[i] = make_float4(s.tmax, s.u, s.v, __int_as_float(s.tri)); });
+        [&](int64_t i, const TravState& s, bool fin) {
+            // shading order: hits from the front of `order`, misses from the
+            // back, so k_shade's warps see one kind of vertex (except at the seam)
+            const bool hit = fin && s.tri >= 0;
+            const int32_t h = warp_append(&ctr->n_hit, hit);
+            const int32_t m = warp_append(&ctr->n_miss, fin && !hit);
+            if (!fin) return;
+            hits[i] = make_float4(s.tmax, s.u, s.v, __int_as_float(s.tri));
+            order[hit ? h : (int32_t)(n - 1 - m)] = (int32_t)i;
+        });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
     if (kCount && (cnt.nodes | cnt.tris)) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_nodes), (unsigned long long)cnt.nodes);
@@ -288,14 +298,17 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
 constexpr int kShadeThreads = SRT_SHADE_THREADS;
 
 __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(const JobRec* __restrict__ jobs, PathQueue q,
-                                                    const float4* __restrict__ hits, PathQueue qn, ShadowQueue sq,
+                                                    const float4* __restrict__ hits,
+                                                    const int32_t* __restrict__ order, PathQueue qn, ShadowQueue sq,
                                                     int2* __restrict__ done, Counters* ctr, int64_t capacity)
 {
     const int n = (int)min((int64_t)ctr->n_cur, capacity);
     const int stride = gridDim.x * blockDim.x;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
-        const int i = base + (threadIdx.x & 31);
-        const bool valid = i < n;
+        // queue entries in k_closest's shading order: hits first, then misses
+        const int j = base + (threadIdx.x & 31);
+        const bool valid = j < n;
+        const int i = valid ? __ldg(order + j) : 0;
         bool push_next = false, push_shadow = false, terminate = false, push_query = false;
         float4 qrec[4];
         float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
@@ -518,8 +531,8 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_shadow(
             const SceneView& S = jobs[__float_as_int(sq.c[i].w)].scene;
             trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, d.w, stk);
         },
-        [&](int64_t i, const TravState& s) {
-            if (s.tri < 0) {
+        [&](int64_t i, const TravState& s, bool fin) {
+            if (fin && s.tri < 0) {
                 // unoccluded; one path per pixel in flight: plain read-modify-write
                 float4 o = sq.o[i], c = sq.c[i];
                 float4* lp = jobs[__float_as_int(c.w)].lpath + __float_as_int(o.w);
@@ -631,6 +644,8 @@ __global__ void k_advance(Counters* c, const JobRec* __restrict__ jobs, int max_
     c->n_done = 0;
     c->fetch_closest = 0;
     c->fetch_shadow = 0;
+    c->n_hit = 0;
+    c->n_miss = 0;
     c->run_iters += 1;
     if (kCond) {
         const bool again = c->n_cur > 0 && c->run_iters < c->run_limit && c->overflow_queue == 0 &&
@@ -684,7 +699,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     const size_t C = (size_t)capacity;
     size_t per_queue = align_up(C * 16) * 3 + align_up(C * 16) + align_up(C * 8);
     size_t total = 2 * per_queue + align_up(C * 16) * 3 /*shadow*/ + align_up(C * 16) /*hits*/ +
-                   align_up(C * 8) /*done*/ + align_up(sizeof(Counters)) + align_up(sizeof(JobRec) * max_jobs) +
+                   align_up(C * 4) /*order*/ + align_up(C * 8) /*done*/ + align_up(sizeof(Counters)) + align_up(sizeof(JobRec) * max_jobs) +
                    align_up(4 * (size_t)max_jobs);
     SRT_TRY(buf_.alloc(total, "wavefront queues"));
     bytes_ = total;
@@ -705,6 +720,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     sq_.d = (float4*)take(C * 16);
     sq_.c = (float4*)take(C * 16);
     hits_ = (float4*)take(C * 16);
+    order_ = (int32_t*)take(C * 4);
     done_ = (int2*)take(C * 8);
     counters_ = (Counters*)take(sizeof(Counters));
     jobs_ = (JobRec*)take(sizeof(JobRec) * max_jobs);
@@ -766,12 +782,13 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     };
     mark(0, 0);
     if (prof && count_)
-        k_closest<true><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+        k_closest<true><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, order_, counters_, capacity_);
     else
-        k_closest<false><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+        k_closest<false><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, order_, counters_, capacity_);
     mark(0, 1);
     mark(1, 0);
-    k_shade<<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, nxt, sq_, done_, counters_, capacity_);
+    k_shade<<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,
+                                                   capacity_);
     mark(1, 1);
     mark(2, 0);
     if (prof && count_)

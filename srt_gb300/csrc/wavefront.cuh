@@ -69,6 +69,7 @@ struct ShadowQueue {
 
 struct Counters {
     int32_t n_cur, n_next, n_shadow, n_done;
+    int32_t n_hit, n_miss;  // closest-hit results of the iteration, by kind
     unsigned long long fetch_closest, fetch_shadow;
     long long closest_total, shadow_total, iterations, started;
     long long c_nodes, c_tris, s_nodes, s_tris;  // traversal work (profiling kernels)
@@ -140,6 +141,7 @@ private:
     PathQueue q_[2]{};
     ShadowQueue sq_{};
     float4* hits_ = nullptr;
+    int32_t* order_ = nullptr;  // queue indices in shading order (hits, then misses)
     int2* done_ = nullptr;
     Counters* counters_ = nullptr;
     JobRec* jobs_ = nullptr;
