@@ -429,7 +429,9 @@ def main():
                          "per_launch_ms": round(kms[top] / iters, 4),
                          "alg_bytes_per_launch": int(alg_bytes / iters),
                          "nodes_per_ray": round(nodes / max(rays, 1), 2),
-                         "tris_per_ray": round(tris / max(rays, 1), 2)},
+                         "tris_per_ray": round(tris / max(rays, 1), 2),
+                         "shadow_nodes_per_ray": round(st["shadow_nodes"] / max(st["shadow_rays"], 1), 2),
+                         "shadow_tris_per_ray": round(st["shadow_tris"] / max(st["shadow_rays"], 1), 2)},
             "profile_frame": {"kernel_ms": {k: round(v, 2) for k, v in kms.items()},
                               "closest_rays": st["closest_rays"], "shadow_rays": st["shadow_rays"],
                               "iterations": st["iterations"]},

@@ -87,6 +87,28 @@ def test_disney_vs_fp64(cuda):
     assert np.median(r_gpu) < 1e-6
 
 
+def test_disney_local_frame_vs_fp64(cuda):
+    """With the shading frame exact (normal = +z, so world and local
+    coordinates coincide), the kernel's Disney f and pdf at its own sampled
+    direction are within 1e-5 relative of the FP64 evaluation of the same
+    formulas for at least 99 % of the points; the rest are peaked GTR2 lobes
+    (alpha down to 0.001) where one FP32 ulp in the half vector moves D by
+    more."""
+    normal, _, color, params, rnd4 = O.bxdf_inputs(7000, 1 << 16)
+    normal[:] = (0.0, 0.0, 1.0)
+    rng = np.random.default_rng(11)
+    wo = rng.normal(size=(len(normal), 3))
+    wo[:, 2] = np.abs(wo[:, 2]) + 1e-3
+    wo = (wo / np.linalg.norm(wo, axis=1, keepdims=True)).astype(np.float32)
+    wi, f, pdf, delta, _ = _run_bxdf(cuda, 3, normal, wo, color, params, rnd4[:, :2].copy())
+    ok = pdf > 0
+    f64, p64 = O.bxdf_eval_pdf(64, 3, normal, wo, color, params, wi.astype(np.float64))
+    r = np.maximum(rel_err(f[ok], f64[ok], 1e-20).max(1), rel_err(pdf[ok], p64[ok], 1e-20))
+    frac = np.mean(r < 1e-5)
+    print(f"Disney, exact local frame: {frac:.4%} of {ok.sum()} sampled points within 1e-5 of FP64")
+    assert frac > 0.99, (frac, np.quantile(r, [0.5, 0.99, 0.999]))
+
+
 def test_bxdf_eval_kernel(cuda):
     import torch
     import srt_gb300 as S
@@ -157,7 +179,8 @@ def test_trace_cornell_vs_brute_force(cuda):
     sc = S.Scene(sa)
     osc = O.OracleScene(sa.desc())
     rays = _random_rays(20000, -0.99, 0.99, 4)
-    _check_hits(sc, osc, rays, cuda)
+    frac = _check_hits(sc, osc, rays, cuda)
+    print(f"Cornell: primitive-id mismatch rate {frac:.2e} (only rays within 1e-4 of an edge may differ)")
     # shadow rays toward random points: visibility must agree away from edges
     rays[:, 7] = np.random.default_rng(9).uniform(0.1, 3.0, len(rays)).astype(np.float32)
     vis = torch.zeros(len(rays), dtype=torch.int32, device=cuda)
@@ -178,6 +201,7 @@ def test_trace_spheres_vs_oracle(cuda):
     osc = O.OracleScene(sa.desc(), bvh=True)
     rays = _random_rays(30000, -12.0, 12.0, 5)
     frac = _check_hits(sc, osc, rays, cuda)
+    print(f"spheres: primitive-id mismatch rate {frac:.2e} (only rays within 1e-4 of an edge may differ)")
     assert frac < 1e-3
 
 
