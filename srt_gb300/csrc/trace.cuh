@@ -22,11 +22,6 @@ namespace srt {
 #endif
 constexpr int kStackEntries = SRT_STACK_ENTRIES;  // node groups; at most one per tree level
 
-// Node prefetch while a lane tests its leaf triangles: 0 none, 1 the next
-// node into L1, 2 the next node into L1 and the other hit children into L2.
-#ifndef SRT_TRACE_PREFETCH
-#define SRT_TRACE_PREFETCH 0
-#endif
 
 // resident 128-thread traversal blocks per SM the compiler budgets registers for
 #ifndef SRT_TRACE_MIN_BLOCKS
@@ -41,9 +36,14 @@ struct Hit {
 struct RayPre {
     float3 o;
     float3 idir;
-    int kx, ky, kz;
     float sx, sy, sz;
-    uint32_t oct;
+    // packed: kx (bits 0-1), ky (2-3), kz (4-5) of the watertight test's axis
+    // permutation, octant (8-10); one register instead of four
+    uint32_t axes;
+    __device__ __forceinline__ int kx() const { return (int)(axes & 3u); }
+    __device__ __forceinline__ int ky() const { return (int)((axes >> 2) & 3u); }
+    __device__ __forceinline__ int kz() const { return (int)((axes >> 4) & 3u); }
+    __device__ __forceinline__ uint32_t oct() const { return axes >> 8; }
 };
 
 __device__ __forceinline__ float comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
@@ -64,9 +64,6 @@ __device__ __forceinline__ RayPre make_ray(float3 o, float3 d)
         kx = ky;
         ky = t;
     }
-    r.kx = kx;
-    r.ky = ky;
-    r.kz = kz;
     r.sx = comp(d, kx) / dz;
     r.sy = comp(d, ky) / dz;
     r.sz = 1.0f / dz;
@@ -77,7 +74,8 @@ __device__ __forceinline__ RayPre make_ray(float3 o, float3 d)
     r.idir = make_float3(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z);
     // octant = signs of idir (a -0 component counts as negative), so that the
     // near slab plane of every child box is its low plane exactly when the bit is clear
-    r.oct = (r.idir.x < 0.0f ? 1u : 0u) | (r.idir.y < 0.0f ? 2u : 0u) | (r.idir.z < 0.0f ? 4u : 0u);
+    const uint32_t oct = (r.idir.x < 0.0f ? 1u : 0u) | (r.idir.y < 0.0f ? 2u : 0u) | (r.idir.z < 0.0f ? 4u : 0u);
+    r.axes = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4) | (oct << 8);
     return r;
 }
 
@@ -87,10 +85,11 @@ __device__ __forceinline__ bool hit_triangle(const RayPre& r, float3 v0, float3 
                                              float tmax, float& t, float& b1, float& b2)
 {
     float3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
-    float az = comp(A, r.kz), bz = comp(B, r.kz), cz = comp(C, r.kz);
-    float Ax = comp(A, r.kx) - r.sx * az, Ay = comp(A, r.ky) - r.sy * az;
-    float Bx = comp(B, r.kx) - r.sx * bz, By = comp(B, r.ky) - r.sy * bz;
-    float Cx = comp(C, r.kx) - r.sx * cz, Cy = comp(C, r.ky) - r.sy * cz;
+    const int kx = r.kx(), ky = r.ky(), kz = r.kz();
+    float az = comp(A, kz), bz = comp(B, kz), cz = comp(C, kz);
+    float Ax = comp(A, kx) - r.sx * az, Ay = comp(A, ky) - r.sy * az;
+    float Bx = comp(B, kx) - r.sx * bz, By = comp(B, ky) - r.sy * bz;
+    float Cx = comp(C, kx) - r.sx * cz, Cy = comp(C, ky) - r.sy * cz;
     float U = Cx * By - Cy * Bx;
     float V = Ax * Cy - Ay * Cx;
     float W = Bx * Ay - By * Ax;
@@ -107,10 +106,11 @@ __device__ __forceinline__ bool hit_triangle(const RayPre& r, float3 v0, float3 
     return true;
 }
 
-__device__ __forceinline__ float u16f(uint32_t w, int hi)
+// 2^23 + q as a float, q the low (hi = 0) or high (hi = 1) 16 bits of w: one
+// byte permute places q under the exponent of 2^23
+__device__ __forceinline__ float q23(uint32_t w, int hi)
 {
-    uint32_t q = hi ? (w >> 16) : (w & 0xffffu);
-    return __uint_as_float(0x4B000000u | q) - 8388608.0f;
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, hi ? 0x7432u : 0x7410u));
 }
 __device__ __forceinline__ uint32_t word4(uint4 v, int j)
 {
@@ -168,7 +168,7 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     // planes in near/far order replaces the per-child min/max of the two slab
     // distances (fmaf is monotonic in the quantised coordinate, so the
     // selected value equals that min/max exactly).
-    const int ox = (int)(r.oct & 1u), oy = (int)((r.oct >> 1) & 1u), oz = (int)(r.oct >> 2);
+    const int ox = (int)(r.oct() & 1u), oy = (int)((r.oct() >> 1) & 1u), oz = (int)(r.oct() >> 2);
     uint4 nqx = __ldg(np + 2 + 3 * ox), fqx = __ldg(np + 5 - 3 * ox);
     uint4 nqy = __ldg(np + 3 + 3 * oy), fqy = __ldg(np + 6 - 3 * oy);
     uint4 nqz = __ldg(np + 4 + 3 * oz), fqz = __ldg(np + 7 - 3 * oz);
@@ -182,21 +182,31 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     float Bx = (__uint_as_float(w0.x) - r.o.x) * r.idir.x;
     float By = (__uint_as_float(w0.y) - r.o.y) * r.idir.y;
     float Bz = (__uint_as_float(w0.z) - r.o.z) * r.idir.z;
+    // Plane q of an axis is at t = q A + B = (2^23 + q) A + C with C = B - 2^23 A,
+    // so each plane costs one permute and one FMA (the fused product is exact).
+    // Rounding C costs at most |A| / 2 (one quantisation step is |A| in t), so
+    // near planes move |A| nearer and far planes |A| farther: the test stays
+    // conservative (checked against exact slab intervals on 2M random cases).
+    const float K = 8388608.0f;
+    const float Cx = fmaf(-K, Ax, Bx), Cy = fmaf(-K, Ay, By), Cz = fmaf(-K, Az, Bz);
+    const float cnx = Cx - fabsf(Ax), cfx = Cx + fabsf(Ax);
+    const float cny = Cy - fabsf(Ay), cfy = Cy + fabsf(Ay);
+    const float cnz = Cz - fabsf(Az), cfz = Cz + fabsf(Az);
     uint32_t ihits = 0;
     uint32_t tm = 0;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * (s & 3))) & 0xffu;
         int j = s >> 1, hi = s & 1;
-        float nx = fmaf(u16f(word4(nqx, j), hi), Ax, Bx), fx = fmaf(u16f(word4(fqx, j), hi), Ax, Bx);
-        float ny = fmaf(u16f(word4(nqy, j), hi), Ay, By), fy = fmaf(u16f(word4(fqy, j), hi), Ay, By);
-        float nz = fmaf(u16f(word4(nqz, j), hi), Az, Bz), fz = fmaf(u16f(word4(fqz, j), hi), Az, Bz);
+        float nx = fmaf(q23(word4(nqx, j), hi), Ax, cnx), fx = fmaf(q23(word4(fqx, j), hi), Ax, cfx);
+        float ny = fmaf(q23(word4(nqy, j), hi), Ay, cny), fy = fmaf(q23(word4(fqy, j), hi), Ay, cfy);
+        float nz = fmaf(q23(word4(nqz, j), hi), Az, cnz), fz = fmaf(q23(word4(fqz, j), hi), Az, cfz);
         float tn = fmax3(nx, ny, fmaxf(nz, tmin));
         float tf = fmin3(fx, fy, fminf(fz, tmax));
         bool hit = meta != 0u && tn <= tf * 1.00000024f;
         if (hit) {
             if (meta & 0x80u) {
-                ihits |= 1u << (s ^ r.oct);
+                ihits |= 1u << (s ^ r.oct());
             } else {
                 tm |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
             }
@@ -206,9 +216,6 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     tmask = tm;
     tri_base = w1.y;
 }
-
-__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 __device__ __forceinline__ uint32_t group_next_node(uint2& g, uint32_t oct)
 {
@@ -238,14 +245,14 @@ __device__ __forceinline__ Hit trace_closest(const SceneView& S, float3 o, float
     h.tri = -1;
     RayPre r = make_ray(o, d);
     st.sp = 0;
-    uint2 group = make_uint2(0u, 1u | ((1u << r.oct) << 8));  // root = child rank 0 of slot 0
+    uint2 group = make_uint2(0u, 1u | ((1u << r.oct()) << 8));  // root = child rank 0 of slot 0
     for (;;) {
         if ((group.y >> 8) == 0u) {
             if (st.sp == 0) break;
             group = st.pop();
             continue;
         }
-        uint32_t ni = group_next_node(group, r.oct);
+        uint32_t ni = group_next_node(group, r.oct());
         if ((group.y >> 8) != 0u) st.push(group, overflow);
         uint32_t tmask, tri_base;
         visit_node(S.nodes, ni, r, tmin, h.t, group, tmask, tri_base);
@@ -285,6 +292,9 @@ __device__ __forceinline__ Hit trace_closest(const SceneView& S, float3 o, float
 #ifndef SRT_TRACE_STEPS
 #define SRT_TRACE_STEPS 4
 #endif
+#ifndef SRT_TRACE_POSTPONE
+#define SRT_TRACE_POSTPONE 0  // percent of active lanes; 0 = test leaf triangles at once
+#endif
 constexpr int kRefill = SRT_TRACE_REFILL;     // idle lanes that trigger a fetch
 constexpr int kStepBudget = SRT_TRACE_STEPS;  // node visits per lane between refill checks
 
@@ -293,8 +303,7 @@ struct TravState {
     float tmin, tmax;  // tmax shrinks with closest hits
     uint2 group;
     uint32_t tmask, tri_base;
-    float u, v;
-    int32_t tri;
+    int32_t tri;  // closest (or any) hit so far; its barycentrics: hit_barycentrics
     const WideNode* nodes;
     const float4* tris;
 };
@@ -305,14 +314,28 @@ __device__ __forceinline__ void trav_init(TravState& s, const WideNode* nodes, c
     s.r = make_ray(o, d);
     s.tmin = tmin;
     s.tmax = tmax;
-    s.group = make_uint2(0u, 1u | ((1u << s.r.oct) << 8));
+    s.group = make_uint2(0u, 1u | ((1u << s.r.oct()) << 8));
     s.tmask = 0;
     s.tri_base = 0;
-    s.u = s.v = 0.0f;
     s.tri = -1;
     s.nodes = nodes;
     s.tris = tris;
     st.sp = 0;
+}
+
+// Barycentrics of the finished ray's hit triangle, recomputed once at the
+// end instead of kept in registers through the traversal: the same test on
+// the same inputs gives the same u, v (with tmax open it accepts the hit).
+__device__ __forceinline__ float2 hit_barycentrics(const TravState& s)
+{
+    float u = 0.0f, v = 0.0f;
+    if (s.tri >= 0) {
+        const float4* tp = s.tris + 3 * (size_t)s.tri;
+        float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
+        float t;
+        if (!hit_triangle(s.r, f3(a), f3(bb), f3(c), s.tmin, __int_as_float(0x7f800000), t, u, v)) u = v = 0.0f;
+    }
+    return make_float2(u, v);
 }
 
 // Advances one ray; returns true when its traversal is complete (for any-hit
@@ -321,6 +344,21 @@ template <bool kAny, bool kCount>
 __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overflow, TraceCount& cnt)
 {
     for (int it = 0; it < kStepBudget; ++it) {
+        if (SRT_TRACE_POSTPONE > 0) {
+            // When fewer than SRT_TRACE_POSTPONE % of the warp's active lanes
+            // have leaf triangles, a lane that also has a node to visit keeps its
+            // triangles for later (a triangle group on its stack, bit 31 set) and
+            // visits the node, so node visits and triangle tests each run with
+            // more lanes together (Ylitie et al. 2017).  Every postponement is
+            // followed by a node visit, so the traversal always progresses.
+            const uint32_t act = __activemask();
+            const uint32_t with_tris = __ballot_sync(act, s.tmask != 0u);
+            if (s.tmask && (s.group.y >> 8) != 0u && st.sp < kStackEntries - 4 &&
+                __popc(with_tris) * 100 < SRT_TRACE_POSTPONE * __popc(act)) {
+                st.push(make_uint2(s.tri_base | 0x80000000u, s.tmask), overflow);
+                s.tmask = 0;
+            }
+        }
         while (s.tmask) {
             uint32_t b = __ffs(s.tmask) - 1;
             s.tmask &= s.tmask - 1;
@@ -329,8 +367,6 @@ __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overf
             float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
             float t, u, v;
             if (hit_triangle(s.r, f3(a), f3(bb), f3(c), s.tmin, s.tmax, t, u, v)) {
-                s.u = u;
-                s.v = v;
                 s.tri = (int32_t)ti;
                 if (kAny) return true;
                 s.tmax = t;
@@ -338,21 +374,21 @@ __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overf
         }
         if ((s.group.y >> 8) == 0u) {
             if (st.sp == 0) return true;
-            s.group = st.pop();
+            const uint2 e = st.pop();
+            if (SRT_TRACE_POSTPONE > 0 && (e.x & 0x80000000u)) {
+                // a postponed leaf: its triangles are tested in the next step
+                s.tri_base = e.x & 0x7fffffffu;
+                s.tmask = e.y;
+                continue;
+            }
+            s.group = e;
         }
-        uint32_t ni = group_next_node(s.group, s.r.oct);
+        uint32_t ni = group_next_node(s.group, s.r.oct());
         if ((s.group.y >> 8) != 0u) st.push(s.group, overflow);
         visit_node(s.nodes, ni, s.r, s.tmin, s.tmax, s.group, s.tmask, s.tri_base);
         if (kCount) {
             cnt.nodes += 1;
             cnt.tris += __popc(s.tmask);
-        }
-        if (SRT_TRACE_PREFETCH && s.tmask && (s.group.y >> 8) != 0u) {
-            // the leaf tests of this node come first: start fetching the next node
-            uint2 g = s.group;
-            prefetch_l1(s.nodes + group_next_node(g, s.r.oct));
-            if (SRT_TRACE_PREFETCH == 2)
-                while ((g.y >> 8) != 0u) prefetch_l2(s.nodes + group_next_node(g, s.r.oct));
         }
     }
     return false;
@@ -401,14 +437,14 @@ __device__ __forceinline__ bool trace_any(const SceneView& S, float3 o, float3 d
 {
     RayPre r = make_ray(o, d);
     st.sp = 0;
-    uint2 group = make_uint2(0u, 1u | ((1u << r.oct) << 8));
+    uint2 group = make_uint2(0u, 1u | ((1u << r.oct()) << 8));
     for (;;) {
         if ((group.y >> 8) == 0u) {
             if (st.sp == 0) break;
             group = st.pop();
             continue;
         }
-        uint32_t ni = group_next_node(group, r.oct);
+        uint32_t ni = group_next_node(group, r.oct());
         if ((group.y >> 8) != 0u) st.push(group, overflow);
         uint32_t tmask, tri_base;
         visit_node(S.nodes, ni, r, tmin, tmax, group, tmask, tri_base);

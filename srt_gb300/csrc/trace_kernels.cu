@@ -27,7 +27,8 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace_c
         [&](int64_t i, const TravState& s, bool fin) {
             if (!fin) return;
             int32_t prim = s.tri >= 0 ? __ldg(S.tri_prim + s.tri) : -1;
-            hits[i] = make_float4(s.tmax, s.u, s.v, __int_as_float(prim));
+            const float2 uv = hit_barycentrics(s);
+            hits[i] = make_float4(s.tmax, uv.x, uv.y, __int_as_float(prim));
         });
     if (overflow) atomicAdd(overflow_flag, 1);
 }

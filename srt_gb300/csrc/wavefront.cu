@@ -98,6 +98,16 @@ __device__ __forceinline__ int32_t warp_append_multi(int32_t* counter, bool pred
     return base + __popc(peers & ((1u << lane) - 1u));
 }
 
+// Adds one per lane to *counter (null: nothing); lanes with the same counter
+// share one atomic.  All 32 lanes must call it.
+__device__ __forceinline__ void warp_count(int32_t* counter)
+{
+    uint32_t active = __ballot_sync(kFull, counter != nullptr);
+    if (!counter) return;
+    uint32_t peers = __match_any_sync(active, (unsigned long long)counter);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(counter, __popc(peers));
+}
+
 __device__ __forceinline__ int region_cell(const CacheRec& c, float3 p)
 {
     int r = c.region_res;
@@ -276,7 +286,8 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
             const int32_t h = warp_append(&ctr->n_hit, hit);
             const int32_t m = warp_append(&ctr->n_miss, fin && !hit);
             if (!fin) return;
-            hits[i] = make_float4(s.tmax, s.u, s.v, __int_as_float(s.tri));
+            const float2 uv = hit_barycentrics(s);
+            hits[i] = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
             order[hit ? h : (int32_t)(n - 1 - m)] = (int32_t)i;
         });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
@@ -561,6 +572,8 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
         float3 o = f3(0.0f), d = f3(0.0f);
         uint4 ra = make_uint4(0, 0, 0, 0);
         uint2 rb = make_uint2(0, 0);
+        int32_t* frame_ctr = nullptr;  // progressive-frame counter of the finished sample
+        int32_t* pixel_ctr = nullptr;  // finished-pixel counter, when the pixel's last sample ended
         if (i < n) {
             int2 e = done[i];
             job = e.x;
@@ -593,7 +606,7 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
             J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             int k = J.spp_done[pix] + 1;
             J.spp_done[pix] = k;
-            if (J.frame_done) atomicAdd(J.frame_done + (k - 1), 1);
+            if (J.frame_done) frame_ctr = J.frame_done + (k - 1);
             if (k < J.spp) {
                 Rng rng;
                 rng.load(J.rng_a[pix], J.rng_b[pix]);
@@ -604,9 +617,12 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
                 rng.store(ra, rb);
                 again = true;
             } else {
-                atomicAdd(J.pixels_done, 1);
+                pixel_ctr = J.pixels_done;
             }
         }
+        // progress counters: one atomic per distinct counter in the warp
+        warp_count(frame_ctr);
+        warp_count(pixel_ctr);
         int32_t slot = warp_append(&ctr->n_next, again);
         if (again) {
             if (slot < capacity) {
