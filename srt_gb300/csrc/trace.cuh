@@ -292,9 +292,6 @@ __device__ __forceinline__ Hit trace_closest(const SceneView& S, float3 o, float
 #ifndef SRT_TRACE_STEPS
 #define SRT_TRACE_STEPS 4
 #endif
-#ifndef SRT_TRACE_POSTPONE
-#define SRT_TRACE_POSTPONE 0  // percent of active lanes; 0 = test leaf triangles at once
-#endif
 constexpr int kRefill = SRT_TRACE_REFILL;     // idle lanes that trigger a fetch
 constexpr int kStepBudget = SRT_TRACE_STEPS;  // node visits per lane between refill checks
 
@@ -344,21 +341,6 @@ template <bool kAny, bool kCount>
 __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overflow, TraceCount& cnt)
 {
     for (int it = 0; it < kStepBudget; ++it) {
-        if (SRT_TRACE_POSTPONE > 0) {
-            // When fewer than SRT_TRACE_POSTPONE % of the warp's active lanes
-            // have leaf triangles, a lane that also has a node to visit keeps its
-            // triangles for later (a triangle group on its stack, bit 31 set) and
-            // visits the node, so node visits and triangle tests each run with
-            // more lanes together (Ylitie et al. 2017).  Every postponement is
-            // followed by a node visit, so the traversal always progresses.
-            const uint32_t act = __activemask();
-            const uint32_t with_tris = __ballot_sync(act, s.tmask != 0u);
-            if (s.tmask && (s.group.y >> 8) != 0u && st.sp < kStackEntries - 4 &&
-                __popc(with_tris) * 100 < SRT_TRACE_POSTPONE * __popc(act)) {
-                st.push(make_uint2(s.tri_base | 0x80000000u, s.tmask), overflow);
-                s.tmask = 0;
-            }
-        }
         while (s.tmask) {
             uint32_t b = __ffs(s.tmask) - 1;
             s.tmask &= s.tmask - 1;
@@ -374,14 +356,7 @@ __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overf
         }
         if ((s.group.y >> 8) == 0u) {
             if (st.sp == 0) return true;
-            const uint2 e = st.pop();
-            if (SRT_TRACE_POSTPONE > 0 && (e.x & 0x80000000u)) {
-                // a postponed leaf: its triangles are tested in the next step
-                s.tri_base = e.x & 0x7fffffffu;
-                s.tmask = e.y;
-                continue;
-            }
-            s.group = e;
+            s.group = st.pop();
         }
         uint32_t ni = group_next_node(s.group, s.r.oct());
         if ((s.group.y >> 8) != 0u) st.push(s.group, overflow);

@@ -2,6 +2,7 @@
 //
 //   k_start    raygen for every pixel of a newly admitted job (SoA queue)
 //   k_closest  closest-hit traversal of the current queue -> hit records
+//   k_order    shading order: the queue's hits first, then its misses
 //   k_shade    miss / emitter-hit MIS / NEE + MIS / BSDF sample / Russian
 //              roulette; survivors compacted into the next queue with one
 //              atomic per warp; NEE rays into the shadow queue
@@ -27,6 +28,14 @@
 namespace srt {
 
 namespace {
+
+// shading order: 1 = global, appended by k_closest as rays finish (hits to
+// the front of an order list, misses to the back); 2 = block-local (each
+// shading block permutes its consecutive entries hits first); 3 = global,
+// built by k_order after the traversal (one atomic pair per 256 entries)
+#ifndef SRT_SHADE_ORDER
+#define SRT_SHADE_ORDER 3
+#endif
 
 constexpr int kThreads = 256;
 constexpr int kTraceThreads = 128;
@@ -280,20 +289,66 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
             trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, 1e16f, stk);
         },
         [&](int64_t i, const TravState& s, bool fin) {
+#if SRT_SHADE_ORDER == 1
             // shading order: hits from the front of `order`, misses from the
             // back, so k_shade's warps see one kind of vertex (except at the seam)
             const bool hit = fin && s.tri >= 0;
             const int32_t h = warp_append(&ctr->n_hit, hit);
             const int32_t m = warp_append(&ctr->n_miss, fin && !hit);
+#endif
             if (!fin) return;
             const float2 uv = hit_barycentrics(s);
             hits[i] = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
+#if SRT_SHADE_ORDER == 1
             order[hit ? h : (int32_t)(n - 1 - m)] = (int32_t)i;
+#endif
         });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
     if (kCount && (cnt.nodes | cnt.tris)) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_nodes), (unsigned long long)cnt.nodes);
         atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_tris), (unsigned long long)cnt.tris);
+    }
+}
+
+// Shading order for k_shade: queue entries whose ray hit the scene first (in
+// queue order), then the misses; one pair of atomics per 256 entries.
+constexpr int kOrderThreads = 256;
+__global__ void __launch_bounds__(kOrderThreads) k_order(const float4* __restrict__ hits,
+                                                         int32_t* __restrict__ order, Counters* ctr,
+                                                         int64_t capacity)
+{
+    __shared__ int32_t warp_hits[kOrderThreads / 32];
+    __shared__ int32_t base_hit, base_miss;
+    const int n = (int)min((int64_t)ctr->n_cur, capacity);
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    for (int tile = blockIdx.x * kOrderThreads; tile < n; tile += gridDim.x * kOrderThreads) {
+        const int j = tile + t;
+        const bool valid = j < n;
+        const bool hit = valid && __float_as_int(__ldg(&hits[j].w)) >= 0;
+        const uint32_t hb = __ballot_sync(kFull, hit);
+        const uint32_t vb = __ballot_sync(kFull, valid);
+        if (lane == 0) warp_hits[w] = __popc(hb);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int k = 0; k < kOrderThreads / 32; ++k) {
+            const int c = warp_hits[k];
+            total += c;
+            if (k < w) before += c;
+        }
+        if (t == 0) {
+            const int tile_valid = min(kOrderThreads, n - tile);
+            base_hit = atomicAdd(&ctr->n_hit, total);
+            base_miss = atomicAdd(&ctr->n_miss, tile_valid - total);
+        }
+        __syncthreads();
+        const uint32_t below = (1u << lane) - 1u;
+        if (hit) order[base_hit + before + __popc(hb & below)] = j;
+        if (valid && !hit) {
+            // misses of this tile before this lane: earlier warps' valid entries minus their hits
+            const int miss_rank = (min(w * 32, n - tile) - before) + __popc(vb & ~hb & below);
+            order[n - 1 - (base_miss + miss_rank)] = j;
+        }
+        __syncthreads();  // warp_hits and the bases are rewritten by the next tile
     }
 }
 
@@ -308,18 +363,49 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
 #endif
 constexpr int kShadeThreads = SRT_SHADE_THREADS;
 
+// kCache: the iteration carries radiance-cache jobs (queries and training
+// records); the plain variant leaves that code out
+template <bool kCache>
 __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(const JobRec* __restrict__ jobs, PathQueue q,
                                                     const float4* __restrict__ hits,
                                                     const int32_t* __restrict__ order, PathQueue qn, ShadowQueue sq,
                                                     int2* __restrict__ done, Counters* ctr, int64_t capacity)
 {
     const int n = (int)min((int64_t)ctr->n_cur, capacity);
+#if SRT_SHADE_ORDER == 2
+    // block-local shading order: each block takes kShadeThreads consecutive
+    // entries (coalesced) and permutes them hits first, misses last
+    __shared__ int16_t perm[kShadeThreads];
+    __shared__ int32_t warp_hits[kShadeThreads / 32];
+    for (int blk = blockIdx.x * kShadeThreads; blk < n; blk += gridDim.x * kShadeThreads) {
+        {
+            const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+            const int j0 = blk + t;
+            const bool hit0 = j0 < n && __float_as_int(__ldg(&hits[j0].w)) >= 0;
+            const uint32_t hb = __ballot_sync(kFull, hit0);
+            if (lane == 0) warp_hits[w] = __popc(hb);
+            __syncthreads();
+            int before = 0, total = 0;
+            for (int k = 0; k < kShadeThreads / 32; ++k) {
+                const int c = warp_hits[k];
+                total += c;
+                if (k < w) before += c;
+            }
+            const uint32_t below = (1u << lane) - 1u;
+            const int pos = hit0 ? before + __popc(hb & below) : total + (w * 32 - before) + __popc(~hb & below);
+            perm[pos] = (int16_t)t;
+            __syncthreads();
+        }
+        const int i = blk + perm[threadIdx.x];
+        const bool valid = i < n;
+#else
     const int stride = gridDim.x * blockDim.x;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
         // queue entries in k_closest's shading order: hits first, then misses
         const int j = base + (threadIdx.x & 31);
         const bool valid = j < n;
         const int i = valid ? __ldg(order + j) : 0;
+#endif
         bool push_next = false, push_shadow = false, terminate = false, push_query = false;
         float4 qrec[4];
         float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
@@ -389,7 +475,7 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                     const float3 wo = -rd;
                     // radiance cache: non-training pixels end at the second vertex
                     const CacheRec& Cc = J.cache;
-                    const bool cache_job = Cc.w != nullptr;
+                    const bool cache_job = kCache && Cc.w != nullptr;
                     const bool train_pix = cache_job && (pix % Cc.train_stride) == Cc.train_phase;
                     if (cache_job && !train_pix && depth == 1) {
                         push_query = !Cc.region_off || !Cc.region_off[region_cell(Cc, pos)];
@@ -474,8 +560,8 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
             }
         }
         // network query of a cached path (its radiance is added by k_cache)
-        int32_t qslot = warp_append_multi(jobs[job].cache.q_count, valid && push_query);
-        if (push_query) {
+        int32_t qslot = kCache ? warp_append_multi(jobs[job].cache.q_count, valid && push_query) : -1;
+        if (kCache && push_query) {
             const CacheRec& Cc = jobs[job].cache;
             float4* qr = Cc.q_rec + 4 * (size_t)qslot;
             qr[0] = qrec[0];
@@ -523,6 +609,9 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
             else
                 atomicAdd(&ctr->overflow_queue, 1);
         }
+#if SRT_SHADE_ORDER == 2
+        __syncthreads();  // perm and warp_hits are rewritten by the next round
+#endif
     }
 }
 
@@ -757,6 +846,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     grid_closest_ = resident(reinterpret_cast<const void*>(k_closest<false>));
     grid_shadow_ = resident(reinterpret_cast<const void*>(k_shadow<false>));
     grid_stride_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kThreads - 1) / kThreads, sms * 8));
+    grid_order_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kOrderThreads - 1) / kOrderThreads, sms * 8));
     grid_shade_ = (int)std::max<int64_t>(
         1, std::min<int64_t>((capacity + kShadeThreads - 1) / kShadeThreads, (int64_t)sms * 8 * (256 / kShadeThreads)));
     return SRT_OK;
@@ -801,10 +891,15 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
         k_closest<true><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, order_, counters_, capacity_);
     else
         k_closest<false><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, order_, counters_, capacity_);
+    if (SRT_SHADE_ORDER == 3) k_order<<<grid_order_, kOrderThreads, 0, st>>>(hits_, order_, counters_, capacity_);
     mark(0, 1);
     mark(1, 0);
-    k_shade<<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,
-                                                   capacity_);
+    if (cache_)
+        k_shade<true><<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,
+                                                             capacity_);
+    else
+        k_shade<false><<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,
+                                                              capacity_);
     mark(1, 1);
     mark(2, 0);
     if (prof && count_)
@@ -942,7 +1037,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         if (e == cudaSuccess) {
             const Counters& c = *host_counters_;
             iters = c.run_iters;
-            times_.launches += 1 + iters * (cache_ ? 6 : 5);
+            times_.launches += 1 + iters * ((cache_ ? 6 : 5) + (SRT_SHADE_ORDER == 3 ? 1 : 0));
             if (c.overflow_queue)
                 status = set_error(SRT_ERR_ARG, "wavefront queue capacity exceeded");
             else if (c.overflow_stack)
@@ -965,7 +1060,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
                 e = cudaGraphLaunch(graph, graph_stream_);
             }
             iters += 2;
-            times_.launches += 10;
+            times_.launches += 2 * ((cache_ ? 6 : 5) + (SRT_SHADE_ORDER == 3 ? 1 : 0));
         }
         if (e != cudaSuccess) break;
         what = "copy counters";

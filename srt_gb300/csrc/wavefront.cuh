@@ -154,7 +154,7 @@ private:
     bool count_ = true;
     bool cache_ = false;
     KernelTimes times_;
-    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0, grid_shade_ = 0;
+    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0, grid_shade_ = 0, grid_order_ = 0;
 };
 
 }  // namespace srt
