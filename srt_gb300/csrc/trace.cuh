@@ -24,6 +24,10 @@ constexpr int kStackEntries = SRT_STACK_ENTRIES;  // node groups; at most one pe
 
 
 // resident 128-thread traversal blocks per SM the compiler budgets registers for
+#ifndef SRT_SLAB_MARGIN
+#define SRT_SLAB_MARGIN 1.0f  // quantisation steps added to each slab side
+#endif
+
 #ifndef SRT_TRACE_MIN_BLOCKS
 #define SRT_TRACE_MIN_BLOCKS 7
 #endif
@@ -185,13 +189,15 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     // Plane q of an axis is at t = q A + B = (2^23 + q) A + C with C = B - 2^23 A,
     // so each plane costs one permute and one FMA (the fused product is exact).
     // Rounding C costs at most |A| / 2 (one quantisation step is |A| in t), so
-    // near planes move |A| nearer and far planes |A| farther: the test stays
-    // conservative (checked against exact slab intervals on 2M random cases).
+    // near planes move SRT_SLAB_MARGIN * |A| nearer and far planes as much
+    // farther: the test stays conservative (no exactly-hit slab missed on 4M
+    // random borderline cases from a margin of 0.625 up).
     const float K = 8388608.0f;
     const float Cx = fmaf(-K, Ax, Bx), Cy = fmaf(-K, Ay, By), Cz = fmaf(-K, Az, Bz);
-    const float cnx = Cx - fabsf(Ax), cfx = Cx + fabsf(Ax);
-    const float cny = Cy - fabsf(Ay), cfy = Cy + fabsf(Ay);
-    const float cnz = Cz - fabsf(Az), cfz = Cz + fabsf(Az);
+    const float mx = SRT_SLAB_MARGIN * fabsf(Ax), my = SRT_SLAB_MARGIN * fabsf(Ay), mz = SRT_SLAB_MARGIN * fabsf(Az);
+    const float cnx = Cx - mx, cfx = Cx + mx;
+    const float cny = Cy - my, cfy = Cy + my;
+    const float cnz = Cz - mz, cfz = Cz + mz;
     uint32_t ihits = 0;
     uint32_t tm = 0;
 #pragma unroll
@@ -320,19 +326,23 @@ __device__ __forceinline__ void trav_init(TravState& s, const WideNode* nodes, c
     st.sp = 0;
 }
 
-// Barycentrics of the finished ray's hit triangle, recomputed once at the
-// end instead of kept in registers through the traversal: the same test on
-// the same inputs gives the same u, v (with tmax open it accepts the hit).
-__device__ __forceinline__ float2 hit_barycentrics(const TravState& s)
+// Barycentrics of a finished ray's hit triangle, recomputed once at the end
+// instead of kept in registers through the traversal: the same test on the
+// same inputs gives the same u, v (with tmax open it accepts the hit).
+__device__ __forceinline__ float2 tri_barycentrics(const RayPre& r, const float4* tris, int32_t tri, float tmin)
 {
     float u = 0.0f, v = 0.0f;
-    if (s.tri >= 0) {
-        const float4* tp = s.tris + 3 * (size_t)s.tri;
+    if (tri >= 0) {
+        const float4* tp = tris + 3 * (size_t)tri;
         float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
         float t;
-        if (!hit_triangle(s.r, f3(a), f3(bb), f3(c), s.tmin, __int_as_float(0x7f800000), t, u, v)) u = v = 0.0f;
+        if (!hit_triangle(r, f3(a), f3(bb), f3(c), tmin, __int_as_float(0x7f800000), t, u, v)) u = v = 0.0f;
     }
     return make_float2(u, v);
+}
+__device__ __forceinline__ float2 hit_barycentrics(const TravState& s)
+{
+    return tri_barycentrics(s.r, s.tris, s.tri, s.tmin);
 }
 
 // Advances one ray; returns true when its traversal is complete (for any-hit

@@ -275,12 +275,12 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
                                                               int32_t* __restrict__ order, Counters* ctr,
                                                               int64_t capacity)
 {
-    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
-    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
     // a counter past the capacity (overflow, reported by the host) never indexes past the queue
     const int64_t n = min((int64_t)ctr->n_cur, capacity);
     int overflow = 0;
     TraceCount cnt;
+    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
+    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
     trace_persistent<false, kCount>(
         n, &ctr->fetch_closest, st, overflow, cnt,
         [&](int64_t i, TravState& s, Stack& stk) {
@@ -619,11 +619,11 @@ template <bool kCount>
 __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_shadow(const JobRec* __restrict__ jobs, ShadowQueue sq,
                                                              Counters* ctr, int64_t capacity)
 {
-    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
-    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
     const int64_t n = min((int64_t)ctr->n_shadow, capacity);
     int overflow = 0;
     TraceCount cnt;
+    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
+    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
     trace_persistent<true, kCount>(
         n, &ctr->fetch_shadow, st, overflow, cnt,
         [&](int64_t i, TravState& s, Stack& stk) {
