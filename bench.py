@@ -14,6 +14,16 @@ Multi-GPU runs (torchrun) render independent replicas: each rank renders
 the full frame, value = all ranks' samples / max rank time (weak scaling).
 `--impl reference` times the reference's path-tracing algorithm on the
 host cores (the oracle's CPU restatement) on a bounded crop.
+
+Extra keys: `roofline` for the kernel with the most device time in a
+timed profile frame (CUDA events around the production kernels; the work
+per ray from a second frame of the same seed with the counting traversal
+kernels), `traffic` scaled from the DRAM bytes per ray of one ncu capture
+(profiles/<kernel>_dram.json); `cache` (learned-cache time to the plain
+tracer's 64-spp relMSE, 1280x720), `serving` (a 10 s Poisson run at 20
+jobs/s), `cpu_baseline`.  `--no-cache`, `--no-serving`,
+`--no-cpu-baseline` skip those parts; `--profile-case` runs the short
+case the ncu captures use.
 """
 from __future__ import annotations
 

@@ -173,9 +173,6 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     // distances (fmaf is monotonic in the quantised coordinate, so the
     // selected value equals that min/max exactly).
     const int ox = (int)(r.oct() & 1u), oy = (int)((r.oct() >> 1) & 1u), oz = (int)(r.oct() >> 2);
-    uint4 nqx = __ldg(np + 2 + 3 * ox), fqx = __ldg(np + 5 - 3 * ox);
-    uint4 nqy = __ldg(np + 3 + 3 * oy), fqy = __ldg(np + 6 - 3 * oy);
-    uint4 nqz = __ldg(np + 4 + 3 * oz), fqz = __ldg(np + 7 - 3 * oz);
     int ex = (int)(int8_t)(w0.w & 0xffu);
     int ey = (int)(int8_t)((w0.w >> 8) & 0xffu);
     int ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
@@ -200,13 +197,12 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     const float cnz = Cz - mz, cfz = Cz + mz;
     uint32_t ihits = 0;
     uint32_t tm = 0;
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
+    auto child = [&](int s, uint32_t wnx, uint32_t wfx, uint32_t wny, uint32_t wfy, uint32_t wnz, uint32_t wfz) {
         uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * (s & 3))) & 0xffu;
-        int j = s >> 1, hi = s & 1;
-        float nx = fmaf(q23(word4(nqx, j), hi), Ax, cnx), fx = fmaf(q23(word4(fqx, j), hi), Ax, cfx);
-        float ny = fmaf(q23(word4(nqy, j), hi), Ay, cny), fy = fmaf(q23(word4(fqy, j), hi), Ay, cfy);
-        float nz = fmaf(q23(word4(nqz, j), hi), Az, cnz), fz = fmaf(q23(word4(fqz, j), hi), Az, cfz);
+        int hi = s & 1;
+        float nx = fmaf(q23(wnx, hi), Ax, cnx), fx = fmaf(q23(wfx, hi), Ax, cfx);
+        float ny = fmaf(q23(wny, hi), Ay, cny), fy = fmaf(q23(wfy, hi), Ay, cfy);
+        float nz = fmaf(q23(wnz, hi), Az, cnz), fz = fmaf(q23(wfz, hi), Az, cfz);
         float tn = fmax3(nx, ny, fmaxf(nz, tmin));
         float tf = fmin3(fx, fy, fminf(fz, tmax));
         bool hit = meta != 0u && tn <= tf * 1.00000024f;
@@ -217,6 +213,14 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
                 tm |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
             }
         }
+    };
+    const uint4 nqx = __ldg(np + 2 + 3 * ox), fqx = __ldg(np + 5 - 3 * ox);
+    const uint4 nqy = __ldg(np + 3 + 3 * oy), fqy = __ldg(np + 6 - 3 * oy);
+    const uint4 nqz = __ldg(np + 4 + 3 * oz), fqz = __ldg(np + 7 - 3 * oz);
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int j = s >> 1;
+        child(s, word4(nqx, j), word4(fqx, j), word4(nqy, j), word4(fqy, j), word4(nqz, j), word4(fqz, j));
     }
     group = make_uint2(w1.x, imask | (ihits << 8));
     tmask = tm;
