@@ -29,13 +29,6 @@ namespace srt {
 
 namespace {
 
-// shading order: 1 = global, appended by k_closest as rays finish (hits to
-// the front of an order list, misses to the back); 2 = block-local (each
-// shading block permutes its consecutive entries hits first); 3 = global,
-// built by k_order after the traversal (one atomic pair per 256 entries)
-#ifndef SRT_SHADE_ORDER
-#define SRT_SHADE_ORDER 3
-#endif
 
 constexpr int kThreads = 256;
 constexpr int kTraceThreads = 128;
@@ -271,8 +264,7 @@ __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ j
 
 template <bool kCount>
 __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest(const JobRec* __restrict__ jobs, PathQueue q,
-                                                              float4* __restrict__ hits,
-                                                              int32_t* __restrict__ order, Counters* ctr,
+                                                              float4* __restrict__ hits, Counters* ctr,
                                                               int64_t capacity)
 {
     // a counter past the capacity (overflow, reported by the host) never indexes past the queue
@@ -289,19 +281,9 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest
             trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, 1e16f, stk);
         },
         [&](int64_t i, const TravState& s, bool fin) {
-#if SRT_SHADE_ORDER == 1
-            // shading order: hits from the front of `order`, misses from the
-            // back, so k_shade's warps see one kind of vertex (except at the seam)
-            const bool hit = fin && s.tri >= 0;
-            const int32_t h = warp_append(&ctr->n_hit, hit);
-            const int32_t m = warp_append(&ctr->n_miss, fin && !hit);
-#endif
             if (!fin) return;
             const float2 uv = hit_barycentrics(s);
             hits[i] = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
-#if SRT_SHADE_ORDER == 1
-            order[hit ? h : (int32_t)(n - 1 - m)] = (int32_t)i;
-#endif
         });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
     if (kCount && (cnt.nodes | cnt.tris)) {
@@ -372,40 +354,12 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                                                     int2* __restrict__ done, Counters* ctr, int64_t capacity)
 {
     const int n = (int)min((int64_t)ctr->n_cur, capacity);
-#if SRT_SHADE_ORDER == 2
-    // block-local shading order: each block takes kShadeThreads consecutive
-    // entries (coalesced) and permutes them hits first, misses last
-    __shared__ int16_t perm[kShadeThreads];
-    __shared__ int32_t warp_hits[kShadeThreads / 32];
-    for (int blk = blockIdx.x * kShadeThreads; blk < n; blk += gridDim.x * kShadeThreads) {
-        {
-            const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-            const int j0 = blk + t;
-            const bool hit0 = j0 < n && __float_as_int(__ldg(&hits[j0].w)) >= 0;
-            const uint32_t hb = __ballot_sync(kFull, hit0);
-            if (lane == 0) warp_hits[w] = __popc(hb);
-            __syncthreads();
-            int before = 0, total = 0;
-            for (int k = 0; k < kShadeThreads / 32; ++k) {
-                const int c = warp_hits[k];
-                total += c;
-                if (k < w) before += c;
-            }
-            const uint32_t below = (1u << lane) - 1u;
-            const int pos = hit0 ? before + __popc(hb & below) : total + (w * 32 - before) + __popc(~hb & below);
-            perm[pos] = (int16_t)t;
-            __syncthreads();
-        }
-        const int i = blk + perm[threadIdx.x];
-        const bool valid = i < n;
-#else
     const int stride = gridDim.x * blockDim.x;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
-        // queue entries in k_closest's shading order: hits first, then misses
+        // queue entries in k_order's shading order: hits first, then misses
         const int j = base + (threadIdx.x & 31);
         const bool valid = j < n;
         const int i = valid ? __ldg(order + j) : 0;
-#endif
         bool push_next = false, push_shadow = false, terminate = false, push_query = false;
         float4 qrec[4];
         float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
@@ -609,9 +563,6 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
             else
                 atomicAdd(&ctr->overflow_queue, 1);
         }
-#if SRT_SHADE_ORDER == 2
-        __syncthreads();  // perm and warp_hits are rewritten by the next round
-#endif
     }
 }
 
@@ -888,11 +839,11 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     };
     mark(0, 0);
     if (prof && count_)
-        k_closest<true><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, order_, counters_, capacity_);
+        k_closest<true><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
     else
-        k_closest<false><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, order_, counters_, capacity_);
-    if (SRT_SHADE_ORDER == 3) k_order<<<grid_order_, kOrderThreads, 0, st>>>(hits_, order_, counters_, capacity_);
-    mark(0, 1);
+        k_closest<false><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+    k_order<<<grid_order_, kOrderThreads, 0, st>>>(hits_, order_, counters_, capacity_);
+    mark(0, 1);  // the closest-hit time includes the shading-order pass
     mark(1, 0);
     if (cache_)
         k_shade<true><<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,
@@ -1037,7 +988,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         if (e == cudaSuccess) {
             const Counters& c = *host_counters_;
             iters = c.run_iters;
-            times_.launches += 1 + iters * ((cache_ ? 6 : 5) + (SRT_SHADE_ORDER == 3 ? 1 : 0));
+            times_.launches += 1 + iters * (cache_ ? 7 : 6);
             if (c.overflow_queue)
                 status = set_error(SRT_ERR_ARG, "wavefront queue capacity exceeded");
             else if (c.overflow_stack)
@@ -1060,7 +1011,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
                 e = cudaGraphLaunch(graph, graph_stream_);
             }
             iters += 2;
-            times_.launches += 2 * ((cache_ ? 6 : 5) + (SRT_SHADE_ORDER == 3 ? 1 : 0));
+            times_.launches += 2 * (cache_ ? 7 : 6);
         }
         if (e != cudaSuccess) break;
         what = "copy counters";
