@@ -201,6 +201,53 @@ def measured_traffic(kernel, rays_per_launch):
     return int(d["dram_bytes_per_ray"] * rays_per_launch), d["capture"]
 
 
+def bxdf_eval_bench(S, n=1 << 20, launches=20, cpu=True):
+    """Disney BSDF batch (sample + f + pdf, GMaterial::sample) on n = 2^20
+    shading points generated in device memory from the PCG32 streams of
+    the config-0 definition; kernel time from CUDA events per launch with
+    L2 flushed between launches.  Algorithmic bytes per point = inputs
+    (normal, wo, colour: 36 B; 12 parameters: 48 B; 2 uniforms: 8 B) +
+    outputs (wi, f: 24 B; pdf, delta: 8 B) = 124 B.  CPU baseline: the
+    oracle's FP32 restatement (bit-identical to the reference's bxdf.h on
+    the golden vectors) on all host threads."""
+    import torch
+    dev = torch.device("cuda")
+    f32 = dict(dtype=torch.float32, device=dev)
+    normal, wo, color = (torch.empty((n, 3), **f32) for _ in range(3))
+    params, rnd = torch.empty((n, 12), **f32), torch.empty((n, 2), **f32)
+    wi, f = torch.empty((n, 3), **f32), torch.empty((n, 3), **f32)
+    pdf, delta = torch.empty(n, **f32), torch.empty(n, dtype=torch.int32, device=dev)
+    S.bxdf_generate(0, normal, wo, color, params, rnd, wi, f, pdf)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MB > L2
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(launches)]
+    for _ in range(3):
+        S.bxdf_sample(S.BXDF_DISNEY, normal, wo, color, params, rnd, wi, f, pdf, delta)
+    for a, b in evs:
+        flush.fill_(1.0)
+        a.record()
+        S.bxdf_sample(S.BXDF_DISNEY, normal, wo, color, params, rnd, wi, f, pdf, delta)
+        b.record()
+    torch.cuda.synchronize()
+    ms = statistics.median(a.elapsed_time(b) for a, b in evs)
+    peak, peak_kind = peaks()
+    gbs = 124.0 * n / (ms / 1e3) / 1e9
+    out = {"workload": "Disney BSDF sample + f + pdf, 2^20 points (config-0 inputs, PCG32 per point)",
+           "mpoints_per_s": round(n / (ms / 1e3) / 1e6, 1), "kernel_ms": round(ms, 4),
+           "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "peak_kind": peak_kind,
+                        "unit": "GB/s", "frac": round(gbs / peak, 4), "alg_bytes_per_point": 124},
+           "l2": "flushed (256 MB write) before every launch"}
+    if cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        nrm, w_o, col, prm, r4 = O.bxdf_inputs(0, n)
+        t0 = time.perf_counter()
+        O.bxdf_sample(32, S.BXDF_DISNEY, nrm, w_o, col, prm, r4[:, :2].copy(), threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(n / dt / 1e6, 2), "unit": "Mpoints/s", "cores": threads,
+                               "kind": "port", "sample": "the same 2^20 points, oracle FP32 BxDF"}
+    return out
+
+
 def relmse(S, x, ref):
     """Reference relMSE (metrics.h:30-34, largest 0.1 % dropped) on the GPU."""
     import torch
@@ -446,6 +493,7 @@ def main():
                               "closest_rays": st["closest_rays"], "shadow_rays": st["shadow_rays"],
                               "iterations": st["iterations"]},
         }
+        line["bxdf"] = bxdf_eval_bench(S, cpu=not args.no_cpu_baseline)
         if not args.no_cache:
             line["cache"] = cache_eval(S, arrays, scene)
         if not args.no_serving:

@@ -45,6 +45,8 @@ def lib():
             "oracle_pcg_uniforms": (None, [C.c_uint64, C.c_uint64, C.c_int, _vp]),
             "oracle_bxdf_generate": (None, [_i64, _i64, _vp, _vp, _vp, _vp, _vp]),
             "oracle_bxdf_sample": (None, [C.c_int, C.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+            "oracle_bxdf_sample_mt": (None, [C.c_int, C.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                             C.c_int]),
             "oracle_bxdf_eval_pdf": (None, [C.c_int, C.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
             "oracle_scene_create": (_vp, [_vp]),
             "oracle_scene_destroy": (None, [_vp]),
@@ -112,15 +114,15 @@ def bxdf_inputs(first, n):
     return normal, wo, color, params, rnd4
 
 
-def bxdf_sample(precision, type_, normal, wo, color, params, rnd2):
+def bxdf_sample(precision, type_, normal, wo, color, params, rnd2, threads=1):
     n = len(normal)
     wi = np.zeros((n, 3), np.float64)
     f = np.zeros((n, 3), np.float64)
     pdf = np.zeros(n, np.float64)
     delta = np.zeros(n, np.int32)
     rnd2 = np.ascontiguousarray(rnd2, np.float32)
-    lib().oracle_bxdf_sample(precision, type_, n, _np(normal), _np(wo), _np(color), _np(params), _np(rnd2),
-                             _np(wi), _np(f), _np(pdf), _np(delta))
+    lib().oracle_bxdf_sample_mt(precision, type_, n, _np(normal), _np(wo), _np(color), _np(params), _np(rnd2),
+                                _np(wi), _np(f), _np(pdf), _np(delta), int(threads))
     return wi, f, pdf, delta
 
 

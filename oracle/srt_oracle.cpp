@@ -1162,7 +1162,17 @@ void oracle_bxdf_generate(int64_t first, int64_t n, float* normal, float* wo, fl
 void oracle_bxdf_sample(int precision, int type, int64_t n, const float* normal, const float* wo, const float* color,
                         const float* params, const float* rnd, double* wi, double* f, double* pdf, int32_t* delta)
 {
-    for (int64_t k = 0; k < n; ++k) {
+    oracle_bxdf_sample_mt(precision, type, n, normal, wo, color, params, rnd, wi, f, pdf, delta, 1);
+}
+
+// The same, points split over `threads` host threads (chunks of 4096).
+void oracle_bxdf_sample_mt(int precision, int type, int64_t n, const float* normal, const float* wo,
+                           const float* color, const float* params, const float* rnd, double* wi, double* f,
+                           double* pdf, int32_t* delta, int threads)
+{
+    const int64_t chunk = 4096;
+    parallel_for((n + chunk - 1) / chunk, threads, [&](int64_t c) {
+    for (int64_t k = c * chunk; k < std::min(n, (c + 1) * chunk); ++k) {
         if (precision == 64) {
             Bx<double> b = bx_from<double>(type, params + 12 * k);
             Onb<double> ob = Onb<double>::from_n(cvt<double>(normal + 3 * k));
@@ -1183,6 +1193,7 @@ void oracle_bxdf_sample(int precision, int type, int64_t n, const float* normal,
             delta[k] = s.delta;
         }
     }
+    });
 }
 
 void oracle_bxdf_eval_pdf(int precision, int type, int64_t n, const float* normal, const float* wo, const float* color,

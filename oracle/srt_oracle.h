@@ -37,6 +37,9 @@ void oracle_bxdf_generate(int64_t first, int64_t n, float* normal, float* wo, fl
 void oracle_bxdf_sample(int precision, int type, int64_t n, const float* normal, const float* wo,
                         const float* color, const float* params, const float* rnd,
                         double* wi, double* f, double* pdf, int32_t* delta);
+void oracle_bxdf_sample_mt(int precision, int type, int64_t n, const float* normal, const float* wo,
+                           const float* color, const float* params, const float* rnd, double* wi, double* f,
+                           double* pdf, int32_t* delta, int threads);
 void oracle_bxdf_eval_pdf(int precision, int type, int64_t n, const float* normal, const float* wo,
                           const float* color, const float* params, const double* wi,
                           double* f, double* pdf);

@@ -105,6 +105,33 @@ def test_bad_arguments_fail_loudly(cuda):
         pt.render(film, pt_params(1, 8, 3, 1, 1, 0, rng_mode=7))
 
 
+def test_profiling_modes(cuda):
+    """Mode 1: per-kernel times and traversal work counters (counting kernel
+    variants); mode 2: times only; both leave the film unchanged; other
+    modes are rejected."""
+    import torch
+    import srt_gb300 as S
+    sa = _cornell()
+    sc = S.Scene(sa)
+    pt = S.PathTracer(sc, 16, 16)
+    film = torch.zeros((256, 4), dtype=torch.float32, device=cuda)
+    p = pt_params(4, 8, 3, 1, 1, 5)
+    pt.render(film, p)
+    torch.cuda.synchronize()
+    plain = film.cpu().numpy().copy()
+    for mode in (1, 2):
+        pt.set_profiling(mode)
+        pt.render(film, p)
+        torch.cuda.synchronize()
+        st = pt.stats()
+        np.testing.assert_array_equal(film.cpu().numpy(), plain)
+        assert sum(st["kernel_ms"]) > 0
+        assert (st["closest_nodes"] > 0) == (mode == 1)
+    pt.set_profiling(0)
+    with pytest.raises(S.SrtError):
+        pt.set_profiling(3)
+
+
 def test_film_passes_vs_oracle(cuda):
     import torch
     import srt_gb300 as S

@@ -162,3 +162,45 @@ def test_slot_of_a_finished_cached_job_is_emptied(cuda):
         assert np.all(np.isfinite(img)) and np.all(img[:, 3] == 1.0)
     del srv
     S.lib().srt_mlp_destroy(mlp)
+
+
+def test_cached_jobs_equal_alone_and_in_the_mix(cuda):
+    """Cached jobs (frozen network) give the same film alone and packed with
+    plain and other cached jobs: each job's queries, fallback and film
+    updates touch only its own pixels and state."""
+    import srt_gb300 as S
+    cornell, spheres = _scenes(S)
+    cornell.set_aspect(1.0)
+    spheres.set_aspect(1.0)
+    sc1, sc2 = S.Scene(cornell), S.Scene(spheres)
+    nets = []
+    for seed, arr in ((4, cornell), (5, spheres)):
+        verts = np.concatenate([m["vertices"] for m in arr.meshes])
+        lo, hi = verts.min(0) - 0.05, verts.max(0) + 0.05
+        h = C.c_void_p()
+        S.check(S.lib().srt_mlp_create(seed, C.byref(h)))
+        S.check(S.lib().srt_mlp_set_box(h, (C.c_float * 3)(*lo), (C.c_float * 3)(*hi)))
+        nets.append(h)
+    jobs = [(sc1, 48, 4, 8, 31, nets[0]), (sc2, 40, 2, 16, 32, nets[1]), (sc1, 32, 3, 8, 33, None),
+            (sc2, 24, 5, 16, 34, nets[1])]
+
+    def run(subset):
+        srv = S.Server(hbm_budget_bytes=4 << 30, max_paths=1 << 15, max_jobs=8, iterations_per_step=3)
+        F = Films(cuda)
+        films = []
+        for sc, w, spp, md, seed, net in subset:
+            f = F.new(w * w)
+            films.append(f)
+            srv.submit(sc, w, w, pt_params(spp, md, 3, 1, 1, seed), film=f, cache=net)
+        srv.drain(300)
+        out = [F.host(f) for f in films]
+        srv.close()
+        return out
+
+    mixed = run(jobs)
+    for k, job in enumerate(jobs):
+        alone = run([job])[0]
+        np.testing.assert_array_equal(mixed[k], alone)
+        assert np.all(np.isfinite(alone)) and np.all(alone[:, 3] == 1.0)
+    for h in nets:
+        S.lib().srt_mlp_destroy(h)
