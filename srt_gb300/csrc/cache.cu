@@ -40,9 +40,11 @@ struct CacheBuffers {
     float4* b_tgt;
     float4* b_pred;
     float* loss_hist;  // loss of each Adam step of the frame
+    int32_t* g_block;  // valid training vertices per gather block
 };
 
 constexpr int kMaxTrainSteps = 64;
+constexpr int kGatherThreads = 256;  // training-vertex slots per gather block
 
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -70,6 +72,7 @@ CacheBuffers carve(char* base, int64_t npix, int64_t n_train, int res)
     b.b_tgt = (float4*)take(nv * 16);
     b.b_pred = (float4*)take(nv * 16);
     b.loss_hist = (float*)take(kMaxTrainSteps * 4);
+    b.g_block = (int32_t*)take((nv / kGatherThreads + 1) * 4);
     return b;
 }
 
@@ -79,21 +82,59 @@ size_t carve_bytes(int64_t npix, int64_t n_train, int res)
     const size_t nv = (size_t)n_train * kTrainVertices;
     return a256((size_t)npix * 64) + a256((size_t)npix * 16) + a256(64) + a256(cells) + 2 * a256(cells * 16) +
            a256(nv * 64) + a256(nv * 32) + a256((size_t)n_train * 4) + a256(nv * 64) + 2 * a256(nv * 16) +
-           a256(kMaxTrainSteps * 4) + 256;
+           a256(kMaxTrainSteps * 4) + a256((nv / kGatherThreads + 1) * 4) + 256;
 }
 
-// valid training vertices -> contiguous (record, target) batch
-__global__ void k_gather(CacheBuffers b, int n_train, int32_t* count)
+// Valid training vertices -> contiguous (record, target) batch, in vertex
+// order (a stable compaction, so the batch and hence the training steps are
+// the same on every run): k_gather_count counts each block's valid slots,
+// k_gather_scatter places them after the earlier blocks' ones.
+__device__ __forceinline__ bool train_vertex_valid(const CacheBuffers& b, int n_train, int i)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_train * kTrainVertices) return;
-    int ts = i / kTrainVertices, k = i % kTrainVertices;
-    if (k >= b.t_len[ts]) return;
-    float4 tgt = b.t_aux[2 * (size_t)i + 1];
-    if (tgt.w <= 0.0f) return;
-    int slot = atomicAdd(count, 1);
-    for (int j = 0; j < 4; ++j) b.b_rec[4 * (size_t)slot + j] = b.t_rec[4 * (size_t)i + j];
-    b.b_tgt[slot] = tgt;
+    if (i >= n_train * kTrainVertices) return false;
+    const int ts = i / kTrainVertices, k = i % kTrainVertices;
+    return k < b.t_len[ts] && b.t_aux[2 * (size_t)i + 1].w > 0.0f;
+}
+
+__global__ void __launch_bounds__(kGatherThreads) k_gather_count(CacheBuffers b, int n_train)
+{
+    const int i = blockIdx.x * kGatherThreads + threadIdx.x;
+    const int c = __syncthreads_count(train_vertex_valid(b, n_train, i));
+    if (threadIdx.x == 0) b.g_block[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(kGatherThreads) k_gather_scatter(CacheBuffers b, int n_train, int32_t* count)
+{
+    __shared__ int32_t part[kGatherThreads / 32];
+    __shared__ int32_t warp_valid[kGatherThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    // valid slots of the earlier blocks
+    int before = 0;
+    for (int k = t; k < (int)blockIdx.x; k += kGatherThreads) before += b.g_block[k];
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    const int i = blockIdx.x * kGatherThreads + t;
+    const bool valid = train_vertex_valid(b, n_train, i);
+    const uint32_t vb = __ballot_sync(0xffffffffu, valid);
+    if (lane == 0) {
+        part[w] = before;
+        warp_valid[w] = __popc(vb);
+    }
+    __syncthreads();
+    int offset = 0, in_block = 0;
+    for (int k = 0; k < kGatherThreads / 32; ++k) {
+        offset += part[k];
+        if (k < w) in_block += warp_valid[k];
+    }
+    if (valid) {
+        const int slot = offset + in_block + __popc(vb & ((1u << lane) - 1u));
+        for (int j = 0; j < 4; ++j) b.b_rec[4 * (size_t)slot + j] = b.t_rec[4 * (size_t)i + j];
+        b.b_tgt[slot] = b.t_aux[2 * (size_t)i + 1];
+    }
+    if (blockIdx.x == gridDim.x - 1 && t == 0) {
+        int total = 0;
+        for (int k = 0; k < kGatherThreads / 32; ++k) total += warp_valid[k];
+        *count = offset + total;
+    }
 }
 
 __device__ __forceinline__ int cell_of(float4 p, MlpBox box, int r)
@@ -230,7 +271,9 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
     srt_cache_stats out{};
     int32_t host_counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (cp->train) {
-        k_gather<<<(n_train * kTrainVertices + 255) / 256, 256, 0, st>>>(b, n_train, b.q_count + 2);
+        const int gblocks = (n_train * kTrainVertices + kGatherThreads - 1) / kGatherThreads;
+        k_gather_count<<<gblocks, kGatherThreads, 0, st>>>(b, n_train);
+        k_gather_scatter<<<gblocks, kGatherThreads, 0, st>>>(b, n_train, b.q_count + 2);
         SRT_CUDA_TRY(cudaGetLastError());
         SRT_CUDA_TRY(cudaMemcpyAsync(host_counts, b.q_count, 32, cudaMemcpyDeviceToHost, st));
         SRT_CUDA_TRY(cudaStreamSynchronize(st));

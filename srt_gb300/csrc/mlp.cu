@@ -33,12 +33,6 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-__device__ __forceinline__ float2 unpack_bf16(uint32_t u)
-{
-    __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162*>(&u);
-    return __bfloat1622float2(v);
-}
-
 __device__ __forceinline__ void mma16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
 {
     asm volatile(
@@ -363,13 +357,14 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_train(const __nv_bfloat16* 
 
 // dW_l = dZ_l^T A_l over a chunk of rows: M = out, N = in, K = rows.
 // The chunk's rows of dZ_l and A_l are staged in shared memory; each warp
-// owns a set of 16x8 output tiles and adds its partial sums to the FP32
-// gradient with one atomic per element at the end.
-constexpr int kDwRows = 32;  // rows staged per step (two k16 steps)
+// owns a set of 16x8 output tiles and writes its FP32 sums to the chunk's
+// slice of the partial-gradient buffer (summed by k_dw_reduce).
+constexpr int kDwRows = 32;         // rows staged per step (two k16 steps)
+constexpr int kMaxDwChunks = 256;  // row chunks of one weight-gradient pass
 
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_dw(const __nv_bfloat16* __restrict__ act,
                                                         const __nv_bfloat16* __restrict__ dz, int64_t n,
-                                                        int64_t rows_per_block, float* __restrict__ grad)
+                                                        int64_t rows_per_block, float* __restrict__ partial)
 {
     const int l = blockIdx.y;
     const int in = mlp_in(l), out = mlp_out(l);
@@ -422,17 +417,27 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_dw(const __nv_bfloat16* __r
             }
         }
     }
-    float* gl = grad + mlp_offset(l);
+    // this chunk's partial gradient; k_dw_reduce sums the chunks in a fixed
+    // order, so training is deterministic (no floating-point atomics)
+    float* gl = partial + (size_t)blockIdx.x * kMlpParams + mlp_offset(l);
 #pragma unroll
     for (int i = 0; i < 12; ++i) {
         int tile = warp + 4 * i;
         if (tile >= tiles) break;
         int mt = tile / ntiles, nt = tile % ntiles;
         int m0 = mt * 16 + g, n0 = nt * 8 + 2 * t;
-        atomicAdd(gl + m0 * in + n0, acc[i][0]);
-        atomicAdd(gl + m0 * in + n0 + 1, acc[i][1]);
-        atomicAdd(gl + (m0 + 8) * in + n0, acc[i][2]);
-        atomicAdd(gl + (m0 + 8) * in + n0 + 1, acc[i][3]);
+        *reinterpret_cast<float2*>(gl + m0 * in + n0) = make_float2(acc[i][0], acc[i][1]);
+        *reinterpret_cast<float2*>(gl + (m0 + 8) * in + n0) = make_float2(acc[i][2], acc[i][3]);
+    }
+}
+
+// grad += sum of the chunks' partial gradients, chunk 0 first
+__global__ void k_dw_reduce(const float* __restrict__ partial, int chunks, float* __restrict__ grad)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kMlpParams; p += gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int c = 0; c < chunks; ++c) s += __ldg(partial + (size_t)c * kMlpParams + p);
+        grad[p] += s;
     }
 }
 
@@ -517,6 +522,8 @@ namespace {
 
 srt_status ensure_scratch(srt_mlp* p, int64_t n)
 {
+    if (!p->partial.get())
+        SRT_TRY(p->partial.alloc((size_t)kMaxDwChunks * kMlpParams * 4, "mlp gradient partials"));
     if (n <= p->scratch_rows) return SRT_OK;
     int64_t rows = std::max<int64_t>(n, 1 << 16);
     SRT_TRY(p->scratch.alloc((size_t)rows * (kActCols + kGradCols) * 2, "mlp training scratch"));
@@ -566,9 +573,12 @@ srt_status mlp_train_launch(srt_mlp* p, const float4* rec, const float4* target,
     __nv_bfloat16* dz = act + (size_t)p->scratch_rows * kActCols;
     SRT_CUDA_TRY(cudaMemsetAsync(p->loss, 0, 4, st));
     k_mlp_train<<<grid_rows(n), kMlpThreads, train_smem(), st>>>(p->wb, p->box, rec, target, n, act, dz, p->loss);
-    int64_t chunk = std::max<int64_t>(kDwRows, ((n + 255) / 256 + kDwRows - 1) / kDwRows * kDwRows);
-    dim3 grid((unsigned)((n + chunk - 1) / chunk), kMlpLayers);
-    k_mlp_dw<<<grid, kMlpThreads, 0, st>>>(act, dz, n, chunk, p->grad);
+    // at most kMaxDwChunks chunks of a multiple of kDwRows rows
+    int64_t chunk = std::max<int64_t>(kDwRows, ((n + kMaxDwChunks - 1) / kMaxDwChunks + kDwRows - 1) / kDwRows * kDwRows);
+    const int chunks = (int)((n + chunk - 1) / chunk);
+    dim3 grid((unsigned)chunks, kMlpLayers);
+    k_mlp_dw<<<grid, kMlpThreads, 0, st>>>(act, dz, n, chunk, p->partial.as<float>());
+    k_dw_reduce<<<(kMlpParams + 255) / 256, 256, 0, st>>>(p->partial.as<float>(), chunks, p->grad);
     if (update) {
         p->step += 1;
         float c1 = 1.0f - std::pow(p->b1, (float)p->step), c2 = 1.0f - std::pow(p->b2, (float)p->step);

@@ -64,6 +64,7 @@ struct srt_mlp {
     float* grad = nullptr;
     float* loss = nullptr;
     srt::DeviceBuffer scratch;  // per-row layer inputs and gradients for training
+    srt::DeviceBuffer partial;  // per-chunk weight gradients, summed in a fixed order
     int64_t scratch_rows = 0;
     srt::MlpBox box{};
     int64_t step = 0;

@@ -105,6 +105,28 @@ def test_bad_arguments_fail_loudly(cuda):
         pt.render(film, pt_params(1, 8, 3, 1, 1, 0, rng_mode=7))
 
 
+def test_empty_scene_renders_the_environment(cuda):
+    """A scene without triangles (empty BVH, no lights): every camera ray
+    misses, so every pixel is exactly the environment colour."""
+    import torch
+    import srt_gb300 as S
+    sa = S.SceneArrays()
+    sa.camera = _cornell().camera
+    sa.env = (0.25, 0.5, 0.75)
+    sa.set_aspect(1.0)
+    sc = S.Scene(sa)
+    assert sc.info()["num_triangles"] == 0
+    pt = S.PathTracer(sc, 8, 8)
+    film = torch.zeros((64, 4), dtype=torch.float32, device=cuda)
+    pt.render(film, pt_params(3, 8, 3, 1, 1, 9))
+    torch.cuda.synchronize()
+    img = film.cpu().numpy()
+    np.testing.assert_allclose(img[:, :3], np.tile([0.25, 0.5, 0.75], (64, 1)), rtol=1e-6)
+    assert np.all(img[:, 3] == 1.0)
+    st = pt.stats()
+    assert st["samples"] == 64 * 3 and st["shadow_rays"] == 0
+
+
 def test_profiling_modes(cuda):
     """Mode 1: per-kernel times and traversal work counters (counting kernel
     variants); mode 2: times only; both leave the film unchanged; other
