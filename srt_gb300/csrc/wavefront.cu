@@ -335,13 +335,13 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(const float4* __restric
 }
 
 // shading block size and the resident blocks per SM the compiler budgets
-// registers for: 128 x 6 (80 registers, a few spills) measured 2 % faster
-// than 256 x 2 (125 registers, none) and 15 % faster than 256 x 1
+// registers for: 256 x 2 (125 registers, no spills); with the shading order
+// it measured 1 % faster than 128 x 6 (80 registers, spills) and 128 x 4
 #ifndef SRT_SHADE_THREADS
-#define SRT_SHADE_THREADS 128
+#define SRT_SHADE_THREADS 256
 #endif
 #ifndef SRT_SHADE_MIN_BLOCKS
-#define SRT_SHADE_MIN_BLOCKS 6
+#define SRT_SHADE_MIN_BLOCKS 2
 #endif
 constexpr int kShadeThreads = SRT_SHADE_THREADS;
 
