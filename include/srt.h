@@ -459,6 +459,24 @@ srt_status srt_renderer_size(const srt_renderer* r, int32_t* width, int32_t* hei
 srt_status srt_renderer_read_film(const srt_renderer* r, float* host_rgba);
 /* Writes the film as a little-endian PFM (RGB float) to `path`. */
 srt_status srt_renderer_save_pfm(const srt_renderer* r, const char* path);
+/* create_renderer with main.cu's -r / -p / -s overrides (src/main/main.cu:57-62):
+ * each non-NULL JSON text replaces that section of `json_config`. */
+srt_status srt_renderer_create_ex(const char* json_config, const char* render, const char* passes, const char* scene,
+                                  srt_renderer** out);
+/* render.output of the config ("" when absent): the image file name, which
+ * ImageRenderer::run resolves against the config file's directory. */
+const char* srt_renderer_output(const srt_renderer* r);
+/* ImageRenderer::run's save step (renderer.cu:183-187): the film through
+ * srt_image_write with the reference's flip. */
+srt_status srt_renderer_save(const srt_renderer* r, const char* path);
+/* Image::save_to_file (src/scene/texture.cu:219-230, save_ldr / save_hdr
+ * :132-168), host memory in, no GPU needed: rgba is float4[w*h] in film
+ * order (row 0 = bottom of the picture).  By extension: .png (8-bit RGBA,
+ * clamp(x,0,1)*255 truncated), .bmp (24-bit), .hdr (Radiance RGBE), .pfm
+ * (float RGB).  flip != 0 mirrors x and y first, as the reference does
+ * before saving; PFM keeps its bottom-to-top rows.  Other extensions
+ * (.jpg, .exr) return SRT_ERR_UNSUPPORTED. */
+srt_status srt_image_write(const char* path, int32_t width, int32_t height, const float* rgba, int32_t flip);
 void srt_renderer_destroy(srt_renderer* r);
 /* Names of the registered passes, ';'-separated (print_registered_pass). */
 const char* srt_registered_passes(void);

@@ -173,6 +173,10 @@ _PROTOS = [
     ("srt_renderer_size", C.c_int, [C.c_void_p, i32p, i32p]),
     ("srt_renderer_read_film", C.c_int, [C.c_void_p, f32p]),
     ("srt_renderer_save_pfm", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("srt_renderer_create_ex", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_void_p]),
+    ("srt_renderer_output", C.c_char_p, [C.c_void_p]),
+    ("srt_renderer_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("srt_image_write", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]),
     ("srt_renderer_destroy", None, [C.c_void_p]),
     ("srt_registered_passes", C.c_char_p, []),
 ]

@@ -348,6 +348,7 @@ srt_status Renderer::load(const Json& config)
             width = (int)res->arr[0].num;
             height = (int)res->arr[1].num;
         }
+        output = render->string("output", "");
         std::string type = render->string("type", "image");
         if (type != "image") return set_error(SRT_ERR_UNSUPPORTED, "only the image renderer is built (no GUI / video)");
     }
@@ -378,12 +379,33 @@ struct srt_renderer {
 
 extern "C" srt_status srt_renderer_create(const char* json_config, srt_renderer** out)
 {
+    return srt_renderer_create_ex(json_config, nullptr, nullptr, nullptr, out);
+}
+
+extern "C" srt_status srt_renderer_create_ex(const char* json_config, const char* render, const char* passes,
+                                             const char* scene, srt_renderer** out)
+{
     clear_error();
     if (!json_config || !out) return set_error(SRT_ERR_ARG, "NULL argument");
     *out = nullptr;
     Json cfg;
     std::string err;
     if (!Json::parse(json_config, cfg, err)) return set_error(SRT_ERR_PARSE, "config: " + err);
+    if (!cfg.is_object()) return set_error(SRT_ERR_PARSE, "config: not a JSON object");
+    // each given section replaces the config's (src/main/main.cu:57-62)
+    const std::pair<const char*, const char*> over[3] = {{"render", render}, {"passes", passes}, {"scene", scene}};
+    for (const auto& o : over) {
+        if (!o.second) continue;
+        Json sec;
+        if (!Json::parse(o.second, sec, err)) return set_error(SRT_ERR_PARSE, std::string(o.first) + ": " + err);
+        bool found = false;
+        for (auto& kv : cfg.obj)
+            if (kv.first == o.first) {
+                kv.second = sec;
+                found = true;
+            }
+        if (!found) cfg.obj.emplace_back(o.first, sec);
+    }
     srt_renderer* r = new (std::nothrow) srt_renderer();
     if (!r) return set_error(SRT_ERR_OOM, "host allocation failed");
     srt_status st = r->r.load(cfg);
@@ -435,6 +457,17 @@ extern "C" srt_status srt_renderer_save_pfm(const srt_renderer* r, const char* p
         for (int c = 0; c < 3; ++c) rgb[3 * i + c] = rgba[4 * i + c];
     f.write(reinterpret_cast<const char*>(rgb.data()), (std::streamsize)(rgb.size() * 4));
     return f ? SRT_OK : set_error(SRT_ERR_ARG, "write failed");
+}
+
+extern "C" const char* srt_renderer_output(const srt_renderer* r) { return r ? r->r.output.c_str() : ""; }
+
+extern "C" srt_status srt_renderer_save(const srt_renderer* r, const char* path)
+{
+    clear_error();
+    if (!r || !path) return set_error(SRT_ERR_ARG, "NULL argument");
+    std::vector<float> rgba((size_t)r->r.width * r->r.height * 4);
+    SRT_TRY(srt_renderer_read_film(r, rgba.data()));
+    return srt_image_write(path, r->r.width, r->r.height, rgba.data(), 1);
 }
 
 extern "C" void srt_renderer_destroy(srt_renderer* r) { delete r; }

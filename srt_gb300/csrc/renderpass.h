@@ -63,6 +63,7 @@ protected:
     bool enable = true;
     bool online = false;
     int width = 0, height = 0;
+    std::string output;  // render.output: image file name, relative to the config file
     std::shared_ptr<Scene> scene;
 };
 
@@ -89,6 +90,7 @@ public:
     srt_status load(const Json& config);
     srt_status run(int frames);
     int width = 0, height = 0;
+    std::string output;  // render.output: image file name, relative to the config file
     std::shared_ptr<Scene> scene;
     std::shared_ptr<Film> film;
     std::vector<std::shared_ptr<RenderPass>> passes;

@@ -29,7 +29,6 @@ namespace srt {
 
 namespace {
 
-
 constexpr int kThreads = 256;
 constexpr int kTraceThreads = 128;
 constexpr uint32_t kFull = 0xffffffffu;

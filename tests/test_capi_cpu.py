@@ -105,3 +105,88 @@ def test_batch_argument_checks_without_gpu():
     # keep == 0 returns NaN like the reference's 0/0
     assert L.srt_film_metric(None, None, 1, 0, 0.1, None, C.byref(out), None) == 0 and np.isnan(out.value)
     assert L.srt_film_metric_scratch_bytes(1000) >= 4000
+
+
+def _film(w, h):
+    rng = np.random.default_rng(3)
+    f = rng.uniform(-0.2, 1.3, (h * w, 4)).astype(np.float32)
+    f[0, :3] = (2.0, 0.5, 0.25)
+    f[5, :3] = (1e-3, 4e-3, 0.0)
+    return f
+
+
+def _write(path, w, h, film, flip):
+    return S.lib().srt_image_write(str(path).encode(), w, h, film.ctypes.data_as(C.c_void_p), flip)
+
+
+def _flipped(film, w, h):
+    """The reference's save order: film mirrored in x and y (Image::flip(true, true))."""
+    return film.reshape(h, w, 4)[::-1, ::-1]
+
+
+def _u8(x):
+    return (np.clip(np.nan_to_num(x, nan=0.0), 0.0, 1.0) * np.float32(255.0)).astype(np.uint8)
+
+
+def test_image_write_png_bmp(tmp_path):
+    import struct
+    import zlib
+    w, h = 37, 23
+    film = _film(w, h)
+    want = _u8(_flipped(film, w, h))
+    assert _write(tmp_path / "a.png", w, h, film, 1) == 0
+    data = (tmp_path / "a.png").read_bytes()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, ihdr = 8, b"", None
+    while pos < len(data):
+        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        assert struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0] == zlib.crc32(typ + body)
+        if typ == b"IHDR":
+            ihdr = struct.unpack(">IIBBBBB", body)
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    assert ihdr == (w, h, 8, 6, 0, 0, 0)
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, w * 4 + 1)
+    assert np.all(raw[:, 0] == 0)
+    np.testing.assert_array_equal(raw[:, 1:].reshape(h, w, 4), want)
+    # BMP: 24-bit BGR rows bottom to top, padded to 4 bytes
+    assert _write(tmp_path / "a.bmp", w, h, film, 1) == 0
+    b = (tmp_path / "a.bmp").read_bytes()
+    assert b[:2] == b"BM" and struct.unpack("<iiHH", b[18:30]) == (w, h, 1, 24)
+    row = (w * 3 + 3) & ~3
+    px = np.frombuffer(b[54:], np.uint8).reshape(h, row)[::-1, :w * 3].reshape(h, w, 3)
+    np.testing.assert_array_equal(px[..., ::-1], want[..., :3])
+
+
+def test_image_write_hdr_pfm(tmp_path):
+    w, h = 19, 11
+    film = np.abs(_film(w, h))
+    assert _write(tmp_path / "a.hdr", w, h, film, 1) == 0
+    d = (tmp_path / "a.hdr").read_bytes()
+    head, _, body = d.partition(b"\n\n")
+    assert head.startswith(b"#?RADIANCE")
+    dims, _, px = body.partition(b"\n")
+    assert dims == f"-Y {h} +X {w}".encode()
+    e = np.frombuffer(px, np.uint8).reshape(h, w, 4).astype(np.float64)
+    got = np.where(e[..., 3:] > 0, (e[..., :3] + 0.5) * np.ldexp(1.0, e[..., 3:].astype(int) - 136), 0.0)
+    want = _flipped(film, w, h)[..., :3]
+    big = want.max(-1, keepdims=True)
+    assert np.all(np.abs(got - want) <= big / 128 + 1e-30)
+    # PFM: float RGB, rows bottom to top (film order), x mirrored with flip
+    head = f"PF\n{w} {h}\n-1.0\n".encode()
+    assert _write(tmp_path / "a.pfm", w, h, film, 1) == 0
+    p = (tmp_path / "a.pfm").read_bytes()
+    assert p.startswith(head)
+    rgb = np.frombuffer(p[len(head):], np.float32).reshape(h, w, 3)
+    np.testing.assert_array_equal(rgb, film.reshape(h, w, 4)[:, ::-1, :3])
+    assert _write(tmp_path / "b.pfm", w, h, film, 0) == 0
+    rgb0 = np.frombuffer((tmp_path / "b.pfm").read_bytes()[len(head):], np.float32)
+    np.testing.assert_array_equal(rgb0.reshape(h, w, 3), film.reshape(h, w, 4)[..., :3])
+
+
+def test_image_write_rejects_other_formats(tmp_path):
+    film = _film(4, 4)
+    assert _write(tmp_path / "a.jpg", 4, 4, film, 1) == 9  # SRT_ERR_UNSUPPORTED
+    assert _write(tmp_path / "a.png", 0, 4, film, 1) == 1  # SRT_ERR_ARG
