@@ -101,6 +101,24 @@ def build_library(verbose: bool = False) -> str:
     return LIB
 
 
+CLI = os.path.join(HERE, "srt")
+
+
+def build_cli() -> str:
+    """The `srt -c config.json` command (srt_gb300/cli/srt_main.cpp), linked
+    against the library through its C ABI only."""
+    drop_foreign(CLI)
+    src = os.path.join(HERE, "cli", "srt_main.cpp")
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        return CLI
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", CLI, "-L", HERE,
+           "-lsrt_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"cli build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return CLI
+
+
 def build_oracle() -> str:
     """CPU oracle (test infrastructure): oracle/liboracle.so."""
     d = os.path.join(ROOT, "oracle")
@@ -132,5 +150,6 @@ def clean():
 
 if __name__ == "__main__":
     print(build_library(verbose="-v" in sys.argv))
+    print(build_cli())
     print(build_oracle())
     print(build_reference())

@@ -190,3 +190,14 @@ def test_image_write_rejects_other_formats(tmp_path):
     film = _film(4, 4)
     assert _write(tmp_path / "a.jpg", 4, 4, film, 1) == 9  # SRT_ERR_UNSUPPORTED
     assert _write(tmp_path / "a.png", 0, 4, film, 1) == 1  # SRT_ERR_ARG
+
+
+def test_cli_usage_and_missing_config(tmp_path):
+    import subprocess
+    cli = os.path.join(ROOT, "srt_gb300", "srt")
+    r = subprocess.run([cli, "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "-c config.json" in r.stdout
+    r = subprocess.run([cli, "-c", str(tmp_path / "missing.json")], capture_output=True, text=True)
+    assert r.returncode == 1 and "Failed to open file" in r.stderr
+    r = subprocess.run([cli], capture_output=True, text=True)
+    assert r.returncode == 1

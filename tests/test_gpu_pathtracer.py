@@ -6,6 +6,8 @@ differ by an ulp at a Russian-roulette or lobe decision diverges from there,
 so per-pixel equality is asked for most pixels, and every pixel's mean at
 1024 spp must lie within 3 standard errors of the oracle's.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -205,3 +207,47 @@ def test_json_renderer_passes(cuda):
     with pytest.raises(S.SrtError):
         S.Renderer({"render": {"resolution": [8, 8]}, "passes": [{"name": "NoSuchPass"}],
                     "scene": {"model": "procedural:cornell"}})
+
+
+def test_cli_renders_and_saves(cuda, tmp_path):
+    """`srt -c config.json` (src/main/main.cu): renders the config's passes
+    once and saves render.output next to the config; -r replaces the render
+    section.  Each run starts the host frame-seed generator afresh, so the
+    PNG of one run is the 8-bit, x/y-mirrored version of the PFM of the
+    other."""
+    import json
+    import struct
+    import subprocess
+    import zlib
+    w, h = 32, 24
+    cfg = {
+        "render": {"type": "image", "resolution": [w, h], "output": "out.png"},
+        "passes": [{"name": "PathTracer", "params": {"samples_per_pixel": 8, "max_depth": 8, "rr_depth": 3}},
+                   {"name": "ToneMapping", "params": {"type": "ACES", "exposure": 0.0, "use_gamma": True}}],
+        "scene": {"model": "procedural:cornell",
+                  "camera": {"type": "perspective", "position": [0, 0, 3.5], "target": [0, 0, 0],
+                             "up": [0, 1, 0], "fov": 40}},
+    }
+    (tmp_path / "cfg.json").write_text("// comments are allowed\n" + json.dumps(cfg))
+    (tmp_path / "render_pfm.json").write_text(json.dumps({"type": "image", "resolution": [w, h], "output": "out.pfm"}))
+    cli = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "srt_gb300", "srt")
+    r = subprocess.run([cli, "-c", str(tmp_path / "cfg.json")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([cli, "-c", str(tmp_path / "cfg.json"), "-r", str(tmp_path / "render_pfm.json")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    head = f"PF\n{w} {h}\n-1.0\n".encode()
+    pfm = np.frombuffer((tmp_path / "out.pfm").read_bytes()[len(head):], np.float32).reshape(h, w, 3)
+    film = pfm[:, ::-1]  # PFM rows are film rows; x was mirrored
+    assert np.all(np.isfinite(film)) and film.max() > 0.1
+    data = (tmp_path / "out.png").read_bytes()
+    pos, idat = 8, b""
+    while pos < len(data):
+        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        if typ == b"IDAT":
+            idat += data[pos + 8:pos + 8 + n]
+        pos += 12 + n
+    png = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, w * 4 + 1)[:, 1:].reshape(h, w, 4)
+    want = (np.clip(film[::-1, ::-1], 0.0, 1.0) * np.float32(255.0)).astype(np.uint8)
+    np.testing.assert_array_equal(png[..., :3], want)
+    assert np.all(png[..., 3] == 255)
