@@ -96,6 +96,13 @@ typedef enum srt_camera_type {
     SRT_CAMERA_ENVIRONMENT = 3
 } srt_camera_type;
 
+/* Flag OR'd into srt_camera_desc.type: the camera's x axis is
+ * -normalize(cross(up, z)) instead of +normalize(cross(up, z)), the
+ * left-handed frame the reference builds from a pbrt camera transform by
+ * negating the first column of Inverse(Transpose(M))
+ * (src/importer/pbrtparse.cu:346-357).  y stays cross(z, +x). */
+#define SRT_CAMERA_MIRROR_X 0x100
+
 /* The "camera" JSON block of Renderer::load_scene, src/renderer/renderer.cu:125-140:
  * LookAt(position, target, up), radius = |position - target|, vertical fov
  * in degrees, aspect = width / height. */
@@ -440,13 +447,28 @@ srt_status srt_procedural_create(const char* name, uint64_t seed, int32_t n_sphe
 srt_status srt_procedural_desc(const srt_procedural* p, srt_scene_desc* desc);
 void srt_procedural_destroy(srt_procedural* p);
 
+/* Scene file into host arrays (Renderer::load_scene's model loading,
+ * src/renderer/renderer.cu:102-123): ".pbrt" (the PBRTParser subset,
+ * src/importer/pbrtparse.cu: shapes trianglemesh / plymesh, materials
+ * diffuse / coateddiffuse / conductor / dielectric / diffusetransmission,
+ * diffuse area lights, Film resolution and Camera fov and transform),
+ * ".obj" with its ".mtl" (AssimpImporter, src/importer/assimp.cu:17-79) or
+ * a lone ".ply" mesh.  Textures are not built: a pbrt Texture statement or
+ * texture parameter returns SRT_ERR_UNSUPPORTED.  Malformed files return
+ * SRT_ERR_PARSE; unreadable ones SRT_ERR_ARG.  The result is read with
+ * srt_procedural_desc and released with srt_procedural_destroy. */
+srt_status srt_import_scene(const char* path, srt_procedural** out);
+/* Film size a pbrt file asks for (0 x 0 when it gives none). */
+srt_status srt_procedural_resolution(const srt_procedural* p, int32_t* width, int32_t* height);
+
 /* ------------------------------------------------------------------ */
 /* Render-pass plugin API (src/passes/renderpass.h:10-80)               */
 /* ------------------------------------------------------------------ */
 
 /* JSON config with "render", "passes", "scene" (example/example.json).
  * Passes registered: PathTracer, Wavefront, Accumulate, ToneMapping.
- * scene.model: "procedural:cornell" | "procedural:spheres[:n[:subdiv[:seed]]]". */
+ * scene.model: "procedural:cornell" | "procedural:spheres[:n[:subdiv[:seed]]]"
+ * | a scene file (.pbrt, .obj, .ply). */
 typedef struct srt_renderer srt_renderer;
 /* create_renderer + load_scene + load_passes (src/main/main.cu:19-41,
  * src/renderer/renderer.cu:3-17, 42-174). */
@@ -463,6 +485,15 @@ srt_status srt_renderer_save_pfm(const srt_renderer* r, const char* path);
  * each non-NULL JSON text replaces that section of `json_config`. */
 srt_status srt_renderer_create_ex(const char* json_config, const char* render, const char* passes, const char* scene,
                                   srt_renderer** out);
+/* create_renderer(config_path, ...) of src/main/main.cu:19-41 with the same
+ * overrides: reads the config file, and a scene.model that names a file
+ * (.pbrt, .obj, .ply; see srt_import_scene) resolves against the config
+ * file's directory, as Renderer::load_scene does (renderer.cu:44-46).
+ * srt_renderer_create / _ex resolve such paths against the working
+ * directory.  A pbrt film size stands in for an unset render.resolution;
+ * obj / ply scenes need a "camera" block ("No camera specified"). */
+srt_status srt_renderer_create_file(const char* config_path, const char* render, const char* passes,
+                                    const char* scene, srt_renderer** out);
 /* render.output of the config ("" when absent): the image file name, which
  * ImageRenderer::run resolves against the config file's directory. */
 const char* srt_renderer_output(const srt_renderer* r);

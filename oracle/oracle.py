@@ -86,6 +86,7 @@ def ref():
             "ref_bxdf_sample": (None, [C.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
             "ref_bxdf_eval_pdf": (None, [C.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
             "ref_camera_rays": (None, [_vp, _i64, _vp, _vp]),
+            "ref_pbrt_camera_rays": (None, [_vp, C.c_float, C.c_float, _i64, _vp, _vp]),
             "ref_scene_create": (_vp, [_vp]),
             "ref_scene_destroy": (None, [_vp]),
             "ref_light_sample": (None, [_vp, _i64, _vp, _vp]),

@@ -194,6 +194,30 @@ void ref_camera_rays(const srt_camera_desc* cd, int64_t n, const float* xy, floa
     }
 }
 
+// Camera of a pbrt file, built as PBRTParser::parse_options does
+// (src/importer/pbrtparse.cu:331-387): the 16 numbers of its Transform
+// statement row by row into SquareMatrix<4>, Inverse(Transpose(.)), first
+// column negated, CameraController(transform, radius 1).
+void ref_pbrt_camera_rays(const float* m16, float fov, float aspect, int64_t n, const float* xy, float* rays)
+{
+    SquareMatrix<4> mat(m16);
+    mat = Inverse(Transpose(mat));
+    Transform camera_to_world(SquareMatrix<4>(
+        -mat[0][0], mat[0][1], mat[0][2], mat[0][3],
+        -mat[1][0], mat[1][1], mat[1][2], mat[1][3],
+        -mat[2][0], mat[2][1], mat[2][2], mat[2][3],
+        -mat[3][0], mat[3][1], mat[3][2], mat[3][3]));
+    Camera cam(Camera::Type::Perspective, aspect, fov);
+    cam.set_controller(camera_to_world, 1.0f);
+    RandomGenerator rng;
+    for (int64_t i = 0; i < n; ++i) {
+        Ray r = cam.get_ray(xy[2 * i], xy[2 * i + 1], rng);
+        float* o = rays + 8 * i;
+        o[0] = r.pos.x; o[1] = r.pos.y; o[2] = r.pos.z; o[3] = 0.0f;
+        o[4] = r.dir.x; o[5] = r.dir.y; o[6] = r.dir.z; o[7] = 1e16f;
+    }
+}
+
 // Scene set-up following Scene::build_gscene_{materials,meshes,instances}
 // (src/scene/scene.cu:271-418) and TriangleMesh::compute_area
 // (src/scene/mesh.cpp:3-18), in host memory.

@@ -573,7 +573,7 @@ namespace {
 Camera make_camera(const srt_camera_desc& c)
 {
     Camera k;
-    k.type = c.type;
+    k.type = c.type & ~SRT_CAMERA_MIRROR_X;
     F3 pos(c.position[0], c.position[1], c.position[2]);
     F3 tgt(c.target[0], c.target[1], c.target[2]);
     F3 up(c.up[0], c.up[1], c.up[2]);
@@ -582,6 +582,7 @@ Camera make_camera(const srt_camera_desc& c)
     F3 y = cross(z, x);
     k.pos = pos;
     k.x = normalize(x);
+    if (c.type & SRT_CAMERA_MIRROR_X) k.x = k.x * -1.0f;
     k.y = normalize(y);
     k.z = normalize(z);
     k.radius = length(pos - tgt);

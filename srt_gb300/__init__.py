@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 import json as _json
+import os
 
 import numpy as np
 
@@ -18,7 +19,7 @@ from ._capi import (BXDF_DIELECTRIC, BXDF_DIFFUSE, BXDF_DIFFUSE_TRANSMISSION, BX
                     SrtError, check, lib)
 
 __all__ = [
-    "SceneArrays", "Scene", "PathTracer", "procedural", "lib", "check", "SrtError", "bxdf_sample", "bxdf_eval",
+    "SceneArrays", "Scene", "PathTracer", "procedural", "import_scene", "lib", "check", "SrtError", "bxdf_sample", "bxdf_eval",
     "bxdf_generate", "film_accumulate", "film_tonemap", "film_metric", "rng_tape", "Renderer",
 ]
 
@@ -40,6 +41,7 @@ class SceneArrays:
         self.materials = []   # _capi.Material
         self.camera = _capi.CameraDesc()
         self.env = (0.0, 0.0, 0.0)
+        self.resolution = (0, 0)  # film size an imported file asks for
 
     def desc(self):
         n = len(self.meshes)
@@ -79,29 +81,53 @@ class SceneArrays:
         self.camera.aspect = float(aspect)
 
 
+def _arrays_of(h) -> SceneArrays:
+    """Copy of the host scene behind an srt_procedural handle."""
+    L = lib()
+    d = _capi.SceneDesc()
+    check(L.srt_procedural_desc(h, C.byref(d)))
+    s = SceneArrays()
+    for i in range(d.num_meshes):
+        m = d.meshes[i]
+        v = np.ctypeslib.as_array(m.vertices, shape=(m.num_vertices * 3,)).reshape(-1, 3).copy()
+        f = np.ctypeslib.as_array(m.indices, shape=(m.num_faces * 3,)).reshape(-1, 3).copy()
+        n = None
+        if m.normals and m.num_vertices:
+            n = np.ctypeslib.as_array(m.normals, shape=(m.num_vertices * 3,)).reshape(-1, 3).copy()
+        s.meshes.append({"vertices": v, "indices": f, "normals": n, "material": m.material_id})
+    for i in range(d.num_instances):
+        s.instances.append((d.instances[i].mesh_id, np.array(d.instances[i].transform[:], np.float32)))
+    for i in range(d.num_materials):
+        mm = _capi.Material()
+        C.memmove(C.byref(mm), C.byref(d.materials[i]), C.sizeof(_capi.Material))
+        s.materials.append(mm)
+    C.memmove(C.byref(s.camera), C.byref(d.camera), C.sizeof(_capi.CameraDesc))
+    s.env = tuple(d.env_color[:])
+    w, hh = C.c_int32(), C.c_int32()
+    check(L.srt_procedural_resolution(h, C.byref(w), C.byref(hh)))
+    s.resolution = (w.value, hh.value)
+    return s
+
+
 def procedural(name: str, seed: int = 1, n_spheres: int = 64, subdiv: int = 6) -> SceneArrays:
     """Host copy of a generated scene ("cornell" or "spheres")."""
     L = lib()
     h = C.c_void_p()
     check(L.srt_procedural_create(name.encode(), seed, n_spheres, subdiv, C.byref(h)))
     try:
-        d = _capi.SceneDesc()
-        check(L.srt_procedural_desc(h, C.byref(d)))
-        s = SceneArrays()
-        for i in range(d.num_meshes):
-            m = d.meshes[i]
-            v = np.ctypeslib.as_array(m.vertices, shape=(m.num_vertices * 3,)).reshape(-1, 3).copy()
-            f = np.ctypeslib.as_array(m.indices, shape=(m.num_faces * 3,)).reshape(-1, 3).copy()
-            s.meshes.append({"vertices": v, "indices": f, "normals": None, "material": m.material_id})
-        for i in range(d.num_instances):
-            s.instances.append((d.instances[i].mesh_id, np.array(d.instances[i].transform[:], np.float32)))
-        for i in range(d.num_materials):
-            mm = _capi.Material()
-            C.memmove(C.byref(mm), C.byref(d.materials[i]), C.sizeof(_capi.Material))
-            s.materials.append(mm)
-        C.memmove(C.byref(s.camera), C.byref(d.camera), C.sizeof(_capi.CameraDesc))
-        s.env = tuple(d.env_color[:])
-        return s
+        return _arrays_of(h)
+    finally:
+        L.srt_procedural_destroy(h)
+
+
+def import_scene(path: str) -> SceneArrays:
+    """Host copy of a scene file (.pbrt, .obj + .mtl, .ply) read by
+    srt_import_scene; `resolution` holds the pbrt Film size or (0, 0)."""
+    L = lib()
+    h = C.c_void_p()
+    check(L.srt_import_scene(os.fsencode(path), C.byref(h)))
+    try:
+        return _arrays_of(h)
     finally:
         L.srt_procedural_destroy(h)
 
@@ -243,10 +269,16 @@ def rng_tape(seed, npix, ndraws, out, stream=0):
 class Renderer:
     """JSON-configured renderer (render / passes / scene) over the C ABI."""
 
-    def __init__(self, config):
-        text = config if isinstance(config, str) else _json.dumps(config)
+    def __init__(self, config=None, *, path=None):
+        """config: JSON text or dict (scene files resolve against the working
+        directory); path: a config file (scene files resolve against its
+        directory, srt_renderer_create_file)."""
         self.handle = C.c_void_p()
-        check(lib().srt_renderer_create(text.encode(), C.byref(self.handle)))
+        if path is not None:
+            check(lib().srt_renderer_create_file(os.fsencode(path), None, None, None, C.byref(self.handle)))
+        else:
+            text = config if isinstance(config, str) else _json.dumps(config)
+            check(lib().srt_renderer_create(text.encode(), C.byref(self.handle)))
         w, h = C.c_int32(), C.c_int32()
         check(lib().srt_renderer_size(self.handle, C.byref(w), C.byref(h)))
         self.width, self.height = w.value, h.value

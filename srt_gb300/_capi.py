@@ -20,6 +20,7 @@ STATUS_NAMES = {
 
 BXDF_DIFFUSE, BXDF_DIFFUSE_TRANSMISSION, BXDF_DIELECTRIC, BXDF_DISNEY = 0, 1, 2, 3
 CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC = 0, 1
+CAMERA_MIRROR_X = 0x100  # flag OR'd into CameraDesc.type (left-handed pbrt camera frame)
 RNG_CURAND, RNG_HASH = 0, 1
 PT_FIXED_CDF_REMAP = 1
 TONE_NONE, TONE_CLAMP, TONE_REINHARD, TONE_UNCHARTED2, TONE_ACES = 0, 1, 2, 3, 4
@@ -168,12 +169,15 @@ _PROTOS = [
     ("srt_procedural_create", C.c_int, [C.c_char_p, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     ("srt_procedural_desc", C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
     ("srt_procedural_destroy", None, [C.c_void_p]),
+    ("srt_import_scene", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("srt_procedural_resolution", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     ("srt_renderer_create", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     ("srt_renderer_run", C.c_int, [C.c_void_p, C.c_int32]),
     ("srt_renderer_size", C.c_int, [C.c_void_p, i32p, i32p]),
     ("srt_renderer_read_film", C.c_int, [C.c_void_p, f32p]),
     ("srt_renderer_save_pfm", C.c_int, [C.c_void_p, C.c_char_p]),
     ("srt_renderer_create_ex", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_void_p]),
+    ("srt_renderer_create_file", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_void_p]),
     ("srt_renderer_output", C.c_char_p, [C.c_void_p]),
     ("srt_renderer_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("srt_image_write", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]),

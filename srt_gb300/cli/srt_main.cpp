@@ -1,7 +1,8 @@
 // srt — command-line renderer (src/main/main.cu): reads a JSON config with
 // "render", "passes" and "scene" sections, lets -r / -p / -s replace a
 // section with the contents of another file, renders once with the image
-// renderer and saves render.output next to the config file.  Uses only the
+// renderer and saves render.output next to the config file; a scene file
+// named by scene.model is found next to the config file too.  Uses only the
 // library's C ABI (include/srt.h).
 //
 //   srt -c config.json [-r render.json] [-p passes.json] [-s scene.json]
@@ -50,14 +51,14 @@ int main(int argc, char* argv[])
         return 1;
     }
     std::string text[4];
-    for (int k = 0; k < 4; ++k)
+    for (int k = 1; k < 4; ++k)
         if (!paths[k].empty() && !read_file(paths[k], text[k])) {
             std::fprintf(stderr, "ERROR::Failed to open file: %s\n", paths[k].c_str());
             return 1;
         }
     auto opt = [&](int k) { return paths[k].empty() ? nullptr : text[k].c_str(); };
     srt_renderer* r = nullptr;
-    if (srt_renderer_create_ex(text[0].c_str(), opt(1), opt(2), opt(3), &r) != SRT_OK) return fail("config");
+    if (srt_renderer_create_file(paths[0].c_str(), opt(1), opt(2), opt(3), &r) != SRT_OK) return fail("config");
     const auto t0 = std::chrono::steady_clock::now();
     if (srt_renderer_run(r, 1) != SRT_OK) return fail("render");
     const auto t1 = std::chrono::steady_clock::now();

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "common.h"
+#include "host_scene.h"
 
 namespace {
 
@@ -65,18 +66,7 @@ float value_noise(float x, float y, float z, uint32_t seed)
     return L(L(x00, x10, ty), L(x01, x11, ty), tz);
 }
 
-struct Mesh {
-    std::vector<float> v;
-    std::vector<uint32_t> idx;
-    int material;
-    void quad(const float* a, const float* b, const float* c, const float* d)
-    {
-        uint32_t base = (uint32_t)(v.size() / 3);
-        for (const float* p : {a, b, c, d}) v.insert(v.end(), p, p + 3);
-        uint32_t t[6] = {base, base + 1, base + 2, base, base + 2, base + 3};
-        idx.insert(idx.end(), t, t + 6);
-    }
-};
+using Mesh = srt::HostMesh;
 
 srt_material lambert(float r, float g, float b)
 {
@@ -167,43 +157,6 @@ void icosphere(int subdiv, std::vector<float>& v, std::vector<uint32_t>& f)
 
 }  // namespace
 
-struct srt_procedural {
-    std::vector<Mesh> meshes;
-    std::vector<srt_mesh> mesh_desc;
-    std::vector<srt_instance> inst;
-    std::vector<srt_material> mats;
-    srt_scene_desc desc{};
-
-    void finish(const srt_camera_desc& cam, const float env[3])
-    {
-        mesh_desc.clear();
-        inst.clear();
-        for (size_t i = 0; i < meshes.size(); ++i) {
-            srt_mesh d{};
-            d.vertices = meshes[i].v.data();
-            d.indices = meshes[i].idx.data();
-            d.normals = nullptr;
-            d.num_vertices = (int32_t)(meshes[i].v.size() / 3);
-            d.num_faces = (int32_t)(meshes[i].idx.size() / 3);
-            d.material_id = meshes[i].material;
-            mesh_desc.push_back(d);
-            srt_instance in{};
-            in.mesh_id = (int32_t)i;
-            float id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
-            std::memcpy(in.transform, id, sizeof(id));
-            inst.push_back(in);
-        }
-        desc.meshes = mesh_desc.data();
-        desc.num_meshes = (int32_t)mesh_desc.size();
-        desc.instances = inst.data();
-        desc.num_instances = (int32_t)inst.size();
-        desc.materials = mats.data();
-        desc.num_materials = (int32_t)mats.size();
-        desc.camera = cam;
-        for (int k = 0; k < 3; ++k) desc.env_color[k] = env[k];
-    }
-};
-
 namespace {
 
 // Cornell box: [-1,1]^3 open at +z; tall box 0.6x1.2x0.6 rotated +15 deg,
@@ -248,6 +201,7 @@ void make_cornell(srt_procedural& p)
     cam.aspect = 1.0f;
     cam.focal = 1.0f;
     const float env[3] = {0.0f, 0.0f, 0.0f};
+    p.has_camera = true;
     p.finish(cam, env);
 }
 
@@ -327,6 +281,7 @@ void make_spheres(srt_procedural& p, uint64_t seed, int n_spheres, int subdiv)
     cam.aspect = 16.0f / 9.0f;
     cam.focal = 1.0f;
     const float env[3] = {0.05f, 0.05f, 0.05f};
+    p.has_camera = true;
     p.finish(cam, env);
 }
 

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "common.h"
+#include "host_scene.h"
 #include "renderpass.h"
 
 namespace srt {
@@ -275,18 +276,28 @@ srt_status Renderer::load_scene(const Json& config)
 {
     std::string model = config.string("model", "");
     const std::string pre = "procedural:";
-    if (model.compare(0, pre.size(), pre) != 0)
-        return set_error(SRT_ERR_UNSUPPORTED, "scene.model must be procedural:<name> (file importers are not built)");
-    std::vector<std::string> parts;
-    std::stringstream ss(model.substr(pre.size()));
-    std::string tok;
-    while (std::getline(ss, tok, ':')) parts.push_back(tok);
-    if (parts.empty()) return set_error(SRT_ERR_ARG, "empty procedural scene name");
-    int n_spheres = parts.size() > 1 ? std::atoi(parts[1].c_str()) : 64;
-    int subdiv = parts.size() > 2 ? std::atoi(parts[2].c_str()) : 6;
-    uint64_t seed = parts.size() > 3 ? std::strtoull(parts[3].c_str(), nullptr, 10) : 1;
     scene = std::make_shared<Scene>();
-    SRT_TRY(srt_procedural_create(parts[0].c_str(), seed, n_spheres, subdiv, &scene->proc));
+    if (model.compare(0, pre.size(), pre) == 0) {
+        std::vector<std::string> parts;
+        std::stringstream ss(model.substr(pre.size()));
+        std::string tok;
+        while (std::getline(ss, tok, ':')) parts.push_back(tok);
+        if (parts.empty()) return set_error(SRT_ERR_ARG, "empty procedural scene name");
+        int n_spheres = parts.size() > 1 ? std::atoi(parts[1].c_str()) : 64;
+        int subdiv = parts.size() > 2 ? std::atoi(parts[2].c_str()) : 6;
+        uint64_t seed = parts.size() > 3 ? std::strtoull(parts[3].c_str(), nullptr, 10) : 1;
+        SRT_TRY(srt_procedural_create(parts[0].c_str(), seed, n_spheres, subdiv, &scene->proc));
+    } else {
+        // a scene file beside the config (renderer.cu:44-63): the pbrt film
+        // size stands in for an unset resolution
+        if (model.empty()) return set_error(SRT_ERR_ARG, "scene.model is empty");
+        const std::string path = model[0] == '/' ? model : base_dir + model;
+        SRT_TRY(srt_import_scene(path.c_str(), &scene->proc));
+        if ((width == 0 || height == 0) && scene->proc->width > 0 && scene->proc->height > 0) {
+            width = scene->proc->width;
+            height = scene->proc->height;
+        }
+    }
     if (width == 0 || height == 0) {
         width = 1920;
         height = 1080;
@@ -294,6 +305,7 @@ srt_status Renderer::load_scene(const Json& config)
     srt_scene_desc desc;
     SRT_TRY(srt_procedural_desc(scene->proc, &desc));
     desc.camera.aspect = (float)width / (float)height;
+    if (!scene->proc->has_camera && !config.find("camera")) return set_error(SRT_ERR_ARG, "No camera specified");
     if (const Json* cam = config.find("camera")) {
         float pos[3], tgt[3], up[3];
         if (!vec3(cam->find("position"), pos) || !vec3(cam->find("target"), tgt) || !vec3(cam->find("up"), up))
@@ -377,15 +389,11 @@ struct srt_renderer {
     Renderer r;
 };
 
-extern "C" srt_status srt_renderer_create(const char* json_config, srt_renderer** out)
-{
-    return srt_renderer_create_ex(json_config, nullptr, nullptr, nullptr, out);
-}
+namespace {
 
-extern "C" srt_status srt_renderer_create_ex(const char* json_config, const char* render, const char* passes,
-                                             const char* scene, srt_renderer** out)
+srt_status create_renderer(const char* json_config, const std::string& base_dir, const char* render,
+                           const char* passes, const char* scene, srt_renderer** out)
 {
-    clear_error();
     if (!json_config || !out) return set_error(SRT_ERR_ARG, "NULL argument");
     *out = nullptr;
     Json cfg;
@@ -408,6 +416,7 @@ extern "C" srt_status srt_renderer_create_ex(const char* json_config, const char
     }
     srt_renderer* r = new (std::nothrow) srt_renderer();
     if (!r) return set_error(SRT_ERR_OOM, "host allocation failed");
+    r->r.base_dir = base_dir;
     srt_status st = r->r.load(cfg);
     if (st != SRT_OK) {
         delete r;
@@ -415,6 +424,36 @@ extern "C" srt_status srt_renderer_create_ex(const char* json_config, const char
     }
     *out = r;
     return SRT_OK;
+}
+
+}  // namespace
+
+extern "C" srt_status srt_renderer_create(const char* json_config, srt_renderer** out)
+{
+    clear_error();
+    return create_renderer(json_config, "", nullptr, nullptr, nullptr, out);
+}
+
+extern "C" srt_status srt_renderer_create_ex(const char* json_config, const char* render, const char* passes,
+                                             const char* scene, srt_renderer** out)
+{
+    clear_error();
+    return create_renderer(json_config, "", render, passes, scene, out);
+}
+
+extern "C" srt_status srt_renderer_create_file(const char* config_path, const char* render, const char* passes,
+                                               const char* scene, srt_renderer** out)
+{
+    clear_error();
+    if (!config_path || !out) return set_error(SRT_ERR_ARG, "NULL argument");
+    std::ifstream f(config_path, std::ios::binary);
+    if (!f) return set_error(SRT_ERR_ARG, std::string("Failed to open file: ") + config_path);
+    std::ostringstream text;
+    text << f.rdbuf();
+    const std::string p(config_path);
+    const size_t slash = p.find_last_of('/');
+    return create_renderer(text.str().c_str(), slash == std::string::npos ? std::string() : p.substr(0, slash + 1),
+                           render, passes, scene, out);
 }
 
 extern "C" srt_status srt_renderer_run(srt_renderer* r, int32_t frames)

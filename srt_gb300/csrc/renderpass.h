@@ -63,7 +63,6 @@ protected:
     bool enable = true;
     bool online = false;
     int width = 0, height = 0;
-    std::string output;  // render.output: image file name, relative to the config file
     std::shared_ptr<Scene> scene;
 };
 
@@ -91,6 +90,7 @@ public:
     srt_status run(int frames);
     int width = 0, height = 0;
     std::string output;  // render.output: image file name, relative to the config file
+    std::string base_dir;  // directory of the config file ("" or ending in '/'): scene files resolve against it
     std::shared_ptr<Scene> scene;
     std::shared_ptr<Film> film;
     std::vector<std::shared_ptr<RenderPass>> passes;

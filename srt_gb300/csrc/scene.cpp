@@ -60,7 +60,8 @@ srt_status validate(const srt_scene_desc* d)
     for (int i = 0; i < d->num_instances; ++i)
         if (d->instances[i].mesh_id < 0 || d->instances[i].mesh_id >= d->num_meshes)
             return set_error(SRT_ERR_ARG, "instance " + std::to_string(i) + ": mesh id out of range");
-    if (d->camera.type != SRT_CAMERA_PERSPECTIVE && d->camera.type != SRT_CAMERA_ORTHOGRAPHIC)
+    const int cam_type = d->camera.type & ~SRT_CAMERA_MIRROR_X;
+    if (cam_type != SRT_CAMERA_PERSPECTIVE && cam_type != SRT_CAMERA_ORTHOGRAPHIC)
         return set_error(SRT_ERR_UNSUPPORTED, "only perspective and orthographic cameras are supported");
     return SRT_OK;
 }
@@ -100,6 +101,7 @@ CameraRec make_camera(const srt_camera_desc& c)
     CameraRec k{};
     k.pos = pos;
     k.x = normalize(x);
+    if (c.type & SRT_CAMERA_MIRROR_X) k.x = -1.0f * k.x;
     k.y = normalize(y);
     k.z = normalize(z);
     k.radius = length(pos - tgt);
@@ -108,7 +110,7 @@ CameraRec make_camera(const srt_camera_desc& c)
     k.nw = k.nh * c.aspect;
     k.aperture = c.aperture;
     k.focal = c.focal;
-    k.type = c.type;
+    k.type = c.type & ~SRT_CAMERA_MIRROR_X;
     return k;
 }
 
@@ -307,7 +309,8 @@ extern "C" srt_status srt_scene_set_camera(srt_scene* s, const srt_camera_desc* 
 {
     clear_error();
     if (!s || !c) return set_error(SRT_ERR_ARG, "NULL argument");
-    if (c->type != SRT_CAMERA_PERSPECTIVE && c->type != SRT_CAMERA_ORTHOGRAPHIC)
+    const int cam_type = c->type & ~SRT_CAMERA_MIRROR_X;
+    if (cam_type != SRT_CAMERA_PERSPECTIVE && cam_type != SRT_CAMERA_ORTHOGRAPHIC)
         return set_error(SRT_ERR_UNSUPPORTED, "only perspective and orthographic cameras are supported");
     s->camera_desc = *c;
     s->camera = make_camera(*c);

@@ -100,6 +100,49 @@ def camera_set():
     np.savez_compressed(os.path.join(OUT, "camera.npz"), **out)
 
 
+def pbrt_lookat(eye, look, up, mirror=False):
+    """The 16 numbers of a pbrt `Transform` statement for a camera made by
+    pbrt's LookAt (camera-from-world; pbrt lists a matrix column by column),
+    after an optional `Scale -1 1 1`."""
+    eye, look, up = (np.asarray(a, np.float64) for a in (eye, look, up))
+    d = look - eye
+    d /= np.linalg.norm(d)
+    right = np.cross(up / np.linalg.norm(up), d)
+    right /= np.linalg.norm(right)
+    new_up = np.cross(d, right)
+    world_from_camera = np.eye(4)
+    world_from_camera[:3, 0], world_from_camera[:3, 1], world_from_camera[:3, 2] = right, new_up, d
+    world_from_camera[:3, 3] = eye
+    m = np.linalg.inv(world_from_camera)
+    if mirror:
+        m = np.diag([-1.0, 1.0, 1.0, 1.0]) @ m
+    return m.T.reshape(16).astype(np.float32)
+
+
+PBRT_CAMERAS = (
+    ("front", ([0.3, 1.2, 4.0], [0.0, 0.5, 0.0], [0.0, 1.0, 0.0]), False, 40.0, 4 / 3),
+    ("above", ([-2.0, 3.0, -1.0], [0.5, 0.0, 0.2], [0.0, 1.0, 0.0]), False, 55.0, 16 / 9),
+    ("tilted", ([1.0, 1.0, 1.0], [0.0, 0.0, 0.0], [0.1, 0.9, 0.2]), False, 30.0, 1.0),
+    ("mirrored", ([0.5, 1.5, -3.0], [0.0, 1.0, 0.0], [0.0, 1.0, 0.0]), True, 45.0, 1.5),
+)
+
+
+def pbrt_camera_set():
+    """Rays of the reference's pbrt camera (PBRTParser::parse_options)."""
+    out = {}
+    rng = np.random.default_rng(12)
+    xy = rng.random((256, 2), dtype=np.float32)
+    for name, look, mirror, fov, aspect in PBRT_CAMERAS:
+        m16 = pbrt_lookat(*look, mirror=mirror)
+        rays = np.zeros((256, 8), np.float32)
+        O.ref().ref_pbrt_camera_rays(_np(m16), fov, aspect, 256, _np(xy), _np(rays))
+        out[f"{name}_m16"] = m16
+        out[f"{name}_fov_aspect"] = np.array([fov, aspect], np.float32)
+        out[f"{name}_rays"] = rays
+    out["xy"] = xy
+    np.savez_compressed(os.path.join(OUT, "pbrt_camera.npz"), **out)
+
+
 def scene_arrays_to_npz(s):
     out = {}
     out["num_meshes"] = np.int32(len(s.meshes))
@@ -158,5 +201,6 @@ if __name__ == "__main__":
     O.build()
     bxdf_sets()
     camera_set()
+    pbrt_camera_set()
     scene_set()
     print("golden vectors written to", OUT)

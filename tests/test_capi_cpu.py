@@ -63,7 +63,9 @@ def test_config_parse_errors_and_unknown_names():
     h = C.c_void_p()
     assert L.srt_renderer_create(b"{ not json", C.byref(h)) == 8
     assert b"offset" in L.srt_last_error()
-    cfg = b'{"render": {"resolution": [4, 4]}, "passes": [], "scene": {"model": "cornell_box.obj"}}'
+    cfg = b'{"render": {"resolution": [4, 4]}, "passes": [], "scene": {"model": "no_such_dir/cornell_box.obj"}}'
+    assert L.srt_renderer_create(cfg, C.byref(h)) == 1  # a scene file that cannot be opened
+    cfg = b'{"render": {"resolution": [4, 4]}, "passes": [], "scene": {"model": "cornell_box.gltf"}}'
     assert L.srt_renderer_create(cfg, C.byref(h)) == 9
     cfg = b'{"render": {"type": "interactive"}, "passes": [], "scene": {"model": "procedural:cornell"}}'
     assert L.srt_renderer_create(cfg, C.byref(h)) == 9
