@@ -304,6 +304,12 @@ enum { SRT_METRIC_MSE = 0, SRT_METRIC_MAPE = 1, SRT_METRIC_SMAPE = 2, SRT_METRIC
  * `scratch` is a device buffer of at least srt_film_metric_scratch_bytes(n)
  * bytes owned by the caller; *out (host) receives the trimmed mean. */
 size_t srt_film_metric_scratch_bytes(int64_t n);
+/* Measure's "option" (measure.h:16, measure.cu:29-39): REFERENCE overwrites
+ * the film with (ref.rgb, 1), ERROR with the per-pixel error of `type` as
+ * (e, e, e, 1); NONE leaves it.  Both buffers float4[n] on the device. */
+enum { SRT_MEASURE_NONE = 0, SRT_MEASURE_REFERENCE = 1, SRT_MEASURE_ERROR = 2 };
+srt_status srt_film_measure_view(float* film, const float* ref, int64_t n, int32_t type, int32_t option,
+                                 void* stream);
 srt_status srt_film_metric(const float* x, const float* ref, int64_t n, int32_t type,
                            float discard, void* scratch, float* out, void* stream);
 
@@ -504,10 +510,22 @@ srt_status srt_renderer_save(const srt_renderer* r, const char* path);
  * :132-168), host memory in, no GPU needed: rgba is float4[w*h] in film
  * order (row 0 = bottom of the picture).  By extension: .png (8-bit RGBA,
  * clamp(x,0,1)*255 truncated), .bmp (24-bit), .hdr (Radiance RGBE), .pfm
- * (float RGB).  flip != 0 mirrors x and y first, as the reference does
- * before saving; PFM keeps its bottom-to-top rows.  Other extensions
- * (.jpg, .exr) return SRT_ERR_UNSUPPORTED. */
+ * (float RGB), .exr (OpenEXR: channels B, G, R, A as half, no
+ * compression, as the reference's save_exr writes them through tinyexr,
+ * :69-130).  flip != 0 mirrors x and y first, as the reference does before
+ * saving; PFM keeps its bottom-to-top rows.  Other extensions (.jpg)
+ * return SRT_ERR_UNSUPPORTED. */
 srt_status srt_image_write(const char* path, int32_t width, int32_t height, const float* rgba, int32_t flip);
+/* Image::load_from_file for float images (texture.cu:170-217), by content:
+ * OpenEXR (single-part scanline; half / float / uint; no compression, RLE,
+ * ZIPS or ZIP; R, G, B and optional A, or one grey channel), Radiance HDR
+ * (converted as stbi_loadf does) and PFM.  rgba == NULL asks for the size
+ * only; otherwise rgba receives float4[w*h].  flip != 0 undoes
+ * srt_image_write's flip (for EXR / HDR: the reference's
+ * load_from_file(path, true, true), which the Measure pass uses), so a
+ * film written with flip and read with flip comes back in film order.
+ * 8-bit formats return SRT_ERR_UNSUPPORTED; malformed files SRT_ERR_PARSE. */
+srt_status srt_image_read(const char* path, int32_t* width, int32_t* height, float* rgba, int32_t flip);
 void srt_renderer_destroy(srt_renderer* r);
 /* Names of the registered passes, ';'-separated (print_registered_pass). */
 const char* srt_registered_passes(void);

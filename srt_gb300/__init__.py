@@ -20,7 +20,8 @@ from ._capi import (BXDF_DIELECTRIC, BXDF_DIFFUSE, BXDF_DIFFUSE_TRANSMISSION, BX
 
 __all__ = [
     "SceneArrays", "Scene", "PathTracer", "procedural", "import_scene", "lib", "check", "SrtError", "bxdf_sample", "bxdf_eval",
-    "bxdf_generate", "film_accumulate", "film_tonemap", "film_metric", "rng_tape", "Renderer",
+    "bxdf_generate", "film_accumulate", "film_tonemap", "film_metric", "film_measure_view", "rng_tape", "Renderer", "image_write",
+    "image_read",
 ]
 
 DISNEY_PARAM_NAMES = ("ior", "metallic", "subsurface", "roughness", "specular", "specularTint", "anisotropic",
@@ -107,6 +108,23 @@ def _arrays_of(h) -> SceneArrays:
     check(L.srt_procedural_resolution(h, C.byref(w), C.byref(hh)))
     s.resolution = (w.value, hh.value)
     return s
+
+
+def image_write(path, rgba, width, height, flip=True):
+    """srt_image_write of float4[w*h] host pixels (film order)."""
+    px = np.ascontiguousarray(rgba, np.float32).reshape(-1)
+    assert px.size == 4 * width * height
+    check(lib().srt_image_write(os.fsencode(str(path)), width, height, _ptr(px), 1 if flip else 0))
+
+
+def image_read(path, flip=True):
+    """srt_image_read: (float4[w*h] array, width, height) of an exr / hdr / pfm."""
+    L = lib()
+    w, h = C.c_int32(), C.c_int32()
+    check(L.srt_image_read(os.fsencode(str(path)), C.byref(w), C.byref(h), None, 1 if flip else 0))
+    out = np.empty((w.value * h.value, 4), np.float32)
+    check(L.srt_image_read(os.fsencode(str(path)), C.byref(w), C.byref(h), _ptr(out), 1 if flip else 0))
+    return out, w.value, h.value
 
 
 def procedural(name: str, seed: int = 1, n_spheres: int = 64, subdiv: int = 6) -> SceneArrays:
@@ -262,6 +280,12 @@ def film_metric(x, ref, type_, discard=0.1, scratch=None, stream=0):
     return out.value
 
 
+def film_measure_view(film, ref, type_, option, stream=0):
+    """Measure's display option on device float4 tensors (in place on film)."""
+    check(lib().srt_film_measure_view(C.c_void_p(film.data_ptr()), C.c_void_p(ref.data_ptr()), film.shape[0], type_,
+                                      option, C.c_void_p(stream)))
+
+
 def rng_tape(seed, npix, ndraws, out, stream=0):
     check(lib().srt_rng_tape(seed, npix, ndraws, C.c_void_p(out.data_ptr()), C.c_void_p(stream)))
 
@@ -293,6 +317,11 @@ class Renderer:
 
     def save_pfm(self, path):
         check(lib().srt_renderer_save_pfm(self.handle, str(path).encode()))
+
+    def save(self, path):
+        """The film through srt_image_write with the reference's flip
+        (png, bmp, hdr, pfm, exr by extension)."""
+        check(lib().srt_renderer_save(self.handle, str(path).encode()))
 
     def close(self):
         if self.handle:

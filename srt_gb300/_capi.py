@@ -25,6 +25,7 @@ RNG_CURAND, RNG_HASH = 0, 1
 PT_FIXED_CDF_REMAP = 1
 TONE_NONE, TONE_CLAMP, TONE_REINHARD, TONE_UNCHARTED2, TONE_ACES = 0, 1, 2, 3, 4
 METRIC_MSE, METRIC_MAPE, METRIC_SMAPE, METRIC_RELMSE = 0, 1, 2, 3
+MEASURE_NONE, MEASURE_REFERENCE, MEASURE_ERROR = 0, 1, 2
 
 f32p = C.POINTER(C.c_float)
 u32p = C.POINTER(C.c_uint32)
@@ -142,6 +143,7 @@ _PROTOS = [
     ("srt_film_accumulate", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
     ("srt_film_tonemap", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_float, C.c_int32, C.c_void_p]),
     ("srt_film_metric_scratch_bytes", C.c_size_t, [C.c_int64]),
+    ("srt_film_measure_view", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p]),
     ("srt_film_metric", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_float, C.c_void_p,
                                   f32p, C.c_void_p]),
     ("srt_mlp_create", C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
@@ -181,6 +183,7 @@ _PROTOS = [
     ("srt_renderer_output", C.c_char_p, [C.c_void_p]),
     ("srt_renderer_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("srt_image_write", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]),
+    ("srt_image_read", C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_int32]),
     ("srt_renderer_destroy", None, [C.c_void_p]),
     ("srt_registered_passes", C.c_char_p, []),
 ]

@@ -93,6 +93,23 @@ __device__ __forceinline__ float pixel_error(float4 xa, float4 ra, int type)
     return dot(t, t) / 3.0f;
 }
 
+// Measure's display options (measure.cu:29-39): the film shows the
+// reference, or each pixel's error as grey.
+__global__ void __launch_bounds__(kThreads) k_measure_view(float4* __restrict__ film, const float4* __restrict__ r,
+                                                           int64_t n, int type, int option)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float4 ref = __ldg(r + i);
+        if (option == SRT_MEASURE_REFERENCE) {
+            film[i] = make_float4(ref.x, ref.y, ref.z, 1.0f);
+        } else {
+            const float e = pixel_error(film[i], ref, type);
+            film[i] = make_float4(e, e, e, 1.0f);
+        }
+    }
+}
+
 // Radix-select scratch (after the per-pixel error array).
 struct SelectState {
     uint32_t prefix;       // bits of the cut value fixed so far
@@ -249,6 +266,24 @@ extern "C" srt_status srt_film_tonemap(float* film, int64_t n, int32_t type, flo
 }
 
 extern "C" size_t srt_film_metric_scratch_bytes(int64_t n) { return n < 0 ? 0 : scratch_bytes(n); }
+
+extern "C" srt_status srt_film_measure_view(float* film, const float* ref, int64_t n, int32_t type, int32_t option,
+                                            void* stream)
+{
+    clear_error();
+    if (n < 0 || type < SRT_METRIC_MSE || type > SRT_METRIC_RELMSE || option < SRT_MEASURE_NONE ||
+        option > SRT_MEASURE_ERROR)
+        return set_error(SRT_ERR_ARG, "bad arguments");
+    if (n == 0 || option == SRT_MEASURE_NONE) return SRT_OK;
+    if (!film || !ref) return set_error(SRT_ERR_ARG, "NULL buffer");
+    if ((reinterpret_cast<uintptr_t>(film) | reinterpret_cast<uintptr_t>(ref)) % 16)
+        return set_error(SRT_ERR_ARG, "film buffers must be 16-byte aligned");
+    k_measure_view<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(reinterpret_cast<float4*>(film),
+                                                                    reinterpret_cast<const float4*>(ref), n, type,
+                                                                    option);
+    SRT_CUDA_TRY(cudaGetLastError());
+    return SRT_OK;
+}
 
 extern "C" srt_status srt_film_metric(const float* x, const float* ref, int64_t n, int32_t type, float discard,
                                       void* scratch, float* out, void* stream)

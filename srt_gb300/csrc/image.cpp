@@ -1,25 +1,40 @@
 // image.cpp — film images on disk (Image::save_to_file, src/scene/texture.cu:
-// 219-230 with save_ldr / save_hdr :132-168).  Host code only.
+// 219-230 with save_exr / save_hdr / save_ldr :69-168, and
+// Image::load_from_file :170-217 for float images).  Host code only.
 //
 //   .png  8-bit RGBA, channels clamp(x, 0, 1) * 255 truncated (Image::f_to_u,
 //         texture.cu:11-21); zlib stream of stored (uncompressed) deflate blocks
 //   .bmp  24-bit BGR, same 8-bit conversion
 //   .hdr  Radiance RGBE, flat (not run-length encoded) scanlines
 //   .pfm  float RGB
+//   .exr  OpenEXR scanline file, channels B, G, R, A stored as half, no
+//         compression: the layout the reference's tinyexr call writes
+//         (save_exr), float-to-half rounding ties away from zero as it does
 // With `flip` set the image is mirrored in x and in y before it is written,
 // as the reference's save_to_file does (texture.cu:221); the film's row 0 is
-// the bottom of the picture, so png / bmp / hdr rows then run top to bottom.
-// PFM stores its rows bottom to top, so it is written unflipped in y.
+// the bottom of the picture, so png / bmp / hdr / exr rows then run top to
+// bottom.  PFM stores its rows bottom to top, so it is written unflipped in y.
+//
+// Reading (srt_image_read) takes float images: OpenEXR (single-part
+// scanline; half / float / uint channels; no compression, RLE, ZIPS, ZIP),
+// Radiance HDR (flat or run-length scanlines, converted like stbi_loadf)
+// and PFM.  `flip` undoes the writer's flip, as the reference's
+// load_from_file(path, true, true) does for the Measure pass.
 #include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <cstdio>
 #include <fstream>
+#include <functional>
 #include <string>
 #include <vector>
 
 #include "common.h"
+#include "inflate.h"
+
+using namespace srt;
 
 namespace {
 
@@ -130,17 +145,426 @@ void rgbe(float r, float g, float b, uint8_t* out)
     out[3] = (uint8_t)(e + 128);
 }
 
-}  // namespace
+// ---- half floats -----------------------------------------------------------
 
-using namespace srt;
+// float -> IEEE binary16 with ties rounded away from zero (what the
+// reference's EXR writer does; CUDA's __float2half_rn would round ties to
+// even), overflow to infinity, float denormals to signed zero, NaN to the
+// quiet NaN 0x7e00 with its sign.
+uint16_t f32_to_f16(float f)
+{
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint16_t sign = (uint16_t)((x >> 16) & 0x8000u);
+    const uint32_t e = (x >> 23) & 0xffu, m = x & 0x7fffffu;
+    if (e == 0xffu) return sign | 0x7c00u | (m ? 0x200u : 0u);
+    if (e == 0) return sign;
+    const int he = (int)e - 127 + 15;
+    if (he >= 31) return sign | 0x7c00u;
+    if (he <= 0) {
+        // subnormal half: the 24-bit significand shifted into units of 2^-24
+        const int shift = 14 - he;
+        if (shift > 24) return sign;
+        const uint32_t mant = m | 0x800000u;
+        uint32_t h = mant >> shift;
+        if ((mant >> (shift - 1)) & 1u) ++h;
+        return sign | (uint16_t)h;
+    }
+    uint32_t h = ((uint32_t)he << 10) | (m >> 13);
+    if (m & 0x1000u) ++h;  // a carry into the exponent is the correct result (up to infinity)
+    return sign | (uint16_t)h;
+}
+
+float f16_to_f32(uint16_t h)
+{
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    const uint32_t e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+    uint32_t x;
+    if (e == 0) {
+        if (m == 0) {
+            x = sign;
+        } else {  // subnormal: renormalise
+            int k = 0;
+            uint32_t mm = m;
+            while (!(mm & 0x400u)) {
+                mm <<= 1;
+                ++k;
+            }
+            x = sign | ((uint32_t)(127 - 15 - k + 1) << 23) | ((mm & 0x3ffu) << 13);
+        }
+    } else if (e == 31) {
+        x = sign | 0x7f800000u | (m << 13);
+    } else {
+        x = sign | ((e - 15 + 127) << 23) | (m << 13);
+    }
+    float f;
+    std::memcpy(&f, &x, 4);
+    return f;
+}
+
+// ---- OpenEXR ------------------------------------------------------------------
+// File layout from the OpenEXR file-format description: magic 20000630,
+// version 2 with flags, attributes (name, type, size, value) ending in a
+// zero byte, a table of 64-bit chunk offsets, then chunks (y, packed size,
+// data); inside a scanline block the lines follow each other and each line
+// holds every channel's row in channel-list order.
+
+void put_le32(std::vector<uint8_t>& v, uint32_t x)
+{
+    for (int k = 0; k < 4; ++k) v.push_back((uint8_t)(x >> (8 * k)));
+}
+
+void put_attr(std::vector<uint8_t>& v, const char* name, const char* type, const std::vector<uint8_t>& value)
+{
+    v.insert(v.end(), name, name + std::strlen(name) + 1);
+    v.insert(v.end(), type, type + std::strlen(type) + 1);
+    put_le32(v, (uint32_t)value.size());
+    v.insert(v.end(), value.begin(), value.end());
+}
+
+// header + offsets + uncompressed one-line chunks; `row(y)` gives the film
+// row shown as image line y (top first), `col(x)` the film column
+std::vector<uint8_t> encode_exr(int w, int h, const std::function<const float*(int, int)>& px)
+{
+    std::vector<uint8_t> f = {0x76, 0x2f, 0x31, 0x01, 2, 0, 0, 0};
+    std::vector<uint8_t> ch;
+    for (const char* n : {"B", "G", "R", "A"}) {
+        ch.push_back((uint8_t)n[0]);
+        ch.push_back(0);
+        put_le32(ch, 1);  // HALF
+        put_le32(ch, 0);  // pLinear + reserved
+        put_le32(ch, 1);  // x sampling
+        put_le32(ch, 1);  // y sampling
+    }
+    ch.push_back(0);
+    put_attr(f, "channels", "chlist", ch);
+    put_attr(f, "compression", "compression", {0});
+    std::vector<uint8_t> box;
+    for (uint32_t x : {0u, 0u, (uint32_t)(w - 1), (uint32_t)(h - 1)}) put_le32(box, x);
+    put_attr(f, "dataWindow", "box2i", box);
+    put_attr(f, "displayWindow", "box2i", box);
+    put_attr(f, "lineOrder", "lineOrder", {0});
+    const std::vector<uint8_t> one = {0, 0, 0x80, 0x3f};
+    put_attr(f, "pixelAspectRatio", "float", one);
+    put_attr(f, "screenWindowCenter", "v2f", std::vector<uint8_t>(8, 0));
+    put_attr(f, "screenWindowWidth", "float", one);
+    f.push_back(0);
+    const size_t line = (size_t)w * 4 * 2;
+    const size_t table = f.size();
+    for (int y = 0; y < h; ++y) {
+        const uint64_t off = table + 8 * (uint64_t)h + (uint64_t)y * (8 + line);
+        for (int k = 0; k < 8; ++k) f.push_back((uint8_t)(off >> (8 * k)));
+    }
+    f.reserve(f.size() + (size_t)h * (8 + line));
+    const int order[4] = {2, 1, 0, 3};  // B, G, R, A
+    for (int y = 0; y < h; ++y) {
+        put_le32(f, (uint32_t)y);
+        put_le32(f, (uint32_t)line);
+        for (int c : order)
+            for (int x = 0; x < w; ++x) {
+                const uint16_t v = f32_to_f16(px(x, y)[c]);
+                f.push_back((uint8_t)v);
+                f.push_back((uint8_t)(v >> 8));
+            }
+    }
+    return f;
+}
+
+struct Reader {
+    const std::vector<uint8_t>& b;
+    size_t pos = 0;
+    bool bad = false;
+    uint32_t u32()
+    {
+        if (pos + 4 > b.size()) {
+            bad = true;
+            return 0;
+        }
+        uint32_t x = b[pos] | (uint32_t)b[pos + 1] << 8 | (uint32_t)b[pos + 2] << 16 | (uint32_t)b[pos + 3] << 24;
+        pos += 4;
+        return x;
+    }
+    uint64_t u64()
+    {
+        uint64_t lo = u32(), hi = u32();
+        return lo | hi << 32;
+    }
+    std::string cstr()
+    {
+        size_t e = pos;
+        while (e < b.size() && b[e]) ++e;
+        if (e >= b.size()) {
+            bad = true;
+            return std::string();
+        }
+        std::string s(b.begin() + pos, b.begin() + e);
+        pos = e + 1;
+        return s;
+    }
+};
+
+// undo the EXR byte predictor and the two-half interleave (ZIP and RLE)
+void exr_unpredict(std::vector<uint8_t>& t, std::vector<uint8_t>& out)
+{
+    for (size_t i = 1; i < t.size(); ++i) t[i] = (uint8_t)(t[i - 1] + t[i] - 128);
+    out.resize(t.size());
+    const size_t half = (t.size() + 1) / 2;
+    for (size_t i = 0; i < t.size(); ++i) out[i] = (i & 1) ? t[half + i / 2] : t[i / 2];
+}
+
+bool exr_rle(const uint8_t* in, size_t n, std::vector<uint8_t>& out, size_t limit)
+{
+    size_t i = 0;
+    while (i < n) {
+        const int c = (int8_t)in[i++];
+        if (c < 0) {
+            const size_t k = (size_t)(-c);
+            if (i + k > n || out.size() + k > limit) return false;
+            out.insert(out.end(), in + i, in + i + k);
+            i += k;
+        } else {
+            if (i >= n || out.size() + c + 1 > limit) return false;
+            out.insert(out.end(), (size_t)c + 1, in[i++]);
+        }
+    }
+    return true;
+}
+
+srt_status read_exr(const std::vector<uint8_t>& b, const std::string& path, int& w, int& h, std::vector<float>& rgba)
+{
+    auto bad = [&](const std::string& why) { return set_error(SRT_ERR_PARSE, path + ": " + why); };
+    Reader r{b};
+    if (r.u32() != 20000630u) return bad("not an OpenEXR file");
+    const uint32_t ver = r.u32();
+    if ((ver & 0xff) != 2) return bad("unknown OpenEXR version");
+    if (ver & 0x200u) return set_error(SRT_ERR_UNSUPPORTED, path + ": tiled OpenEXR files are not read");
+    if (ver & 0x1800u) return set_error(SRT_ERR_UNSUPPORTED, path + ": deep or multi-part OpenEXR files are not read");
+    struct Chan {
+        std::string name;
+        int type;
+        int xs, ys;
+    };
+    std::vector<Chan> chans;
+    int comp = -1;
+    int32_t dw[4] = {0, 0, -1, -1};
+    bool have_dw = false;
+    for (;;) {
+        std::string name = r.cstr();
+        if (r.bad) return bad("truncated header");
+        if (name.empty()) break;
+        std::string type = r.cstr();
+        const uint32_t size = r.u32();
+        if (r.bad || r.pos + size > b.size()) return bad("truncated header");
+        const size_t end = r.pos + size;
+        if (name == "channels" && type == "chlist") {
+            while (r.pos < end && b[r.pos]) {
+                Chan c;
+                c.name = r.cstr();
+                c.type = (int)r.u32();
+                r.u32();
+                c.xs = (int)r.u32();
+                c.ys = (int)r.u32();
+                chans.push_back(c);
+            }
+        } else if (name == "compression") {
+            comp = size >= 1 ? b[r.pos] : -1;
+        } else if (name == "dataWindow" && size == 16) {
+            for (int k = 0; k < 4; ++k) dw[k] = (int32_t)r.u32();
+            have_dw = true;
+        }
+        r.pos = end;
+    }
+    if (!have_dw || chans.empty()) return bad("no dataWindow or channels");
+    const int64_t W = (int64_t)dw[2] - dw[0] + 1, H = (int64_t)dw[3] - dw[1] + 1;
+    if (W <= 0 || H <= 0 || W > (1 << 16) || H > (1 << 16)) return bad("bad dataWindow");
+    int lines;
+    if (comp == 0 || comp == 1 || comp == 2)
+        lines = 1;
+    else if (comp == 3)
+        lines = 16;
+    else
+        return set_error(SRT_ERR_UNSUPPORTED, path + ": OpenEXR compression " + std::to_string(comp) +
+                                                  " (none, RLE, ZIPS and ZIP are read)");
+    size_t line_bytes = 0;
+    for (const Chan& c : chans) {
+        if (c.type < 0 || c.type > 2) return bad("unknown channel type");
+        if (c.xs != 1 || c.ys != 1) return set_error(SRT_ERR_UNSUPPORTED, path + ": subsampled channels");
+        line_bytes += (size_t)W * (c.type == 1 ? 2 : 4);
+    }
+    // which channel fills R, G, B, A (a lone channel is grey)
+    int src[4] = {-1, -1, -1, -1};
+    for (size_t i = 0; i < chans.size(); ++i) {
+        const std::string& n = chans[i].name;
+        if (n == "R") src[0] = (int)i;
+        if (n == "G") src[1] = (int)i;
+        if (n == "B") src[2] = (int)i;
+        if (n == "A") src[3] = (int)i;
+    }
+    if (chans.size() == 1) src[0] = src[1] = src[2] = 0;
+    if (src[0] < 0 || src[1] < 0 || src[2] < 0) return set_error(SRT_ERR_UNSUPPORTED, path + ": no R, G, B channels");
+    const int64_t nchunks = (H + lines - 1) / lines;
+    std::vector<uint64_t> offs((size_t)nchunks);
+    for (auto& o : offs) o = r.u64();
+    if (r.bad) return bad("truncated offset table");
+    w = (int)W;
+    h = (int)H;
+    rgba.assign((size_t)W * H * 4, 0.0f);
+    for (size_t i = 0; i < (size_t)W * H; ++i) rgba[4 * i + 3] = 1.0f;
+    std::vector<uint8_t> raw, tmp;
+    for (int64_t k = 0; k < nchunks; ++k) {
+        r.pos = (size_t)offs[(size_t)k];
+        const int32_t y0 = (int32_t)r.u32();
+        const uint32_t packed = r.u32();
+        if (r.bad || r.pos + packed > b.size()) return bad("truncated chunk");
+        if (y0 < dw[1] || y0 > dw[3]) return bad("chunk outside the dataWindow");
+        const int nl = (int)std::min<int64_t>(lines, (int64_t)dw[3] - y0 + 1);
+        const size_t want = line_bytes * nl;
+        const uint8_t* d = b.data() + r.pos;
+        raw.clear();
+        if (comp == 0 || packed == want) {  // stored as is (also a block that did not compress)
+            if (packed != want) return bad("chunk size");
+            raw.assign(d, d + packed);
+        } else {
+            tmp.clear();
+            const bool ok = comp == 1 ? exr_rle(d, packed, tmp, want) : inflate_zlib(d, packed, tmp, want);
+            if (!ok || tmp.size() != want) return bad("corrupt compressed chunk");
+            exr_unpredict(tmp, raw);
+        }
+        size_t at = 0;
+        for (int l = 0; l < nl; ++l) {
+            const int64_t row = (int64_t)y0 - dw[1] + l;
+            for (size_t c = 0; c < chans.size(); ++c) {
+                const int t = chans[c].type, sz = t == 1 ? 2 : 4;
+                for (int64_t x = 0; x < W; ++x) {
+                    const uint8_t* q = &raw[at + (size_t)x * sz];
+                    float v;
+                    if (t == 1) {
+                        v = f16_to_f32((uint16_t)(q[0] | q[1] << 8));
+                    } else {
+                        uint32_t u = q[0] | (uint32_t)q[1] << 8 | (uint32_t)q[2] << 16 | (uint32_t)q[3] << 24;
+                        if (t == 2)
+                            std::memcpy(&v, &u, 4);
+                        else
+                            v = (float)u;
+                    }
+                    for (int o = 0; o < 4; ++o)
+                        if (src[o] == (int)c) rgba[4 * ((size_t)row * W + x) + o] = v;
+                }
+                at += (size_t)W * sz;
+            }
+        }
+    }
+    return SRT_OK;
+}
+
+// ---- Radiance HDR (read) ------------------------------------------------------
+
+srt_status read_hdr(const std::vector<uint8_t>& b, const std::string& path, int& w, int& h, std::vector<float>& rgba)
+{
+    auto bad = [&](const std::string& why) { return set_error(SRT_ERR_PARSE, path + ": " + why); };
+    size_t pos = 0;
+    auto line = [&]() {
+        std::string s;
+        while (pos < b.size() && b[pos] != '\n') s.push_back((char)b[pos++]);
+        ++pos;
+        return s;
+    };
+    std::string first = line();
+    if (first != "#?RADIANCE" && first != "#?RGBE") return bad("not a Radiance HDR file");
+    for (;;) {
+        if (pos >= b.size()) return bad("truncated header");
+        std::string l = line();
+        if (l.empty()) break;
+        if (l.compare(0, 7, "FORMAT=") == 0 && l != "FORMAT=32-bit_rle_rgbe") return bad("unsupported " + l);
+    }
+    std::string res = line();
+    int hh = 0, ww = 0;
+    char ys[3] = {}, xs[3] = {};
+    if (std::sscanf(res.c_str(), "%2s %d %2s %d", ys, &hh, xs, &ww) != 4 || std::string(ys) != "-Y" ||
+        std::string(xs) != "+X")
+        return set_error(SRT_ERR_UNSUPPORTED, path + ": HDR orientation other than -Y +X");
+    if (ww <= 0 || hh <= 0 || ww > (1 << 16) || hh > (1 << 16)) return bad("bad size");
+    w = ww;
+    h = hh;
+    rgba.assign((size_t)w * h * 4, 1.0f);
+    std::vector<uint8_t> sl((size_t)w * 4);
+    for (int y = 0; y < h; ++y) {
+        const bool rle = w >= 8 && w < 32768 && pos + 4 <= b.size() && b[pos] == 2 && b[pos + 1] == 2 &&
+                         (b[pos + 2] << 8 | b[pos + 3]) == w;
+        if (rle) {
+            pos += 4;
+            for (int c = 0; c < 4; ++c) {
+                int x = 0;
+                while (x < w) {
+                    if (pos >= b.size()) return bad("truncated scanline");
+                    int n = b[pos++];
+                    if (n > 128) {
+                        n -= 128;
+                        if (pos >= b.size() || x + n > w) return bad("bad run");
+                        for (int k = 0; k < n; ++k) sl[4 * (x + k) + c] = b[pos];
+                        ++pos;
+                    } else {
+                        if (n == 0 || x + n > w || pos + n > b.size()) return bad("bad run");
+                        for (int k = 0; k < n; ++k) sl[4 * (x + k) + c] = b[pos + k];
+                        pos += n;
+                    }
+                    x += n;
+                }
+            }
+        } else {
+            if (pos + sl.size() > b.size()) return bad("truncated scanline");
+            std::memcpy(sl.data(), &b[pos], sl.size());
+            pos += sl.size();
+        }
+        for (int x = 0; x < w; ++x) {
+            const uint8_t* e = &sl[4 * (size_t)x];
+            float* o = &rgba[4 * ((size_t)y * w + x)];
+            // RGBE to float as stbi_loadf does: mantissa * 2^(exponent - 136), no half-unit offset
+            const float f = e[3] ? std::ldexp(1.0f, (int)e[3] - 136) : 0.0f;
+            for (int c = 0; c < 3; ++c) o[c] = e[c] * f;
+        }
+    }
+    return SRT_OK;
+}
+
+// ---- PFM (read) ---------------------------------------------------------------
+
+srt_status read_pfm(const std::vector<uint8_t>& b, const std::string& path, int& w, int& h, std::vector<float>& rgba)
+{
+    auto bad = [&](const std::string& why) { return set_error(SRT_ERR_PARSE, path + ": " + why); };
+    std::string head(b.begin(), b.begin() + std::min<size_t>(b.size(), 256));
+    char magic[3] = {};
+    int ww = 0, hh = 0, used = 0;
+    double scale = 0.0;
+    if (std::sscanf(head.c_str(), "%2s %d %d %lf%n", magic, &ww, &hh, &scale, &used) != 4) return bad("bad PFM header");
+    const int ch = std::string(magic) == "PF" ? 3 : std::string(magic) == "Pf" ? 1 : 0;
+    if (!ch || ww <= 0 || hh <= 0 || ww > (1 << 16) || hh > (1 << 16)) return bad("bad PFM header");
+    const size_t start = (size_t)used + 1;  // one whitespace byte after the scale
+    const size_t n = (size_t)ww * hh * ch;
+    if (start + 4 * n > b.size()) return bad("truncated PFM data");
+    w = ww;
+    h = hh;
+    rgba.assign((size_t)w * h * 4, 1.0f);
+    const bool big = scale > 0.0;
+    for (size_t i = 0; i < (size_t)w * h; ++i)
+        for (int c = 0; c < 3; ++c) {
+            const uint8_t* q = &b[start + 4 * (i * ch + (ch == 3 ? c : 0))];
+            uint32_t u = big ? ((uint32_t)q[0] << 24 | (uint32_t)q[1] << 16 | (uint32_t)q[2] << 8 | q[3])
+                             : (q[0] | (uint32_t)q[1] << 8 | (uint32_t)q[2] << 16 | (uint32_t)q[3] << 24);
+            std::memcpy(&rgba[4 * i + c], &u, 4);
+        }
+    return SRT_OK;
+}
+
+}  // namespace
 
 extern "C" srt_status srt_image_write(const char* path, int32_t w, int32_t h, const float* rgba, int32_t flip)
 {
     clear_error();
     if (!path || !rgba || w <= 0 || h <= 0) return set_error(SRT_ERR_ARG, "bad image arguments");
     const std::string ext = extension(path);
-    if (ext != "png" && ext != "bmp" && ext != "hdr" && ext != "pfm")
-        return set_error(SRT_ERR_UNSUPPORTED, "unsupported image format: " + ext + " (png, bmp, hdr, pfm)");
+    if (ext != "png" && ext != "bmp" && ext != "hdr" && ext != "pfm" && ext != "exr")
+        return set_error(SRT_ERR_UNSUPPORTED, "unsupported image format: " + ext + " (png, bmp, hdr, pfm, exr)");
     // film pixel of the image's pixel (x, y), y counted from the first stored
     // row; mirror_y: the format stores rows top to bottom
     auto src = [&](int x, int y, bool mirror_y) -> const float* {
@@ -150,7 +574,10 @@ extern "C" srt_status srt_image_write(const char* path, int32_t w, int32_t h, co
     };
     std::ofstream f(path, std::ios::binary);
     if (!f) return set_error(SRT_ERR_ARG, std::string("cannot open ") + path);
-    if (ext == "png" || ext == "bmp") {
+    if (ext == "exr") {
+        std::vector<uint8_t> exr = encode_exr(w, h, [&](int x, int y) { return src(x, y, true); });
+        f.write(reinterpret_cast<const char*>(exr.data()), (std::streamsize)exr.size());
+    } else if (ext == "png" || ext == "bmp") {
         std::vector<uint8_t> px((size_t)w * h * 4);
         for (int y = 0; y < h; ++y)
             for (int x = 0; x < w; ++x) {
@@ -210,4 +637,37 @@ extern "C" srt_status srt_image_write(const char* path, int32_t w, int32_t h, co
         }
     }
     return f ? SRT_OK : set_error(SRT_ERR_ARG, std::string("write failed: ") + path);
+}
+
+extern "C" srt_status srt_image_read(const char* path, int32_t* width, int32_t* height, float* rgba, int32_t flip)
+{
+    clear_error();
+    if (!path || !width || !height) return set_error(SRT_ERR_ARG, "NULL argument");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return set_error(SRT_ERR_ARG, std::string("Failed to open file: ") + path);
+    std::vector<uint8_t> b((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    int w = 0, h = 0;
+    std::vector<float> px;
+    bool bottom_up = false;  // PFM rows run bottom to top, like the film's
+    if (b.size() >= 4 && b[0] == 0x76 && b[1] == 0x2f && b[2] == 0x31 && b[3] == 0x01) {
+        SRT_TRY(read_exr(b, path, w, h, px));
+    } else if (b.size() >= 2 && b[0] == '#' && b[1] == '?') {
+        SRT_TRY(read_hdr(b, path, w, h, px));
+    } else if (b.size() >= 2 && b[0] == 'P' && (b[1] == 'F' || b[1] == 'f')) {
+        SRT_TRY(read_pfm(b, path, w, h, px));
+        bottom_up = true;
+    } else {
+        return set_error(SRT_ERR_UNSUPPORTED, std::string(path) + ": not a float image (exr, hdr, pfm)");
+    }
+    *width = w;
+    *height = h;
+    if (!rgba) return SRT_OK;
+    // Image::flip(true, true) for the top-to-bottom formats; x alone for PFM
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const int sx = flip ? w - 1 - x : x;
+            const int sy = (flip && !bottom_up) ? h - 1 - y : y;
+            std::memcpy(rgba + 4 * ((size_t)y * w + x), &px[4 * ((size_t)sy * w + sx)], 16);
+        }
+    return SRT_OK;
 }

@@ -192,25 +192,7 @@ private:
 };
 RenderPassFactory::Register<ToneMapping> ToneMapping::reg("ToneMapping");
 
-// ---- Measure (src/passes/postprocess/measure.{h,cu}); reference image as PFM
-
-static bool read_pfm(const std::string& path, int& w, int& h, std::vector<float>& rgba)
-{
-    std::ifstream f(path, std::ios::binary);
-    if (!f) return false;
-    std::string magic;
-    double scale;
-    f >> magic >> w >> h >> scale;
-    f.get();
-    if (magic != "PF" || w <= 0 || h <= 0) return false;
-    std::vector<float> rgb((size_t)w * h * 3);
-    f.read(reinterpret_cast<char*>(rgb.data()), (std::streamsize)(rgb.size() * 4));
-    if (!f) return false;
-    rgba.assign((size_t)w * h * 4, 1.0f);
-    for (size_t i = 0; i < (size_t)w * h; ++i)
-        for (int c = 0; c < 3; ++c) rgba[4 * i + c] = rgb[3 * i + c];
-    return true;
-}
+// ---- Measure (src/passes/postprocess/measure.{h,cu}); reference image: exr, hdr or pfm
 
 class Measure : public RenderPass {
 public:
@@ -221,6 +203,8 @@ public:
         type = t == "MAPE" ? SRT_METRIC_MAPE : t == "SMAPE" ? SRT_METRIC_SMAPE : t == "RelMSE" ? SRT_METRIC_RELMSE
                                                                                                    : SRT_METRIC_MSE;
         discard = (float)j.number("discard", 0.1);
+        const std::string o = j.string("option", "None");  // Measure::string_to_option
+        option = o == "Reference" ? SRT_MEASURE_REFERENCE : o == "Error" ? SRT_MEASURE_ERROR : SRT_MEASURE_NONE;
     }
     ~Measure() override
     {
@@ -230,10 +214,14 @@ public:
     srt_status init() override
     {
         if (ref_path.empty()) return set_error(SRT_ERR_ARG, "Measure: no ref_path specified");
-        int w = 0, h = 0;
-        std::vector<float> rgba;
-        if (!read_pfm(ref_path, w, h, rgba) || w != width || h != height)
-            return set_error(SRT_ERR_ARG, "Measure: reference image size or format not match");
+        // Image::load_from_file(ref_path, true, true) of a float image (measure.cu:5-16)
+        int32_t w = 0, h = 0;
+        srt_status st = srt_image_read(ref_path.c_str(), &w, &h, nullptr, 1);
+        if (st != SRT_OK || w != width || h != height)
+            return set_error(st == SRT_OK || st == SRT_ERR_UNSUPPORTED ? SRT_ERR_ARG : st,
+                             "Measure: reference image size or format not match (" + ref_path + ")");
+        std::vector<float> rgba((size_t)w * h * 4);
+        SRT_TRY(srt_image_read(ref_path.c_str(), &w, &h, rgba.data(), 1));
         size_t n = (size_t)w * h;
         SRT_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&ref), n * 16));
         SRT_CUDA_TRY(cudaMemcpy(ref, rgba.data(), n * 16, cudaMemcpyHostToDevice));
@@ -245,7 +233,11 @@ public:
         if (!enable) return SRT_OK;
         SRT_TRY(srt_film_metric(film->get_pixels(), ref, (int64_t)width * height, type, discard, scratch, &error,
                                 nullptr));
-        if (!online) std::printf("%s error: %g\n\n", type_name(), (double)error);
+        SRT_TRY(srt_film_measure_view(film->get_pixels(), ref, (int64_t)width * height, type, option, nullptr));
+        if (!online) {
+            std::printf("%s error: %g\n\n", type_name(), (double)error);
+            std::fflush(stdout);  // the reference ends the line with endl
+        }
         return SRT_OK;
     }
     const char* type_name() const
@@ -256,6 +248,7 @@ public:
 private:
     std::string ref_path;
     int type = SRT_METRIC_MSE;
+    int option = SRT_MEASURE_NONE;
     float discard = 0.1f, error = 0.0f;
     float* ref = nullptr;
     void* scratch = nullptr;

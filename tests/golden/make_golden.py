@@ -5,7 +5,9 @@ oracle/_ref/libsrtref.so from the reference's own device headers):
 
     python tests/golden/make_golden.py
 
-Outputs (committed): tests/golden/bxdf.npz, camera.npz, scene.npz (the
+Outputs (committed): tests/golden/bxdf.npz, camera.npz, pbrt_camera.npz,
+image.npz with img_*.exr / img_stb.hdr (files written by the reference's
+vendored tinyexr / stb_image_write), scene.npz (the
 Cornell scene arrays plus light samples, hit attributes and a small
 render, all produced by the reference's classes compiled for the host).
 The Cornell scene arrays come from the library's procedural generator.
@@ -143,6 +145,70 @@ def pbrt_camera_set():
     np.savez_compressed(os.path.join(OUT, "pbrt_camera.npz"), **out)
 
 
+def _img_lib():
+    return C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libsrtimg.so"))
+
+
+def golden_image_pixels():
+    """37 x 29 RGBA: smooth ramps (compressible), values above 1 and below 0,
+    and a block of random values."""
+    h, w = 29, 37
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
+    px = np.stack([xx / w * 3.0 - 0.5, yy / h, np.round(xx / 8) / 4, np.ones_like(xx)], -1)
+    rng = np.random.default_rng(21)
+    px[20:26, 3:15] = rng.random((6, 12, 4), dtype=np.float32) * 100.0 - 20.0
+    return px.reshape(-1, 4).astype(np.float32), w, h
+
+
+def half_probe_values():
+    """Float32 inputs whose half encodings pin the writer's rounding:
+    random bit patterns, the midpoints between neighbouring halves (ties),
+    overflow, subnormal and special values."""
+    rng = np.random.default_rng(22)
+    rand = rng.integers(0, 2**32, size=4096, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    hv = np.arange(0, 0x7c00, dtype=np.uint16).view(np.float16).astype(np.float64)
+    mids = ((hv[:-1] + hv[1:]) / 2)[::15].astype(np.float32)
+    special = np.array([0.0, -0.0, 1.0, 65504.0, 65519.0, 65520.0, 1e5, 2.0**-24, 2.0**-25, 1.5 * 2.0**-25,
+                        2.0**-26, 1e-40, np.inf, -np.inf, np.nan, -np.nan], np.float32)
+    return np.concatenate([special, mids, -mids, rand]).astype(np.float32)
+
+
+def image_set():
+    """Files written by the reference's image code (tinyexr as save_exr calls
+    it, stb_image_write as save_hdr does) and what its load_from_file reads
+    back from them."""
+    L = _img_lib()
+    px, w, h = golden_image_pixels()
+    out = {"src": px, "size": np.array([w, h], np.int32)}
+    for name, comp in (("none", 0), ("rle", 1), ("zips", 2), ("zip", 3), ("piz", 4)):
+        path = os.path.join(OUT, f"img_{name}.exr")
+        assert L.ref_save_exr(path.encode(), w, h, _np(px), comp) == 0
+        if name != "piz":
+            out[f"{name}_decoded"] = _ref_load(L, path)
+    path = os.path.join(OUT, "img_stb.hdr")
+    assert L.ref_save_stb(path.encode(), 0, w, h, _np(np.abs(px))) == 0
+    out["stb_hdr_decoded"] = _ref_load(L, path)
+    # half encodings: one-row image, channel B holds the probes
+    v = half_probe_values()
+    probe = np.zeros((len(v), 4), np.float32)
+    probe[:, 2] = v
+    tmp = os.path.join(OUT, "_probe.exr")
+    assert L.ref_save_exr(tmp.encode(), len(v), 1, _np(probe), 0) == 0
+    data = open(tmp, "rb").read()
+    os.remove(tmp)
+    out["half_in"] = v
+    out["half_out"] = np.frombuffer(data[-2 * 4 * len(v):], np.uint16)[:len(v)].copy()  # B is the first channel
+    np.savez_compressed(os.path.join(OUT, "image.npz"), **out)
+
+
+def _ref_load(L, path):
+    w, h = C.c_int(), C.c_int()
+    assert L.ref_load_float_image(path.encode(), C.byref(w), C.byref(h), None) == 0
+    a = np.zeros((w.value * h.value, 4), np.float32)
+    assert L.ref_load_float_image(path.encode(), C.byref(w), C.byref(h), _np(a)) == 0
+    return a
+
+
 def scene_arrays_to_npz(s):
     out = {}
     out["num_meshes"] = np.int32(len(s.meshes))
@@ -202,5 +268,6 @@ if __name__ == "__main__":
     bxdf_sets()
     camera_set()
     pbrt_camera_set()
+    image_set()
     scene_set()
     print("golden vectors written to", OUT)
