@@ -524,8 +524,17 @@ srt_status srt_image_write(const char* path, int32_t width, int32_t height, cons
  * srt_image_write's flip (for EXR / HDR: the reference's
  * load_from_file(path, true, true), which the Measure pass uses), so a
  * film written with flip and read with flip comes back in film order.
- * 8-bit formats return SRT_ERR_UNSUPPORTED; malformed files SRT_ERR_PARSE. */
+ * 8-bit formats return SRT_ERR_UNSUPPORTED; malformed files SRT_ERR_PARSE.
+ * flip is one of SRT_FLIP_*: XY = load_from_file(path, true, true), Y =
+ * load_from_file(path, false, true) (pbrt image textures). */
+enum { SRT_FLIP_NONE = 0, SRT_FLIP_XY = 1, SRT_FLIP_Y = 2 };
 srt_status srt_image_read(const char* path, int32_t* width, int32_t* height, float* rgba, int32_t flip);
+/* load_from_file's 8-bit branch (stbi_load(path, .., 4)): PNG (all colour
+ * types and bit depths, palette and tRNS transparency, Adam7; 16-bit
+ * samples cut to their high byte) and uncompressed 24 / 32-bit BMP into
+ * RGBA8 (rgba: 4*w*h bytes, NULL for the size).  JPEG and other formats
+ * return SRT_ERR_UNSUPPORTED.  flip as srt_image_read. */
+srt_status srt_image_read_rgba8(const char* path, int32_t* width, int32_t* height, uint8_t* rgba, int32_t flip);
 void srt_renderer_destroy(srt_renderer* r);
 /* Names of the registered passes, ';'-separated (print_registered_pass). */
 const char* srt_registered_passes(void);

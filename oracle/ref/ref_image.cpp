@@ -105,4 +105,14 @@ int ref_load_float_image(const char* path, int* w, int* h, float* out)
     return 0;
 }
 
+// Image::load_from_file's 8-bit branch without the flip: stbi_load(.., 4).
+int ref_load_u8_image(const char* path, int* w, int* h, unsigned char* out)
+{
+    unsigned char* data = stbi_load(path, w, h, nullptr, STBI_rgb_alpha);
+    if (!data) return -1;
+    if (out) std::memcpy(out, data, (size_t)(*w) * (*h) * 4);
+    stbi_image_free(data);
+    return 0;
+}
+
 }  // extern "C"

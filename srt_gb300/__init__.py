@@ -21,7 +21,7 @@ from ._capi import (BXDF_DIELECTRIC, BXDF_DIFFUSE, BXDF_DIFFUSE_TRANSMISSION, BX
 __all__ = [
     "SceneArrays", "Scene", "PathTracer", "procedural", "import_scene", "lib", "check", "SrtError", "bxdf_sample", "bxdf_eval",
     "bxdf_generate", "film_accumulate", "film_tonemap", "film_metric", "film_measure_view", "rng_tape", "Renderer", "image_write",
-    "image_read",
+    "image_read", "image_read_rgba8",
 ]
 
 DISNEY_PARAM_NAMES = ("ior", "metallic", "subsurface", "roughness", "specular", "specularTint", "anisotropic",
@@ -117,13 +117,28 @@ def image_write(path, rgba, width, height, flip=True):
     check(lib().srt_image_write(os.fsencode(str(path)), width, height, _ptr(px), 1 if flip else 0))
 
 
+def _flip_code(flip):
+    return {False: 0, True: 1, "xy": 1, "y": 2, None: 0}[flip]
+
+
 def image_read(path, flip=True):
-    """srt_image_read: (float4[w*h] array, width, height) of an exr / hdr / pfm."""
+    """srt_image_read: (float4[w*h] array, width, height) of an exr / hdr / pfm.
+    flip: True / "xy" (load_from_file(p, true, true)), "y", or False."""
     L = lib()
     w, h = C.c_int32(), C.c_int32()
-    check(L.srt_image_read(os.fsencode(str(path)), C.byref(w), C.byref(h), None, 1 if flip else 0))
+    check(L.srt_image_read(os.fsencode(str(path)), C.byref(w), C.byref(h), None, _flip_code(flip)))
     out = np.empty((w.value * h.value, 4), np.float32)
-    check(L.srt_image_read(os.fsencode(str(path)), C.byref(w), C.byref(h), _ptr(out), 1 if flip else 0))
+    check(L.srt_image_read(os.fsencode(str(path)), C.byref(w), C.byref(h), _ptr(out), _flip_code(flip)))
+    return out, w.value, h.value
+
+
+def image_read_rgba8(path, flip=False):
+    """srt_image_read_rgba8: (uint8 RGBA [w*h, 4], width, height) of a png / bmp."""
+    L = lib()
+    w, h = C.c_int32(), C.c_int32()
+    check(L.srt_image_read_rgba8(os.fsencode(str(path)), C.byref(w), C.byref(h), None, _flip_code(flip)))
+    out = np.empty((w.value * h.value, 4), np.uint8)
+    check(L.srt_image_read_rgba8(os.fsencode(str(path)), C.byref(w), C.byref(h), _ptr(out), _flip_code(flip)))
     return out, w.value, h.value
 
 

@@ -184,6 +184,7 @@ _PROTOS = [
     ("srt_renderer_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("srt_image_write", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]),
     ("srt_image_read", C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_int32]),
+    ("srt_image_read_rgba8", C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_int32]),
     ("srt_renderer_destroy", None, [C.c_void_p]),
     ("srt_registered_passes", C.c_char_p, []),
 ]

@@ -556,6 +556,192 @@ srt_status read_pfm(const std::vector<uint8_t>& b, const std::string& path, int&
     return SRT_OK;
 }
 
+// ---- PNG (read, 8 bits per channel out) -----------------------------------------
+// From the PNG specification: chunks, zlib-compressed scanlines with one
+// filter byte each (None, Sub, Up, Average, Paeth), Adam7 interlacing, and
+// the conversions to 8-bit RGBA that stbi_load(..., 4) makes: low bit depths
+// scaled to 0..255, 16-bit samples cut to their high byte, palette and tRNS
+// transparency applied.
+
+uint32_t be32(const uint8_t* p) { return (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | p[3]; }
+
+int paeth(int a, int b, int c)
+{
+    const int p = a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+    return (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+}
+
+srt_status read_png(const std::vector<uint8_t>& b, const std::string& path, int& w, int& h, std::vector<uint8_t>& rgba)
+{
+    auto bad = [&](const std::string& why) { return set_error(SRT_ERR_PARSE, path + ": " + why); };
+    static const uint8_t sig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
+    if (b.size() < 8 || std::memcmp(b.data(), sig, 8) != 0) return bad("not a PNG file");
+    size_t pos = 8;
+    int depth = 0, ctype = -1, interlace = 0;
+    std::vector<uint8_t> idat, plte, trns;
+    bool ihdr = false;
+    while (pos + 12 <= b.size()) {
+        const uint32_t len = be32(&b[pos]);
+        const std::string type(b.begin() + pos + 4, b.begin() + pos + 8);
+        if (pos + 12 + (size_t)len > b.size()) return bad("truncated chunk");
+        const uint8_t* d = &b[pos + 8];
+        if (type == "IHDR") {
+            if (len < 13) return bad("short IHDR");
+            w = (int)be32(d);
+            h = (int)be32(d + 4);
+            depth = d[8];
+            ctype = d[9];
+            interlace = d[12];
+            ihdr = true;
+            if (d[10] != 0 || d[11] != 0 || interlace > 1) return bad("unknown compression, filter or interlace");
+        } else if (type == "PLTE") {
+            plte.assign(d, d + len);
+        } else if (type == "tRNS") {
+            trns.assign(d, d + len);
+        } else if (type == "IDAT") {
+            idat.insert(idat.end(), d, d + len);
+        } else if (type == "IEND") {
+            break;
+        }
+        pos += 12 + (size_t)len;
+    }
+    if (!ihdr || w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16)) return bad("bad IHDR");
+    int ch;
+    switch (ctype) {
+    case 0: ch = 1; break;
+    case 2: ch = 3; break;
+    case 3: ch = 1; break;
+    case 4: ch = 2; break;
+    case 6: ch = 4; break;
+    default: return bad("unknown colour type");
+    }
+    const bool depth_ok = (ctype == 0 && (depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)) ||
+                          (ctype == 3 && (depth == 1 || depth == 2 || depth == 4 || depth == 8)) ||
+                          ((ctype == 2 || ctype == 4 || ctype == 6) && (depth == 8 || depth == 16));
+    if (!depth_ok) return bad("bad bit depth");
+    if (ctype == 3 && (plte.empty() || plte.size() % 3)) return bad("missing palette");
+    const int bits_px = ch * depth, bpp = std::max(1, bits_px / 8);
+    // raw size over the (one or seven) passes
+    static const int ax0[7] = {0, 4, 0, 2, 0, 1, 0}, ay0[7] = {0, 0, 4, 0, 2, 0, 1};
+    static const int adx[7] = {8, 8, 4, 4, 2, 2, 1}, ady[7] = {8, 8, 8, 4, 4, 2, 2};
+    const int passes = interlace ? 7 : 1;
+    size_t need = 0;
+    int pw[7], ph[7];
+    for (int p = 0; p < passes; ++p) {
+        pw[p] = interlace ? (w - ax0[p] + adx[p] - 1) / adx[p] : w;
+        ph[p] = interlace ? (h - ay0[p] + ady[p] - 1) / ady[p] : h;
+        if (pw[p] > 0 && ph[p] > 0) need += (size_t)ph[p] * (1 + ((size_t)pw[p] * bits_px + 7) / 8);
+    }
+    std::vector<uint8_t> raw;
+    if (!inflate_zlib(idat.data(), idat.size(), raw, need) || raw.size() != need) return bad("corrupt image data");
+    // samples of the whole image, as 16-bit values before the 8-bit cut
+    std::vector<uint16_t> smp((size_t)w * h * ch);
+    size_t at = 0;
+    for (int p = 0; p < passes; ++p) {
+        if (pw[p] <= 0 || ph[p] <= 0) continue;
+        const size_t stride = ((size_t)pw[p] * bits_px + 7) / 8;
+        std::vector<uint8_t> prev(stride, 0), cur(stride);
+        for (int y = 0; y < ph[p]; ++y) {
+            const int ft = raw[at++];
+            for (size_t i = 0; i < stride; ++i) {
+                const int x = raw[at + i];
+                const int a = i >= (size_t)bpp ? cur[i - bpp] : 0, up = prev[i], c = i >= (size_t)bpp ? prev[i - bpp] : 0;
+                int v;
+                switch (ft) {
+                case 0: v = x; break;
+                case 1: v = x + a; break;
+                case 2: v = x + up; break;
+                case 3: v = x + ((a + up) >> 1); break;
+                case 4: v = x + paeth(a, up, c); break;
+                default: return bad("unknown filter type");
+                }
+                cur[i] = (uint8_t)v;
+            }
+            at += stride;
+            const int iy = interlace ? ay0[p] + y * ady[p] : y;
+            for (int x = 0; x < pw[p]; ++x) {
+                const int ix = interlace ? ax0[p] + x * adx[p] : x;
+                for (int c = 0; c < ch; ++c) {
+                    uint16_t v;
+                    if (depth == 16) {
+                        const size_t o = ((size_t)x * ch + c) * 2;
+                        v = (uint16_t)(cur[o] << 8 | cur[o + 1]);
+                    } else if (depth == 8) {
+                        v = cur[(size_t)x * ch + c];
+                    } else {
+                        const size_t bit = (size_t)x * depth;  // one channel
+                        v = (uint16_t)((cur[bit / 8] >> (8 - depth - bit % 8)) & ((1 << depth) - 1));
+                    }
+                    smp[((size_t)iy * w + ix) * ch + c] = v;
+                }
+            }
+            std::swap(prev, cur);
+        }
+    }
+    rgba.assign((size_t)w * h * 4, 255);
+    const int scale = depth == 1 ? 255 : depth == 2 ? 85 : depth == 4 ? 17 : 1;
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        const uint16_t* s = &smp[i * ch];
+        uint8_t* o = &rgba[4 * i];
+        auto to8 = [&](uint16_t v) { return (uint8_t)(depth == 16 ? v >> 8 : v * scale); };
+        if (ctype == 3) {
+            const size_t k = s[0];
+            if (3 * k + 2 >= plte.size()) return bad("palette index out of range");
+            o[0] = plte[3 * k];
+            o[1] = plte[3 * k + 1];
+            o[2] = plte[3 * k + 2];
+            o[3] = k < trns.size() ? trns[k] : 255;
+            continue;
+        }
+        if (ch <= 2) {
+            o[0] = o[1] = o[2] = to8(s[0]);
+            if (ch == 2) o[3] = to8(s[1]);
+        } else {
+            for (int c = 0; c < ch; ++c) o[c] = to8(s[c]);
+        }
+        // a tRNS key colour makes matching pixels transparent (compared before the 8-bit cut)
+        if (ctype == 0 && trns.size() >= 2 && s[0] == (uint16_t)(trns[0] << 8 | trns[1])) o[3] = 0;
+        if (ctype == 2 && trns.size() >= 6 && s[0] == (uint16_t)(trns[0] << 8 | trns[1]) &&
+            s[1] == (uint16_t)(trns[2] << 8 | trns[3]) && s[2] == (uint16_t)(trns[4] << 8 | trns[5]))
+            o[3] = 0;
+    }
+    return SRT_OK;
+}
+
+// ---- BMP (read): uncompressed 24- and 32-bit --------------------------------------
+
+srt_status read_bmp(const std::vector<uint8_t>& b, const std::string& path, int& w, int& h, std::vector<uint8_t>& rgba)
+{
+    auto bad = [&](const std::string& why) { return set_error(SRT_ERR_PARSE, path + ": " + why); };
+    auto le32 = [&](size_t o) { return (uint32_t)b[o] | (uint32_t)b[o + 1] << 8 | (uint32_t)b[o + 2] << 16 | (uint32_t)b[o + 3] << 24; };
+    if (b.size() < 54 || b[0] != 'B' || b[1] != 'M') return bad("not a BMP file");
+    const uint32_t off = le32(10);
+    const int32_t bw = (int32_t)le32(18), bh = (int32_t)le32(22);
+    const int bitc = b[28] | b[29] << 8;
+    const uint32_t comp = le32(30);
+    if ((bitc != 24 && bitc != 32) || (comp != 0 && !(comp == 3 && bitc == 32)))
+        return set_error(SRT_ERR_UNSUPPORTED, path + ": only uncompressed 24- and 32-bit BMP files are read");
+    if (bw <= 0 || bh == 0 || bw > (1 << 16) || std::abs(bh) > (1 << 16)) return bad("bad size");
+    w = bw;
+    h = std::abs(bh);
+    const size_t row = ((size_t)w * (bitc / 8) + 3) & ~(size_t)3;
+    if (off + row * h > b.size()) return bad("truncated pixel data");
+    rgba.assign((size_t)w * h * 4, 255);
+    for (int y = 0; y < h; ++y) {
+        const int sy = bh > 0 ? h - 1 - y : y;  // positive height: rows stored bottom to top
+        const uint8_t* r = &b[off + (size_t)sy * row];
+        for (int x = 0; x < w; ++x) {
+            const uint8_t* q = r + (size_t)x * (bitc / 8);
+            uint8_t* o = &rgba[4 * ((size_t)y * w + x)];
+            o[0] = q[2];
+            o[1] = q[1];
+            o[2] = q[0];
+            if (bitc == 32) o[3] = q[3];
+        }
+    }
+    return SRT_OK;
+}
+
 }  // namespace
 
 extern "C" srt_status srt_image_write(const char* path, int32_t w, int32_t h, const float* rgba, int32_t flip)
@@ -662,12 +848,44 @@ extern "C" srt_status srt_image_read(const char* path, int32_t* width, int32_t* 
     *width = w;
     *height = h;
     if (!rgba) return SRT_OK;
-    // Image::flip(true, true) for the top-to-bottom formats; x alone for PFM
+    // Image::flip(flip_x, flip_y) for the top-to-bottom formats; PFM rows
+    // already run bottom to top, so its y flip is the identity
+    const bool fx = flip == SRT_FLIP_XY, fy = (flip == SRT_FLIP_XY || flip == SRT_FLIP_Y) && !bottom_up;
     for (int y = 0; y < h; ++y)
         for (int x = 0; x < w; ++x) {
-            const int sx = flip ? w - 1 - x : x;
-            const int sy = (flip && !bottom_up) ? h - 1 - y : y;
+            const int sx = fx ? w - 1 - x : x;
+            const int sy = fy ? h - 1 - y : y;
             std::memcpy(rgba + 4 * ((size_t)y * w + x), &px[4 * ((size_t)sy * w + sx)], 16);
+        }
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_image_read_rgba8(const char* path, int32_t* width, int32_t* height, uint8_t* rgba,
+                                           int32_t flip)
+{
+    clear_error();
+    if (!path || !width || !height) return set_error(SRT_ERR_ARG, "NULL argument");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return set_error(SRT_ERR_ARG, std::string("Failed to open file: ") + path);
+    std::vector<uint8_t> b((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    int w = 0, h = 0;
+    std::vector<uint8_t> px;
+    if (b.size() >= 8 && b[0] == 0x89 && b[1] == 'P' && b[2] == 'N' && b[3] == 'G') {
+        SRT_TRY(read_png(b, path, w, h, px));
+    } else if (b.size() >= 2 && b[0] == 'B' && b[1] == 'M') {
+        SRT_TRY(read_bmp(b, path, w, h, px));
+    } else {
+        return set_error(SRT_ERR_UNSUPPORTED, std::string(path) + ": not an 8-bit image this library reads (png, bmp)");
+    }
+    *width = w;
+    *height = h;
+    if (!rgba) return SRT_OK;
+    // Image::flip(flip_x, flip_y): SRT_FLIP_XY mirrors both, SRT_FLIP_Y rows only
+    const bool fx = flip == SRT_FLIP_XY, fy = flip == SRT_FLIP_XY || flip == SRT_FLIP_Y;
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const int sx = fx ? w - 1 - x : x, sy = fy ? h - 1 - y : y;
+            std::memcpy(rgba + 4 * ((size_t)y * w + x), &px[4 * ((size_t)sy * w + sx)], 4);
         }
     return SRT_OK;
 }

@@ -201,6 +201,116 @@ def image_set():
     np.savez_compressed(os.path.join(OUT, "image.npz"), **out)
 
 
+def png_bytes(samples, w, h, ctype, depth, interlace=0, palette=None, trns=None):
+    """A PNG written here from the specification (all five filter types in
+    turn, optional Adam7) for the decoder fixtures; samples[y][x][c]."""
+    import zlib
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+
+    def pack_row(row):
+        if depth >= 8:
+            nb = depth // 8
+            return b"".join(int(v).to_bytes(nb, "big") for px in row for v in px[:ch])
+        bits, out, acc, n = depth, bytearray(), 0, 0
+        for px in row:
+            acc = (acc << bits) | int(px[0])
+            n += bits
+            if n == 8:
+                out.append(acc)
+                acc, n = 0, 0
+        if n:
+            out.append(acc << (8 - n))
+        return bytes(out)
+
+    bpp = max(1, ch * depth // 8)
+
+    def filt(rows):
+        out, prev, k = bytearray(), None, 0
+        for r in rows:
+            r = bytearray(r)
+            p = prev if prev is not None else bytearray(len(r))
+            ft = k % 5
+            k += 1
+            f = bytearray(len(r))
+            for i in range(len(r)):
+                a = r[i - bpp] if i >= bpp else 0
+                b = p[i]
+                c = p[i - bpp] if i >= bpp else 0
+                if ft == 0:
+                    pred = 0
+                elif ft == 1:
+                    pred = a
+                elif ft == 2:
+                    pred = b
+                elif ft == 3:
+                    pred = (a + b) >> 1
+                else:
+                    pp = a + b - c
+                    pa, pb, pc = abs(pp - a), abs(pp - b), abs(pp - c)
+                    pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                f[i] = (r[i] - pred) & 0xff
+            out += bytes([ft]) + f
+            prev = r
+        return out
+
+    raw = bytearray()
+    if interlace:
+        for x0, y0, dx, dy in ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2),
+                               (0, 1, 1, 2)):
+            rows = [pack_row([samples[y][x] for x in range(x0, w, dx)]) for y in range(y0, h, dy)]
+            if rows and rows[0]:
+                raw += filt(rows)
+    else:
+        raw += filt([pack_row(samples[y]) for y in range(h)])
+
+    def chunk(t, d):
+        return len(d).to_bytes(4, "big") + t + d + (zlib.crc32(t + d) & 0xffffffff).to_bytes(4, "big")
+    out = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", w.to_bytes(4, "big") + h.to_bytes(4, "big") +
+                                       bytes([depth, ctype, 0, 0, interlace]))
+    if palette is not None:
+        out += chunk(b"PLTE", bytes(palette))
+    if trns is not None:
+        out += chunk(b"tRNS", bytes(trns))
+    return out + chunk(b"IDAT", zlib.compress(bytes(raw), 6)) + chunk(b"IEND", b"")
+
+
+PNG_CASES = (
+    # name, colour type, bit depth, interlace
+    ("g1", 0, 1, 0), ("g2", 0, 2, 0), ("g4", 0, 4, 1), ("g8", 0, 8, 0), ("g16", 0, 16, 1),
+    ("rgb8", 2, 8, 0), ("rgb16", 2, 16, 0), ("rgb8i", 2, 8, 1), ("p1", 3, 1, 0), ("p4", 3, 4, 1), ("p8", 3, 8, 0),
+    ("ga8", 4, 8, 0), ("ga16", 4, 16, 1), ("rgba8", 6, 8, 0), ("rgba16", 6, 16, 0), ("rgba8i", 6, 8, 1),
+    ("g8t", 0, 8, 0), ("rgb8t", 2, 8, 0),
+)
+
+
+def png_set():
+    """PNG decoder fixtures and what the reference's stbi_load(.., 4) makes of them."""
+    L = _img_lib()
+    rng = np.random.default_rng(23)
+    out = {}
+    for name, ctype, depth, inter in PNG_CASES:
+        w, h = 13, 11
+        ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+        top = (1 << depth) - 1 if ctype != 3 else min(15, (1 << depth) - 1)
+        smp = rng.integers(0, top + 1, size=(h, w, ch))
+        smp[2:5, 3:9] = smp[2, 3]  # a flat patch: long runs and zero filter residues
+        palette = trns = None
+        if ctype == 3:
+            palette = rng.integers(0, 256, size=3 * (top + 1)).tolist()
+            trns = rng.integers(0, 256, size=max(1, (top + 1) // 2)).tolist()
+        if name.endswith("t"):
+            key = smp[2, 3]
+            trns = [b for v in key[:ch] for b in int(v).to_bytes(2, "big")]
+        path = os.path.join(OUT, f"png_{name}.png")
+        with open(path, "wb") as f:
+            f.write(png_bytes(smp.tolist(), w, h, ctype, depth, inter, palette, trns))
+        ww, hh = C.c_int(), C.c_int()
+        a = np.zeros((w * h, 4), np.uint8)
+        assert L.ref_load_u8_image(path.encode(), C.byref(ww), C.byref(hh), a.ctypes.data_as(C.c_void_p)) == 0
+        out[name] = a
+    np.savez_compressed(os.path.join(OUT, "png.npz"), **out)
+
+
 def _ref_load(L, path):
     w, h = C.c_int(), C.c_int()
     assert L.ref_load_float_image(path.encode(), C.byref(w), C.byref(h), None) == 0
@@ -269,5 +379,6 @@ if __name__ == "__main__":
     camera_set()
     pbrt_camera_set()
     image_set()
+    png_set()
     scene_set()
     print("golden vectors written to", OUT)

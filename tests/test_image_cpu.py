@@ -196,3 +196,59 @@ def test_live_cross_check_with_the_reference_image_code(tmp_path):
             assert R.ref_load_float_image(str(tmp_path / "c.exr").encode(), C.byref(ww), C.byref(hh),
                                           ref.ctypes.data_as(C.c_void_p)) == 0
             assert _same(ours, ref)
+
+
+PNG_NAMES = ["g1", "g2", "g4", "g8", "g16", "rgb8", "rgb16", "rgb8i", "p1", "p4", "p8", "ga8", "ga16", "rgba8",
+             "rgba16", "rgba8i", "g8t", "rgb8t"]
+
+
+@pytest.mark.parametrize("name", PNG_NAMES)
+def test_png_decoder_matches_stbi_load(name):
+    """Every colour type and bit depth, palettes, tRNS keys, Adam7 and all
+    five filter types, against the reference's stbi_load(.., 4)."""
+    z = np.load(os.path.join(GOLDEN, "png.npz"))
+    px, w, h = S.image_read_rgba8(_fixture(f"png_{name}.png"), flip=False)
+    assert (w, h) == (13, 11)
+    assert np.array_equal(px, z[name])
+
+
+def test_rgba8_reader_flips_and_own_writers(tmp_path):
+    z = golden("image")
+    w, h = (int(x) for x in z["size"])
+    film = z["src"]
+    want = (np.clip(film, 0.0, 1.0) * np.float32(255.0)).astype(np.uint8)  # Image::f_to_u
+    want[~(film > 0)] = 0
+    for ext in ("png", "bmp"):
+        S.image_write(tmp_path / f"o.{ext}", film, w, h, flip=False)
+        px, rw, rh = S.image_read_rgba8(tmp_path / f"o.{ext}", flip=False)
+        assert (rw, rh) == (w, h)
+        assert np.array_equal(px[:, :3], want[:, :3])
+        if ext == "png":
+            assert np.array_equal(px[:, 3], want[:, 3])
+        xy, _, _ = S.image_read_rgba8(tmp_path / f"o.{ext}", flip="xy")
+        y, _, _ = S.image_read_rgba8(tmp_path / f"o.{ext}", flip="y")
+        assert np.array_equal(xy.reshape(h, w, 4), px.reshape(h, w, 4)[::-1, ::-1])
+        assert np.array_equal(y.reshape(h, w, 4), px.reshape(h, w, 4)[::-1])
+    with pytest.raises(S.SrtError) as e:
+        S.image_read_rgba8(_fixture("img_none.exr"))
+    assert e.value.status == 9
+    (tmp_path / "x.jpg").write_bytes(b"\xff\xd8\xff\xe0" + bytes(64))
+    with pytest.raises(S.SrtError) as e:
+        S.image_read_rgba8(tmp_path / "x.jpg")
+    assert e.value.status == 9
+
+
+@pytest.mark.skipif(not os.path.exists(REF_IMG), reason="reference image library not built here")
+def test_png_bmp_written_by_stb_read_like_stbi(tmp_path):
+    R = C.CDLL(REF_IMG)
+    z = golden("image")
+    w, h = (int(x) for x in z["size"])
+    src = np.ascontiguousarray(z["src"])
+    for kind, ext in ((1, "png"), (2, "bmp")):
+        p = str(tmp_path / f"s.{ext}").encode()
+        assert R.ref_save_stb(p, kind, w, h, src.ctypes.data_as(C.c_void_p)) == 0
+        ref = np.zeros((w * h, 4), np.uint8)
+        ww, hh = C.c_int(), C.c_int()
+        assert R.ref_load_u8_image(p, C.byref(ww), C.byref(hh), ref.ctypes.data_as(C.c_void_p)) == 0
+        ours, _, _ = S.image_read_rgba8(tmp_path / f"s.{ext}", flip=False)
+        assert np.array_equal(ours, ref)
