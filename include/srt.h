@@ -69,9 +69,11 @@ typedef struct srt_material {
     float intensity;          /* > 0 makes every instance of it an area light */
 } srt_material;
 
-/* TriangleMesh, src/scene/mesh.h:63-93.  Vertices/normals are float3
- * packed (3 floats each); indices are uint3 packed.  Tangents and
- * texture coordinates are not supported (no textures in this build). */
+/* TriangleMesh, src/scene/mesh.h:63-93.  Vertices/normals/tangents are
+ * float3 packed (3 floats each), texture coordinates float2 packed;
+ * indices are uint3 packed.  Without texcoords a hit's texture coordinate
+ * is its barycentric (u, v); without tangents the shading frame's tangent
+ * is the reference's axis choice (hit_info.h:48-52). */
 typedef struct srt_mesh {
     const float* vertices;     /* 3 * num_vertices                    */
     const uint32_t* indices;   /* 3 * num_faces                       */
@@ -79,7 +81,24 @@ typedef struct srt_mesh {
     int32_t num_vertices;
     int32_t num_faces;
     int32_t material_id;       /* index into srt_scene_desc.materials */
+    int32_t pad;
+    const float* texcoords;    /* 2 * num_vertices, or NULL           */
+    const float* tangents;     /* 3 * num_vertices, or NULL           */
 } srt_mesh;
+
+/* Texture image (Texture / Image, src/scene/texture.h), uploaded as
+ * Scene::build_gscene_textures does (src/scene/scene.cu:92-139): a CUDA
+ * array read with bilinear filtering, wrap addressing and normalised
+ * coordinates; RGBA8 texels decode as sRGB (the reference sets sRGB = 1
+ * for 8-bit images) to normalised floats, RGBA32F texels are linear.
+ * Row 0 of `pixels` is texture coordinate v = 0. */
+enum { SRT_TEXTURE_RGBA8 = 0, SRT_TEXTURE_RGBA32F = 1 };
+typedef struct srt_texture {
+    int32_t width, height;
+    int32_t format;            /* SRT_TEXTURE_*                       */
+    int32_t pad;
+    const void* pixels;        /* 4 * width * height uint8 or float   */
+} srt_texture;
 
 /* Scene::add_instance(transform, mesh), src/scene/scene.cu:194-202.
  * transform: row-major 3x4 (the top 3 rows of the reference's 4x4). */
@@ -128,6 +147,15 @@ typedef struct srt_scene_desc {
     int32_t num_materials;
     srt_camera_desc camera;
     float env_color[3];
+    /* textures (zero / NULL: none) */
+    const srt_texture* textures;
+    int32_t num_textures;
+    /* "uvmap" environment (EnvironmentLight::emission, light.h:27-41):
+     * texture index + 1, or 0 for the constant env_color */
+    int32_t env_map;
+    /* per material: color_tex, normal_tex texture indices or -1
+     * (GMaterial, gmaterial.h:13-56); NULL: no material is textured */
+    const int32_t* material_textures;
 } srt_scene_desc;
 
 typedef struct srt_scene srt_scene;
@@ -168,6 +196,11 @@ srt_status srt_trace_closest(const srt_scene* scene, const float* rays, int64_t 
 /* visible: n int32 (1 = unoccluded in (tmin, tmax), 0 = occluded), device. */
 srt_status srt_trace_shadow(const srt_scene* scene, const float* rays, int64_t n,
                             int32_t* visible, void* stream);
+/* tex2D<float4> of the scene's texture `texture` (srt_scene_desc.textures
+ * order) at n normalised coordinates: uv n x 2 floats, out n x 4 floats,
+ * both device memory.  The lookups the shading kernel makes. */
+srt_status srt_scene_texture_lookup(const srt_scene* scene, int32_t texture, const float* uv, int64_t n,
+                                    float* out, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* Path tracing pass (src/passes/integrator/path_tracer.{h,cu})         */

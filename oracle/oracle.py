@@ -58,6 +58,7 @@ def lib():
             "oracle_camera_rays": (None, [_vp, _i64, _vp, _vp]),
             "oracle_light_sample": (None, [_vp, _i64, _vp, C.c_int, _vp]),
             "oracle_hitinfo": (None, [_vp, _i64, _vp, _vp, _vp]),
+            "oracle_texture_lookup": (None, [_vp, C.c_int, _i64, _vp, _vp]),
             "oracle_render": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int,
                                         C.c_int, _vp, _vp, _vp, _vp]),
             "oracle_accumulate": (None, [_vp, _vp, _i64, C.c_int]),
@@ -179,6 +180,12 @@ class OracleScene:
         uv = np.ascontiguousarray(uv, np.float32)
         out = np.zeros((len(prim), 15), np.float32)
         lib().oracle_hitinfo(self.h, len(prim), _np(prim), _np(uv), _np(out))
+        return out
+
+    def texture_lookup(self, texture, uv):
+        uv = np.ascontiguousarray(uv, np.float32)
+        out = np.zeros((len(uv), 4), np.float32)
+        lib().oracle_texture_lookup(self.h, int(texture), len(uv), _np(uv), _np(out))
         return out
 
     def render(self, w, h, params, crop=None, threads=8):

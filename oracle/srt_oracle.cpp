@@ -522,7 +522,8 @@ struct Xf {  // row-major 3x4 (Transform, math/transform.h:208-240)
 };
 
 struct OMesh {
-    std::vector<F3> v, n;
+    std::vector<F3> v, n, tg;
+    std::vector<float> tc;  // 2 per vertex when the mesh has texture coordinates
     std::vector<uint32_t> idx;
     int material;
     float area = 0.0f;
@@ -548,7 +549,48 @@ struct Camera {
 
 }  // namespace
 
+// A texture read as a CUDA texture object with linear filtering, wrap
+// addressing and normalised coordinates (scene.cu:92-139), computed
+// exactly: texel centres at (i + 0.5) / size, bilinear weights without the
+// hardware's 8-bit fixed-point quantisation, and 8-bit texels decoded with
+// the sRGB transfer function of IEC 61966-2-1 (the hardware's decode is a
+// coarser table), alpha linear.  Comparisons with the GPU carry a tolerance.
+struct OTex {
+    int w = 0, h = 0;
+    std::vector<double> lin;  // RGBA per texel, decoded
+    F3 rgb(float x, float y) const
+    {
+        double fx = (double)x - std::floor((double)x), fy = (double)y - std::floor((double)y);
+        double xb = fx * w - 0.5, yb = fy * h - 0.5;
+        double i0 = std::floor(xb), j0 = std::floor(yb);
+        double a = xb - i0, b = yb - j0;
+        int i = ((int)i0 % w + w) % w, j = ((int)j0 % h + h) % h;
+        int i1 = (i + 1) % w, j1 = (j + 1) % h;
+        double r[3];
+        for (int c = 0; c < 3; ++c)
+            r[c] = (1 - a) * (1 - b) * lin[4 * ((size_t)j * w + i) + c] + a * (1 - b) * lin[4 * ((size_t)j * w + i1) + c] +
+                   (1 - a) * b * lin[4 * ((size_t)j1 * w + i) + c] + a * b * lin[4 * ((size_t)j1 * w + i1) + c];
+        return F3((float)r[0], (float)r[1], (float)r[2]);
+    }
+    void fetch4(float x, float y, float* out) const
+    {
+        double fx = (double)x - std::floor((double)x), fy = (double)y - std::floor((double)y);
+        double xb = fx * w - 0.5, yb = fy * h - 0.5;
+        double i0 = std::floor(xb), j0 = std::floor(yb);
+        double a = xb - i0, b = yb - j0;
+        int i = ((int)i0 % w + w) % w, j = ((int)j0 % h + h) % h;
+        int i1 = (i + 1) % w, j1 = (j + 1) % h;
+        for (int c = 0; c < 4; ++c)
+            out[c] = (float)((1 - a) * (1 - b) * lin[4 * ((size_t)j * w + i) + c] +
+                             a * (1 - b) * lin[4 * ((size_t)j * w + i1) + c] +
+                             (1 - a) * b * lin[4 * ((size_t)j1 * w + i) + c] + a * b * lin[4 * ((size_t)j1 * w + i1) + c]);
+    }
+};
+
 struct oracle_scene {
+    std::vector<OTex> tex;
+    std::vector<int> mat_tex;  // 2 per material (colour, normal), -1 none
+    int env_map = -1;
     std::vector<OMesh> meshes;
     std::vector<OInst> inst;
     std::vector<srt_material> mats;
@@ -667,6 +709,16 @@ LSample light_sample(const oracle_scene& s, float ux, float uy, bool fixed)
     ls.pos = in.xf.point(pos);
     ls.normal = in.xf.vec(nrm);
     ls.emission = cvt<float>(mat.emission_color) * mat.intensity;
+    const int ct = s.mat_tex.empty() ? -1 : s.mat_tex[2 * m.material];
+    if (ct >= 0) {
+        // GMaterial::emission(texcoord) (gmaterial.h:35-41)
+        float tu = bu, tv = bv;
+        if (!m.tc.empty()) {
+            tu = m.tc[2 * i0] * (1.0f - bu - bv) + m.tc[2 * i1] * bu + m.tc[2 * i2] * bv;
+            tv = m.tc[2 * i0 + 1] * (1.0f - bu - bv) + m.tc[2 * i1 + 1] * bu + m.tc[2 * i2 + 1] * bv;
+        }
+        ls.emission = s.tex[ct].rgb(tu, tv) * mat.intensity;
+    }
     ls.pdf = mat.intensity / s.weight_sum;
     return ls;
 }
@@ -911,7 +963,7 @@ Hit trace(const oracle_scene& s, F3 o, F3 d, float tmin, float tmax, bool any_hi
 }
 
 struct HitInfo {
-    F3 pos, normal, color;
+    F3 pos, normal, color, emission;
     Onb<float> onb;
     int mat;
     int light_id;
@@ -926,16 +978,27 @@ HitInfo hit_info(const oracle_scene& s, int64_t prim, float u, float v)
     uint32_t i0 = m.idx[3 * f], i1 = m.idx[3 * f + 1], i2 = m.idx[3 * f + 2];
     F3 v0 = m.v[i0], v1 = m.v[i1], v2 = m.v[i2];
     F3 pos = v0 * (1.0f - u - v) + v1 * u + v2 * v;
+    float tu = u, tv = v;
+    if (!m.tc.empty()) {
+        tu = m.tc[2 * i0] * (1.0f - u - v) + m.tc[2 * i1] * u + m.tc[2 * i2] * v;
+        tv = m.tc[2 * i0 + 1] * (1.0f - u - v) + m.tc[2 * i1 + 1] * u + m.tc[2 * i2 + 1] * v;
+    }
+    const int ct = s.mat_tex.empty() ? -1 : s.mat_tex[2 * m.material];
+    const int nt = s.mat_tex.empty() ? -1 : s.mat_tex[2 * m.material + 1];
     F3 nrm = normalize(cross(v1 - v0, v2 - v0));
     F3 sn = nrm;
     if (!m.n.empty()) sn = normalize(m.n[i0] * (1.0f - u - v) + m.n[i1] * u + m.n[i2] * v);
+    if (nt >= 0) sn = normalize(s.tex[nt].rgb(tu, tv));  // GMaterial::shading_normal (gmaterial.h:43-48)
     if (dot(nrm, sn) < 0.0f) nrm = -nrm;
     F3 tan = (std::fabs(sn.x) > std::fabs(sn.y)) ? F3(0, 1, 0) : F3(1, 0, 0);
+    if (!m.tg.empty()) tan = m.tg[i0] * (1.0f - u - v) + m.tg[i1] * u + m.tg[i2] * v;
     Onb<float> ob = Onb<float>::from_nt(sn, tan);
     HitInfo h;
     h.pos = in.xf.point(pos);
     h.normal = in.xf.vec(nrm);
-    h.color = cvt<float>(s.mats[m.material].base_color);
+    h.color = ct >= 0 ? s.tex[ct].rgb(tu, tv) : cvt<float>(s.mats[m.material].base_color);
+    h.emission = cvt<float>(s.mats[m.material].emission_color) * s.mats[m.material].intensity;
+    if (ct >= 0) h.emission = h.color * s.mats[m.material].intensity;  // GMaterial::emission (gmaterial.h:35-41)
     h.onb.z = in.xf.vec(ob.z);
     h.onb.x = in.xf.vec(ob.x);
     h.onb.y = in.xf.vec(ob.y);
@@ -965,6 +1028,17 @@ struct Rng {
     }
 };
 
+// EnvironmentLight::emission (light.h:27-41): constant, or the "uvmap"
+// texture at the direction's spherical coordinates (world y up)
+F3 env_radiance(const oracle_scene& s, F3 d)
+{
+    if (s.env_map < 0) return s.env;
+    const float mx = -d.x, my = d.z, mz = d.y;
+    const float phi = std::atan2(my, mx), theta = std::acos(mz);  // cartesian_to_spherical_uv (basic.h:41-46)
+    const float u = phi * 0.5f * (float)M_1_PI + 0.5f, v = theta * (float)M_1_PI;
+    return s.tex[s.env_map].rgb(u, v);
+}
+
 // Megakernel raygen loop (src/shader/integrator/path_tracer.cu:50-169).
 void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt_pt_params& p, bool use_bvh,
                   float* film, double* sum, double* sumsq, int64_t* cnt)
@@ -991,7 +1065,7 @@ void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt
             cnt[3]++;
             Hit hit = trace(s, ro, rd, 1e-3f, 1e16f, false, use_bvh);
             if (hit.prim < 0) {
-                L = L + beta * s.env;
+                L = L + beta * env_radiance(s, rd);
                 break;
             }
             HitInfo hi = hit_info(s, hit.prim, hit.u, hit.v);
@@ -1009,8 +1083,7 @@ void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt
                         mis = scatter_pdf / (lpdf + scatter_pdf);
                     }
                 }
-                F3 em = cvt<float>(mat.emission_color) * mat.intensity;
-                L = L + beta * em * mis;
+                L = L + beta * hi.emission * mis;
                 break;
             }
             float cos_i = dot(hi.normal, -rd);
@@ -1233,7 +1306,9 @@ oracle_scene* oracle_scene_create(const srt_scene_desc* d)
         for (int k = 0; k < m.num_vertices; ++k) {
             om.v.push_back(cvt<float>(m.vertices + 3 * k));
             if (m.normals) om.n.push_back(cvt<float>(m.normals + 3 * k));
+            if (m.tangents) om.tg.push_back(cvt<float>(m.tangents + 3 * k));
         }
+        if (m.texcoords) om.tc.assign(m.texcoords, m.texcoords + 2 * (size_t)m.num_vertices);
         om.idx.assign(m.indices, m.indices + 3 * (size_t)m.num_faces);
         // TriangleMesh::compute_area (src/scene/mesh.cpp:3-18)
         om.area_cdf.resize(m.num_faces);
@@ -1280,7 +1355,30 @@ oracle_scene* oracle_scene_create(const srt_scene_desc* d)
     s->weight_sum = wsum;
     s->env = cvt<float>(d->env_color);
     s->cam = make_camera(d->camera);
+    for (int i = 0; i < d->num_textures; ++i) {
+        const srt_texture& t = d->textures[i];
+        OTex o;
+        o.w = t.width;
+        o.h = t.height;
+        o.lin.resize(4 * (size_t)t.width * t.height);
+        for (size_t k = 0; k < o.lin.size(); ++k) {
+            if (t.format == SRT_TEXTURE_RGBA8) {
+                const double c = static_cast<const uint8_t*>(t.pixels)[k] / 255.0;
+                o.lin[k] = (k % 4 == 3) ? c : (c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+            } else {
+                o.lin[k] = static_cast<const float*>(t.pixels)[k];
+            }
+        }
+        s->tex.push_back(std::move(o));
+    }
+    if (d->material_textures) s->mat_tex.assign(d->material_textures, d->material_textures + 2 * d->num_materials);
+    s->env_map = d->env_map - 1;
     return s;
+}
+
+void oracle_texture_lookup(const oracle_scene* s, int texture, int64_t n, const float* uv, float* out)
+{
+    for (int64_t i = 0; i < n; ++i) s->tex[texture].fetch4(uv[2 * i], uv[2 * i + 1], out + 4 * i);
 }
 
 void oracle_scene_destroy(oracle_scene* s) { delete s; }

@@ -67,6 +67,10 @@ void oracle_camera_rays(const srt_camera_desc* cam, int64_t n, const float* xy, 
 /* get_hitinfo for global primitive ids: pos, normal, onb z, x, y (n x 15). */
 void oracle_hitinfo(const oracle_scene* s, int64_t n, const int32_t* prim, const float* uv, float* out);
 
+/* An exact bilinear / sRGB restatement of a tex2D<float4> lookup of the
+ * scene's texture `texture` at n coordinates (uv n x 2 -> out n x 4). */
+void oracle_texture_lookup(const oracle_scene* s, int texture, int64_t n, const float* uv, float* out);
+
 /* Light::sample(u) -> pos, normal, emission, pdf (n x 10 floats). */
 void oracle_light_sample(const oracle_scene* s, int64_t n, const float* u2, int fixed_remap,
                          float* out);

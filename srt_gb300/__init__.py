@@ -37,12 +37,16 @@ class SceneArrays:
     builds the srt_scene_desc struct; it keeps the arrays alive."""
 
     def __init__(self):
-        self.meshes = []      # dicts: vertices (V,3) f32, indices (F,3) u32, normals or None, material
+        self.meshes = []      # dicts: vertices (V,3) f32, indices (F,3) u32, normals, texcoords (V,2),
+        #                       tangents (V,3) (each optional / None), material
         self.instances = []   # (mesh_id, 3x4 transform)
         self.materials = []   # _capi.Material
         self.camera = _capi.CameraDesc()
         self.env = (0.0, 0.0, 0.0)
         self.resolution = (0, 0)  # film size an imported file asks for
+        self.textures = []    # (H, W, 4) uint8 (sRGB) or float32 (linear) arrays, row 0 = v 0
+        self.material_textures = None  # per material (color, normal) texture index or -1; None: untextured
+        self.env_map = None   # texture index of a "uvmap" environment
 
     def desc(self):
         n = len(self.meshes)
@@ -52,11 +56,15 @@ class SceneArrays:
             v = np.ascontiguousarray(m["vertices"], dtype=np.float32).reshape(-1, 3)
             f = np.ascontiguousarray(m["indices"], dtype=np.uint32).reshape(-1, 3)
             nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32).reshape(-1, 3)
-            self._keep += [v, f, nr]
+            tc = None if m.get("texcoords") is None else np.ascontiguousarray(m["texcoords"], np.float32).reshape(-1, 2)
+            tg = None if m.get("tangents") is None else np.ascontiguousarray(m["tangents"], np.float32).reshape(-1, 3)
+            self._keep += [v, f, nr, tc, tg]
             d = self._mesh_arr[i]
             d.vertices = v.ctypes.data_as(_capi.f32p)
             d.indices = f.ctypes.data_as(_capi.u32p)
             d.normals = nr.ctypes.data_as(_capi.f32p) if nr is not None else None
+            d.texcoords = tc.ctypes.data_as(_capi.f32p) if tc is not None else None
+            d.tangents = tg.ctypes.data_as(_capi.f32p) if tg is not None else None
             d.num_vertices, d.num_faces, d.material_id = len(v), len(f), int(m["material"])
         self._inst_arr = (_capi.Instance * max(1, len(self.instances)))()
         for i, (mid, xf) in enumerate(self.instances):
@@ -71,6 +79,22 @@ class SceneArrays:
         d.camera = self.camera
         for k in range(3):
             d.env_color[k] = float(self.env[k])
+        if self.textures:
+            self._tex_arr = (_capi.Texture * len(self.textures))()
+            for i, t in enumerate(self.textures):
+                a = np.ascontiguousarray(t)
+                assert a.ndim == 3 and a.shape[2] == 4 and a.dtype in (np.uint8, np.float32)
+                self._keep.append(a)
+                tt = self._tex_arr[i]
+                tt.height, tt.width = a.shape[0], a.shape[1]
+                tt.format = _capi.TEXTURE_RGBA8 if a.dtype == np.uint8 else _capi.TEXTURE_RGBA32F
+                tt.pixels = a.ctypes.data_as(C.c_void_p)
+            d.textures, d.num_textures = self._tex_arr, len(self.textures)
+        d.env_map = 0 if self.env_map is None else int(self.env_map) + 1
+        if self.material_textures is not None:
+            mt = np.ascontiguousarray(np.asarray(self.material_textures, np.int32).reshape(-1, 2))
+            self._keep.append(mt)
+            d.material_textures = mt.ctypes.data_as(C.POINTER(C.c_int32))
         self._desc = d
         return d
 
@@ -92,10 +116,15 @@ def _arrays_of(h) -> SceneArrays:
         m = d.meshes[i]
         v = np.ctypeslib.as_array(m.vertices, shape=(m.num_vertices * 3,)).reshape(-1, 3).copy()
         f = np.ctypeslib.as_array(m.indices, shape=(m.num_faces * 3,)).reshape(-1, 3).copy()
-        n = None
+        n = tc = tg = None
         if m.normals and m.num_vertices:
             n = np.ctypeslib.as_array(m.normals, shape=(m.num_vertices * 3,)).reshape(-1, 3).copy()
-        s.meshes.append({"vertices": v, "indices": f, "normals": n, "material": m.material_id})
+        if m.texcoords and m.num_vertices:
+            tc = np.ctypeslib.as_array(m.texcoords, shape=(m.num_vertices * 2,)).reshape(-1, 2).copy()
+        if m.tangents and m.num_vertices:
+            tg = np.ctypeslib.as_array(m.tangents, shape=(m.num_vertices * 3,)).reshape(-1, 3).copy()
+        s.meshes.append({"vertices": v, "indices": f, "normals": n, "texcoords": tc, "tangents": tg,
+                         "material": m.material_id})
     for i in range(d.num_instances):
         s.instances.append((d.instances[i].mesh_id, np.array(d.instances[i].transform[:], np.float32)))
     for i in range(d.num_materials):
@@ -104,6 +133,15 @@ def _arrays_of(h) -> SceneArrays:
         s.materials.append(mm)
     C.memmove(C.byref(s.camera), C.byref(d.camera), C.sizeof(_capi.CameraDesc))
     s.env = tuple(d.env_color[:])
+    for i in range(d.num_textures):
+        t = d.textures[i]
+        dt, nb = (np.uint8, 1) if t.format == _capi.TEXTURE_RGBA8 else (np.float32, 4)
+        buf = (C.c_uint8 * (t.width * t.height * 4 * nb)).from_address(t.pixels)
+        s.textures.append(np.frombuffer(buf, dt).reshape(t.height, t.width, 4).copy())
+    s.env_map = d.env_map - 1 if d.env_map > 0 else None
+    if d.material_textures:
+        s.material_textures = [(d.material_textures[2 * i], d.material_textures[2 * i + 1])
+                               for i in range(d.num_materials)]
     w, hh = C.c_int32(), C.c_int32()
     check(L.srt_procedural_resolution(h, C.byref(w), C.byref(hh)))
     s.resolution = (w.value, hh.value)

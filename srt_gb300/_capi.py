@@ -45,7 +45,16 @@ class Material(C.Structure):
 
 class Mesh(C.Structure):
     _fields_ = [("vertices", f32p), ("indices", u32p), ("normals", f32p), ("num_vertices", C.c_int32),
-                ("num_faces", C.c_int32), ("material_id", C.c_int32)]
+                ("num_faces", C.c_int32), ("material_id", C.c_int32), ("pad", C.c_int32),
+                ("texcoords", f32p), ("tangents", f32p)]
+
+
+TEXTURE_RGBA8, TEXTURE_RGBA32F = 0, 1
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("format", C.c_int32), ("pad", C.c_int32),
+                ("pixels", C.c_void_p)]
 
 
 class Instance(C.Structure):
@@ -62,7 +71,9 @@ class SceneDesc(C.Structure):
     _fields_ = [("meshes", C.POINTER(Mesh)), ("num_meshes", C.c_int32),
                 ("instances", C.POINTER(Instance)), ("num_instances", C.c_int32),
                 ("materials", C.POINTER(Material)), ("num_materials", C.c_int32),
-                ("camera", CameraDesc), ("env_color", C.c_float * 3)]
+                ("camera", CameraDesc), ("env_color", C.c_float * 3),
+                ("textures", C.POINTER(Texture)), ("num_textures", C.c_int32), ("env_map", C.c_int32),
+                ("material_textures", C.POINTER(C.c_int32))]
 
 
 class SceneInfo(C.Structure):
@@ -131,6 +142,7 @@ _PROTOS = [
     ("srt_scene_destroy", None, [C.c_void_p]),
     ("srt_trace_closest", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("srt_trace_shadow", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("srt_scene_texture_lookup", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("srt_pt_create", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     ("srt_pt_render", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PtParams), C.c_void_p]),
     ("srt_pt_get_stats", C.c_int, [C.c_void_p, C.POINTER(PtStats)]),

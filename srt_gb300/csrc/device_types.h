@@ -8,6 +8,12 @@
 //   tri_prim  int32[num_tris]         BVH order -> global primitive id
 //   normals   float4[3 * num_tris]    per-corner shading normals (only when
 //                                     some mesh has vertex normals)
+//   texcoords float2[3 * num_tris]    per-corner texture coordinates (only
+//                                     when some mesh has them)
+//   tangents  float4[3 * num_tris]    per-corner world tangents (likewise)
+//   mat_tex   u64[2 * num_mats]       colour / normal texture objects (only
+//                                     when some material is textured)
+//   inst_xf   float4[3 * num_insts]   instance rows (only with normal maps)
 //   insts     InstanceRec[num_insts]  material / light id per instance
 //   mats      MaterialRec[num_mats]   80 B, read with five 16-byte loads
 //   lights    LightRec[num_lights]    area-light table
@@ -42,10 +48,13 @@ struct alignas(128) WideNode {
 };
 static_assert(sizeof(WideNode) == 128, "WideNode must be one 128-byte line");
 
+// InstanceRec::attr bits: which per-corner arrays the instance's mesh has
+constexpr int32_t kAttrNormals = 1, kAttrTexcoords = 2, kAttrTangents = 4;
+
 struct InstanceRec {
     int32_t material;
     int32_t light_id;     // -1 if not an area light
-    int32_t has_normals;
+    int32_t attr;         // kAttr* bits
     int32_t pad;
 };
 
@@ -63,7 +72,7 @@ struct LightRec {
     int32_t face_begin;   // into face_cdf / light_tri
     int32_t num_faces;
     float pdf;            // intensity / weight_sum (light.h:73-76)
-    int32_t pad;
+    int32_t textured;     // the light's material has a colour texture (its emission)
 };
 
 // Camera after Camera::reset / CameraController(LookAt) on the host
@@ -90,6 +99,11 @@ struct SceneView {
     int32_t num_tris;
     float3 env;
     float weight_sum;
+    const float2* texcoords;               // may be null
+    const float4* tangents;                // may be null
+    const unsigned long long* mat_tex;     // may be null: (color, normal) per material, 0 = none
+    const float4* inst_xf;                 // may be null
+    unsigned long long env_tex;            // 0: constant env
 };
 
 }  // namespace srt

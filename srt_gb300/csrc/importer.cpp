@@ -11,11 +11,13 @@
 //   Shape trianglemesh / plymesh, AreaLightSource diffuse "rgb L",
 //   AttributeBegin / AttributeEnd (one shape per attribute block, its
 //   emission written into the block's material, pbrtparse.cu:474-491),
-//   MakeNamedMedium / MediumInterface skipped.  Textures are not built in
-//   this library: a Texture statement is an SRT_ERR_UNSUPPORTED error.
+//   MakeNamedMedium / MediumInterface skipped, Texture "name" "spectrum"
+//   "imagemap" (the image flipped in y as load_texture does) with
+//   "texture reflectance" naming a material's colour texture, and
+//   trianglemesh "point2 uv" / "float3 tangent".
 // .ply meshes: ascii or binary_little_endian; vertex x y z (float or double),
-//   optional nx ny nz, other vertex properties skipped; triangular faces
-//   from a "vertex_indices" (or "vertex_index") list.
+//   optional nx ny nz and u v, other vertex properties skipped; triangular
+//   faces from a "vertex_indices" (or "vertex_index") list.
 // .obj (with .mtl): what the reference reads through Assimp
 //   (src/importer/assimp.cu:17-79, flags Triangulate | GenNormals): one
 //   mesh per object / group and material, polygons split into triangle
@@ -24,8 +26,12 @@
 //   Kd (or Ks when Kd is black) as base colour, Ke as emission (intensity
 //   |Ke|), Ni as ior, Pr roughness, Pm metallic, Ps sheen, Pc clearcoat,
 //   Pcr clearcoat roughness, aniso anisotropic, with ai_convert's defaults
-//   for the rest; faces before any usemtl get a grey (0.6) default.
+//   for the rest; faces before any usemtl get a grey (0.6) default; "vt"
+//   texture coordinates with v flipped (aiProcess_FlipUVs), map_Kd as the
+//   colour texture and norm / map_Kn as the normal texture, loaded
+//   unflipped next to the model (AssimpImporter::load_texture).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -83,6 +89,7 @@ void set_emission(srt_material& m, float r, float g, float b)
 struct ObjMaterial {
     float kd[3] = {0.6f, 0.6f, 0.6f}, ks[3] = {0, 0, 0}, ke[3] = {0, 0, 0};
     float ni = 1.0f, pr = 0.5f, pm = 0.0f, ps = 0.0f, pc = 0.0f, pcr = 0.0f, aniso = 0.0f;
+    std::string map_kd, norm;  // diffuse and normal textures (aiTextureType_DIFFUSE / _NORMALS)
 };
 
 // ai_convert(aiMaterial*), assimp.cu:17-79
@@ -129,6 +136,13 @@ srt_status read_mtl(const std::string& path, std::map<std::string, ObjMaterial>&
         else if (key == "Pc") ls >> m.pc;
         else if (key == "Pcr") ls >> m.pcr;
         else if (key == "aniso") ls >> m.aniso;
+        else if (key == "map_Kd" || key == "norm" || key == "map_Kn") {
+            // the file name is the last word (options such as -s u v come first)
+            std::string w, last;
+            while (ls >> w) last = w;
+            std::replace(last.begin(), last.end(), '\\', '/');
+            (key == "map_Kd" ? m.map_kd : m.norm) = last;
+        }
     }
     return SRT_OK;
 }
@@ -141,13 +155,13 @@ srt_status import_obj(const std::string& path, srt_procedural& p)
 {
     std::ifstream f(path);
     if (!f) return set_error(SRT_ERR_ARG, "cannot open " + path);
-    std::vector<float> pos, nrm;
+    std::vector<float> pos, nrm, uvs;
     std::map<std::string, ObjMaterial> lib;
     struct Build {
         HostMesh mesh;
         std::string material;
-        std::unordered_map<uint64_t, uint32_t> corner;  // (position, normal) -> vertex
-        bool any_normal = false;
+        std::map<std::array<int64_t, 3>, uint32_t> corner;  // (position, texcoord, normal) -> vertex
+        bool any_normal = false, any_uv = false;
     };
     std::vector<Build> built;
     std::string material;
@@ -167,6 +181,10 @@ srt_status import_obj(const std::string& path, srt_procedural& p)
             float x = 0, y = 0, z = 0;
             ls >> x >> y >> z;
             nrm.insert(nrm.end(), {x, y, z});
+        } else if (key == "vt") {
+            float u = 0, v = 0;
+            ls >> u >> v;
+            uvs.insert(uvs.end(), {u, 1.0f - v});  // aiProcess_FlipUVs
         } else if (key == "o" || key == "g") {
             fresh = true;
         } else if (key == "usemtl") {
@@ -179,23 +197,26 @@ srt_status import_obj(const std::string& path, srt_procedural& p)
             ls >> name;
             SRT_TRY(read_mtl(dir_of(path) + name, lib));
         } else if (key == "f") {
-            std::vector<std::pair<int64_t, int64_t>> corners;  // (position, normal or -1)
+            std::vector<std::array<int64_t, 3>> corners;  // (position, texcoord or -1, normal or -1)
             std::string tok;
-            const int64_t np = (int64_t)(pos.size() / 3), nn = (int64_t)(nrm.size() / 3);
+            const int64_t np = (int64_t)(pos.size() / 3), nn = (int64_t)(nrm.size() / 3), nt = (int64_t)(uvs.size() / 2);
             while (ls >> tok) {
-                int64_t vi = 0, ni = 0;
+                int64_t vi = 0, ti = 0, ni = 0;
                 size_t s1 = tok.find('/');
                 vi = std::strtoll(tok.substr(0, s1).c_str(), nullptr, 10);
                 if (s1 != std::string::npos) {
                     size_t s2 = tok.find('/', s1 + 1);
+                    const std::string t = tok.substr(s1 + 1, s2 == std::string::npos ? std::string::npos : s2 - s1 - 1);
+                    if (!t.empty()) ti = std::strtoll(t.c_str(), nullptr, 10);
                     if (s2 != std::string::npos && s2 + 1 < tok.size())
                         ni = std::strtoll(tok.substr(s2 + 1).c_str(), nullptr, 10);
                 }
                 vi = vi < 0 ? np + vi : vi - 1;  // OBJ indices are 1-based; negative ones count back
+                ti = ti == 0 ? -1 : (ti < 0 ? nt + ti : ti - 1);
                 ni = ni == 0 ? -1 : (ni < 0 ? nn + ni : ni - 1);
-                if (vi < 0 || vi >= np || ni >= nn || ni < -1)
+                if (vi < 0 || vi >= np || ni >= nn || ni < -1 || ti >= nt || ti < -1)
                     return set_error(SRT_ERR_PARSE, path + ":" + std::to_string(lineno) + ": face index out of range");
-                corners.emplace_back(vi, ni);
+                corners.push_back({vi, ti, ni});
             }
             if (corners.size() < 3) continue;
             if (fresh || built.empty()) {
@@ -206,16 +227,22 @@ srt_status import_obj(const std::string& path, srt_procedural& p)
             Build& b = built.back();
             std::vector<uint32_t> id(corners.size());
             for (size_t c = 0; c < corners.size(); ++c) {
-                const uint64_t k = (uint64_t)corners[c].first << 32 | (uint64_t)(uint32_t)(corners[c].second + 1);
+                const std::array<int64_t, 3>& k = corners[c];
                 auto ct = b.corner.find(k);
                 if (ct == b.corner.end()) {
                     const uint32_t v = (uint32_t)(b.mesh.v.size() / 3);
-                    b.mesh.v.insert(b.mesh.v.end(), &pos[3 * corners[c].first], &pos[3 * corners[c].first] + 3);
-                    if (corners[c].second >= 0) {
+                    b.mesh.v.insert(b.mesh.v.end(), &pos[3 * k[0]], &pos[3 * k[0]] + 3);
+                    if (k[2] >= 0) {
                         b.any_normal = true;
-                        b.mesh.n.insert(b.mesh.n.end(), &nrm[3 * corners[c].second], &nrm[3 * corners[c].second] + 3);
+                        b.mesh.n.insert(b.mesh.n.end(), &nrm[3 * k[2]], &nrm[3 * k[2]] + 3);
                     } else {
                         b.mesh.n.insert(b.mesh.n.end(), {0.0f, 0.0f, 0.0f});
+                    }
+                    if (k[1] >= 0) {
+                        b.any_uv = true;
+                        b.mesh.tc.insert(b.mesh.tc.end(), &uvs[2 * k[1]], &uvs[2 * k[1]] + 2);
+                    } else {
+                        b.mesh.tc.insert(b.mesh.tc.end(), {0.0f, 0.0f});
                     }
                     ct = b.corner.emplace(k, v).first;
                 }
@@ -226,7 +253,24 @@ srt_status import_obj(const std::string& path, srt_procedural& p)
             for (size_t c = 1; c + 1 < id.size(); ++c) b.mesh.idx.insert(b.mesh.idx.end(), {id[0], id[c], id[c + 1]});
         }
     }
+    std::map<std::string, int> tex_index;  // texture file -> scene texture (load_texture, assimp.cu:170-190)
+    auto texture = [&](const std::string& name, int& out) -> srt_status {
+        out = -1;
+        if (name.empty()) return SRT_OK;
+        auto it = tex_index.find(name);
+        if (it != tex_index.end()) {
+            out = it->second;
+            return SRT_OK;
+        }
+        HostTexture t;
+        t.name = name;
+        SRT_TRY(load_texture_image(dir_of(path) + name, false, t));
+        p.textures.push_back(std::move(t));
+        out = tex_index[name] = (int)p.textures.size() - 1;
+        return SRT_OK;
+    };
     for (Build& b : built) {
+        if (!b.any_uv) b.mesh.tc.clear();
         if (!b.any_normal) {
             b.mesh.n.clear();
         } else {
@@ -252,8 +296,17 @@ srt_status import_obj(const std::string& path, srt_procedural& p)
         // faces before any usemtl, or naming a material the library lacks,
         // get the reader's default material
         auto lt = lib.find(b.material);
-        p.mats.push_back(obj_material(lt == lib.end() ? ObjMaterial() : lt->second));
+        const ObjMaterial om = lt == lib.end() ? ObjMaterial() : lt->second;
+        p.mats.push_back(obj_material(om));
         b.mesh.material = (int)p.mats.size() - 1;
+        int ct = -1, nt = -1;
+        SRT_TRY(texture(om.map_kd, ct));
+        SRT_TRY(texture(om.norm, nt));
+        if (ct >= 0 || nt >= 0 || !p.mat_tex.empty()) {
+            p.mat_tex.resize(2 * p.mats.size(), -1);
+            p.mat_tex[2 * b.mesh.material] = ct;
+            p.mat_tex[2 * b.mesh.material + 1] = nt;
+        }
         p.meshes.push_back(std::move(b.mesh));
     }
     return SRT_OK;
@@ -340,7 +393,7 @@ srt_status read_ply(const std::string& path, HostMesh& m)
     };
     for (const Elem& e : elems) {
         const bool is_v = e.name == "vertex", is_f = e.name == "face";
-        int ix = -1, iy = -1, iz = -1, inx = -1, iny = -1, inz = -1;
+        int ix = -1, iy = -1, iz = -1, inx = -1, iny = -1, inz = -1, iu = -1, iv = -1;
         for (size_t i = 0; i < e.props.size(); ++i) {
             const std::string& n = e.props[i].name;
             if (n == "x") ix = (int)i;
@@ -349,7 +402,10 @@ srt_status read_ply(const std::string& path, HostMesh& m)
             if (n == "nx") inx = (int)i;
             if (n == "ny") iny = (int)i;
             if (n == "nz") inz = (int)i;
+            if (n == "u") iu = (int)i;
+            if (n == "v") iv = (int)i;
         }
+        const bool uvs = is_v && iu >= 0 && iv >= 0 && iu < 16 && iv < 16;
         const bool normals = is_v && inx >= 0 && iny >= 0 && inz >= 0;
         for (int64_t r = 0; r < e.count; ++r) {
             double vals[16] = {};
@@ -378,6 +434,7 @@ srt_status read_ply(const std::string& path, HostMesh& m)
                 m.v.insert(m.v.end(), {(float)vals[ix], (float)vals[iy], (float)vals[iz]});
                 if (normals && inx < 16 && iny < 16 && inz < 16)
                     m.n.insert(m.n.end(), {(float)vals[inx], (float)vals[iny], (float)vals[inz]});
+                if (uvs) m.tc.insert(m.tc.end(), {(float)vals[iu], (float)vals[iv]});
             }
         }
     }
@@ -535,8 +592,6 @@ srt_status pbrt_material(const std::string& type, const std::map<std::string, st
     m = disney_default();
     m.bxdf.roughness = 0.5f;
     m.base_color[0] = m.base_color[1] = m.base_color[2] = 0.0f;
-    if (p.count("texture reflectance"))
-        return set_error(SRT_ERR_UNSUPPORTED, "textures are not built (material reflectance texture)");
     auto it = p.find("rgb reflectance");
     if (it != p.end()) {
         std::vector<float> c = floats(it->second);
@@ -585,7 +640,11 @@ srt_status pbrt_shape(const std::string& dir, const std::string& type, const std
             return set_error(SRT_ERR_PARSE, "No integer indices specified for trianglemesh");
         for (float x : floats(it->second)) m.idx.push_back((uint32_t)x);
         if ((it = p.find("normal N")) != p.end()) m.n = floats(it->second);
-        if (m.v.size() % 3 || m.idx.size() % 3 || (!m.n.empty() && m.n.size() != m.v.size()))
+        if ((it = p.find("point2 uv")) != p.end()) m.tc = floats(it->second);
+        if ((it = p.find("float3 tangent")) != p.end()) m.tg = floats(it->second);
+        const size_t nv = m.v.size() / 3;
+        if (m.v.size() % 3 || m.idx.size() % 3 || (!m.n.empty() && m.n.size() != m.v.size()) ||
+            (!m.tc.empty() && m.tc.size() != 2 * nv) || (!m.tg.empty() && m.tg.size() != m.v.size()))
             return set_error(SRT_ERR_PARSE, "trianglemesh arrays of the wrong size");
         for (uint32_t i : m.idx)
             if (i >= m.v.size() / 3) return set_error(SRT_ERR_PARSE, "trianglemesh index out of range");
@@ -675,6 +734,19 @@ srt_status import_pbrt(const std::string& path, srt_procedural& p, srt_camera_de
     State global, attr;
     bool in_attr = false;
     std::map<std::string, int> named;
+    // "texture reflectance": the colour texture of the material just made
+    // (Scene::find_texture; an unknown name leaves it untextured)
+    auto reflectance_texture = [&](const std::map<std::string, std::string>& prm) {
+        auto it = prm.find("texture reflectance");
+        if (it == prm.end()) return;
+        const std::string tn = unquote(it->second);
+        for (size_t k = 0; k < p.textures.size(); ++k)
+            if (p.textures[k].name == tn) {
+                p.mat_tex.resize(2 * p.mats.size(), -1);
+                p.mat_tex[2 * (p.mats.size() - 1)] = (int32_t)k;
+                return;
+            }
+    };
     for (;;) {
         std::string tok = R.word();
         if (tok.empty() || tok == "WorldEnd") break;
@@ -704,6 +776,7 @@ srt_status import_pbrt(const std::string& path, srt_procedural& p, srt_camera_de
             SRT_TRY(pbrt_material(unquote(it->second), prm, m));
             p.mats.push_back(m);
             named[name] = (int)p.mats.size() - 1;
+            reflectance_texture(prm);
         } else if (tok == "NamedMaterial") {
             std::string name;
             if (!R.quoted(name)) return bad("NamedMaterial without a name");
@@ -717,8 +790,19 @@ srt_status import_pbrt(const std::string& path, srt_procedural& p, srt_camera_de
             SRT_TRY(pbrt_material(type, prm, m));
             p.mats.push_back(m);
             st.material = (int)p.mats.size() - 1;
+            reflectance_texture(prm);
         } else if (tok == "Texture") {
-            return set_error(SRT_ERR_UNSUPPORTED, path + ": textures are not built in this library");
+            // Texture "name" "spectrum" "imagemap" "string filename" ... (pbrtparse.cu:412-419, 319-331):
+            // the image loaded with load_from_file(path, false, true)
+            std::string name, a, b2;
+            if (!R.quoted(name) || !R.quoted(a) || !R.quoted(b2) || !R.params(prm)) return bad("malformed Texture");
+            if (b2 != "imagemap") return set_error(SRT_ERR_UNSUPPORTED, path + ": texture class " + b2 + " (imagemap is read)");
+            auto it = prm.find("string filename");
+            if (it == prm.end()) return bad("No filename specified for texture");
+            HostTexture t;
+            t.name = name;
+            SRT_TRY(load_texture_image(dir + unquote(it->second), true, t));
+            p.textures.push_back(std::move(t));
         } else if (tok == "Shape") {
             std::string type;
             if (!R.quoted(type) || !R.params(prm)) return bad("malformed Shape");

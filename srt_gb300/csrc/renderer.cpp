@@ -295,6 +295,18 @@ srt_status Renderer::load_scene(const Json& config)
         width = 1920;
         height = 1080;
     }
+    const Json* env = config.find("environment");
+    if (env && env->string("type", "constant") == "uvmap") {
+        // a "uvmap" environment image beside the config (renderer.cu:155-161), loaded unflipped
+        const std::string rel = env->string("path", "");
+        if (rel.empty()) return set_error(SRT_ERR_ARG, "environment uvmap needs a path");
+        HostTexture t;
+        t.name = "environment";
+        SRT_TRY(load_texture_image(rel[0] == '/' ? rel : base_dir + rel, false, t));
+        scene->proc->textures.push_back(std::move(t));
+        scene->proc->env_map = (int32_t)scene->proc->textures.size();
+        scene->proc->sync_textures();
+    }
     srt_scene_desc desc;
     SRT_TRY(srt_procedural_desc(scene->proc, &desc));
     desc.camera.aspect = (float)width / (float)height;
@@ -315,10 +327,13 @@ srt_status Renderer::load_scene(const Json& config)
         std::memcpy(desc.camera.up, up, 12);
         desc.camera.fov = (float)cam->number("fov", 60.0);
     }
-    if (const Json* env = config.find("environment")) {
+    if (env) {
         std::string t = env->string("type", "constant");
-        if (t != "constant") return set_error(SRT_ERR_UNSUPPORTED, "Unknown environment type: " + t);
-        if (!vec3(env->find("color"), desc.env_color)) return set_error(SRT_ERR_ARG, "environment needs color");
+        if (t == "constant") {
+            if (!vec3(env->find("color"), desc.env_color)) return set_error(SRT_ERR_ARG, "environment needs color");
+        } else if (t != "uvmap") {
+            return set_error(SRT_ERR_ARG, "Unknown environment type: " + t);
+        }
     }
     SRT_TRY(srt_scene_create(&desc, &scene->handle));
     film = std::make_shared<Film>(width, height);

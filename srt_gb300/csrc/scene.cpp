@@ -63,10 +63,55 @@ srt_status validate(const srt_scene_desc* d)
     const int cam_type = d->camera.type & ~SRT_CAMERA_MIRROR_X;
     if (cam_type != SRT_CAMERA_PERSPECTIVE && cam_type != SRT_CAMERA_ORTHOGRAPHIC)
         return set_error(SRT_ERR_UNSUPPORTED, "only perspective and orthographic cameras are supported");
+    if (d->num_textures < 0 || (d->num_textures && !d->textures))
+        return set_error(SRT_ERR_ARG, "bad texture array in scene desc");
+    for (int i = 0; i < d->num_textures; ++i) {
+        const srt_texture& t = d->textures[i];
+        if (t.width <= 0 || t.height <= 0 || t.width > 65536 || t.height > 65536 || !t.pixels ||
+            (t.format != SRT_TEXTURE_RGBA8 && t.format != SRT_TEXTURE_RGBA32F))
+            return set_error(SRT_ERR_ARG, "texture " + std::to_string(i) + ": bad size, format or pixels");
+    }
+    if (d->env_map < 0 || d->env_map > d->num_textures) return set_error(SRT_ERR_ARG, "env_map out of range");
+    if (d->material_textures)
+        for (int i = 0; i < 2 * d->num_materials; ++i)
+            if (d->material_textures[i] < -1 || d->material_textures[i] >= d->num_textures)
+                return set_error(SRT_ERR_ARG, "material " + std::to_string(i / 2) + ": texture index out of range");
     return SRT_OK;
 }
 
-MaterialRec pack_material(const srt_material& m)
+// a CUDA array + texture object read as the reference reads its textures
+// (Scene::build_gscene_textures, scene.cu:92-139)
+srt_status make_texture(const srt_texture& t, cudaArray_t& arr, cudaTextureObject_t& obj)
+{
+    const bool u8 = t.format == SRT_TEXTURE_RGBA8;
+    cudaChannelFormatDesc cd = u8 ? cudaCreateChannelDesc<uchar4>() : cudaCreateChannelDesc<float4>();
+    const size_t pitch = (size_t)t.width * (u8 ? 4 : 16);
+    if (cudaMallocArray(&arr, &cd, t.width, t.height) != cudaSuccess) {
+        arr = nullptr;
+        cudaGetLastError();
+        return set_error(SRT_ERR_OOM, "texture array allocation failed");
+    }
+    SRT_CUDA_TRY(cudaMemcpy2DToArray(arr, 0, 0, t.pixels, pitch, pitch, t.height, cudaMemcpyHostToDevice));
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td{};
+    td.addressMode[0] = cudaAddressModeWrap;
+    td.addressMode[1] = cudaAddressModeWrap;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = u8 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    td.maxAnisotropy = 1;
+    td.maxMipmapLevelClamp = 99;
+    td.minMipmapLevelClamp = 0;
+    td.mipmapFilterMode = cudaFilterModePoint;
+    td.borderColor[0] = 1.0f;
+    td.sRGB = u8 ? 1 : 0;
+    SRT_CUDA_TRY(cudaCreateTextureObject(&obj, &rd, &td, nullptr));
+    return SRT_OK;
+}
+
+MaterialRec pack_material(const srt_material& m, bool textured)
 {
     Bxdf b{m.bxdf.type, m.bxdf.ior, m.bxdf.metallic, m.bxdf.subsurface, m.bxdf.roughness, m.bxdf.specular,
            m.bxdf.specularTint, m.bxdf.anisotropic, m.bxdf.sheen, m.bxdf.sheenTint, m.bxdf.clearcoat,
@@ -75,6 +120,7 @@ MaterialRec pack_material(const srt_material& m)
     if (bxdf_is_specular(b)) flags |= 1 << 8;
     if (bxdf_is_transmissive(b)) flags |= 1 << 9;
     if (m.intensity > 0.0f) flags |= 1 << 10;
+    if (textured) flags |= 1 << 11;
     MaterialRec r;
     float f;
     std::memcpy(&f, &flags, 4);
@@ -130,10 +176,12 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
     // per-mesh object-space area CDFs (TriangleMesh::compute_area, mesh.cpp:3-18)
     std::vector<float> mesh_area(d->num_meshes, 0.0f);
     std::vector<std::vector<float>> mesh_cdf(d->num_meshes);
-    bool any_normals = false;
+    bool any_normals = false, any_tc = false, any_tg = false;
     for (int i = 0; i < d->num_meshes; ++i) {
         const srt_mesh& m = d->meshes[i];
         if (m.normals) any_normals = true;
+        if (m.texcoords) any_tc = true;
+        if (m.tangents) any_tg = true;
         std::vector<float>& cdf = mesh_cdf[i];
         cdf.resize(m.num_faces);
         float area = 0.0f;
@@ -164,6 +212,7 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
     }
     std::vector<float> tri9((size_t)ntri * 9);
     std::vector<float> nrm9(any_normals ? (size_t)ntri * 9 : 0, 0.0f);
+    std::vector<float> tc6(any_tc ? (size_t)ntri * 6 : 0, 0.0f), tg9(any_tg ? (size_t)ntri * 9 : 0, 0.0f);
     std::vector<int32_t> prim_inst((size_t)ntri);
     for (int i = 0; i < d->num_instances; ++i) {
         Xf xf;
@@ -184,6 +233,16 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
                     nrm9[9 * g + 3 * c + 1] = n.y;
                     nrm9[9 * g + 3 * c + 2] = n.z;
                 }
+                if (m.texcoords) {
+                    tc6[6 * g + 2 * c] = m.texcoords[2 * vi];
+                    tc6[6 * g + 2 * c + 1] = m.texcoords[2 * vi + 1];
+                }
+                if (m.tangents) {
+                    float3 t = xf.vec(ld3(m.tangents + 3 * vi));
+                    tg9[9 * g + 3 * c] = t.x;
+                    tg9[9 * g + 3 * c + 1] = t.y;
+                    tg9[9 * g + 3 * c + 2] = t.z;
+                }
             }
         }
     }
@@ -193,12 +252,14 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
     std::vector<LightRec> lights;
     std::vector<float> light_cdf, face_cdf;
     std::vector<int32_t> light_faces;  // global prim per light face
+    std::vector<int> light_inst;       // instance of each light
     float wsum = 0.0f;
     for (int i = 0; i < d->num_instances; ++i) {
         const srt_mesh& m = d->meshes[d->instances[i].mesh_id];
         const srt_material& mat = d->materials[m.material_id];
         insts[i].material = m.material_id;
-        insts[i].has_normals = m.normals ? 1 : 0;
+        insts[i].attr = (m.normals ? kAttrNormals : 0) | (m.texcoords ? kAttrTexcoords : 0) |
+                        (m.tangents ? kAttrTangents : 0);
         insts[i].light_id = -1;
         insts[i].pad = 0;
         // an emitter without faces cannot be sampled and is never hit
@@ -208,8 +269,9 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
         L.face_begin = (int32_t)face_cdf.size();
         L.num_faces = m.num_faces;
         L.pdf = 0.0f;
-        L.pad = i;
+        L.textured = (d->material_textures && d->material_textures[2 * m.material_id] >= 0) ? 1 : 0;
         lights.push_back(L);
+        light_inst.push_back(i);
         const std::vector<float>& cdf = mesh_cdf[d->instances[i].mesh_id];
         for (int f = 0; f < m.num_faces; ++f) {
             face_cdf.push_back(cdf[f]);
@@ -219,8 +281,9 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
         light_cdf.push_back(wsum);
     }
     for (float& c : light_cdf) c /= wsum;
-    for (LightRec& L : lights) {
-        const srt_mesh& m = d->meshes[d->instances[L.pad].mesh_id];
+    for (size_t k = 0; k < lights.size(); ++k) {
+        LightRec& L = lights[k];
+        const srt_mesh& m = d->meshes[d->instances[light_inst[k]].mesh_id];
         L.pdf = d->materials[m.material_id].intensity / wsum;  // Light::sample_pdf (light.h:73-76)
     }
 
@@ -230,6 +293,8 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
     build_wide_bvh(ntri, tri9.data(), threads, bvh);
     std::vector<float4> tris((size_t)ntri * 3);
     std::vector<float4> norms(any_normals ? (size_t)ntri * 3 : 0);
+    std::vector<float2> tcs(any_tc ? (size_t)ntri * 3 : 0);
+    std::vector<float4> tgs(any_tg ? (size_t)ntri * 3 : 0);
     std::vector<int32_t> tri_prim((size_t)ntri);
     std::vector<int32_t> inv((size_t)ntri);
     for (int64_t k = 0; k < ntri; ++k) {
@@ -249,10 +314,23 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
             norms[3 * k + 1] = make_float4(n[3], n[4], n[5], 0.0f);
             norms[3 * k + 2] = make_float4(n[6], n[7], n[8], 0.0f);
         }
+        if (any_tc)
+            for (int c = 0; c < 3; ++c) tcs[3 * k + c] = make_float2(tc6[6 * (size_t)g + 2 * c], tc6[6 * (size_t)g + 2 * c + 1]);
+        if (any_tg)
+            for (int c = 0; c < 3; ++c)
+                tgs[3 * k + c] = make_float4(tg9[9 * (size_t)g + 3 * c], tg9[9 * (size_t)g + 3 * c + 1],
+                                             tg9[9 * (size_t)g + 3 * c + 2], 0.0f);
     }
     for (int32_t& g : light_faces) g = inv[g];
     std::vector<MaterialRec> mats(d->num_materials);
-    for (int i = 0; i < d->num_materials; ++i) mats[i] = pack_material(d->materials[i]);
+    auto mat_tex_of = [&](int mat, int k) { return d->material_textures ? d->material_textures[2 * mat + k] : -1; };
+    bool any_mat_tex = false, any_normal_tex = false;
+    for (int i = 0; i < d->num_materials; ++i) {
+        const bool tx = mat_tex_of(i, 0) >= 0 || mat_tex_of(i, 1) >= 0;
+        any_mat_tex |= tx;
+        any_normal_tex |= mat_tex_of(i, 1) >= 0;
+        mats[i] = pack_material(d->materials[i], tx);
+    }
 
     srt_status st = SRT_OK;
     auto up = [&](DeviceBuffer& b, const void* p, size_t bytes, const char* what) {
@@ -268,6 +346,34 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
     up(s->light_cdf, light_cdf.data(), light_cdf.size() * 4, "light cdf");
     up(s->face_cdf, face_cdf.data(), face_cdf.size() * 4, "face cdf");
     up(s->light_tri, light_faces.data(), light_faces.size() * 4, "light faces");
+    if (any_tc) up(s->texcoords, tcs.data(), tcs.size() * sizeof(float2), "texture coordinates");
+    if (any_tg) up(s->tangents, tgs.data(), tgs.size() * sizeof(float4), "tangents");
+    // textures, and per material the (colour, normal) texture objects
+    int64_t tex_bytes = 0;
+    for (int i = 0; i < d->num_textures && st == SRT_OK; ++i) {
+        cudaArray_t arr = nullptr;
+        cudaTextureObject_t obj = 0;
+        st = make_texture(d->textures[i], arr, obj);
+        if (arr) s->tex_arrays.push_back(arr);
+        if (obj) s->tex_objects.push_back(obj);
+        tex_bytes += (int64_t)d->textures[i].width * d->textures[i].height *
+                     (d->textures[i].format == SRT_TEXTURE_RGBA8 ? 4 : 16);
+    }
+    if (st == SRT_OK && any_mat_tex) {
+        std::vector<unsigned long long> mt(2 * (size_t)d->num_materials, 0ull);
+        for (int i = 0; i < 2 * d->num_materials; ++i)
+            if (d->material_textures[i] >= 0) mt[i] = s->tex_objects[d->material_textures[i]];
+        up(s->mat_tex, mt.data(), mt.size() * 8, "material textures");
+    }
+    if (st == SRT_OK && any_normal_tex) {
+        // instance rows, to turn normal-map normals (object space) into world space
+        std::vector<float4> xr(3 * (size_t)d->num_instances);
+        for (int i = 0; i < d->num_instances; ++i) {
+            const float* t = d->instances[i].transform;
+            for (int r = 0; r < 3; ++r) xr[3 * i + r] = make_float4(t[4 * r], t[4 * r + 1], t[4 * r + 2], t[4 * r + 3]);
+        }
+        up(s->inst_xf, xr.data(), xr.size() * sizeof(float4), "instance transforms");
+    }
     if (st != SRT_OK) {
         delete s;
         return st;
@@ -287,6 +393,11 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
     v.num_tris = (int32_t)ntri;
     v.env = make_float3(d->env_color[0], d->env_color[1], d->env_color[2]);
     v.weight_sum = wsum;
+    v.texcoords = any_tc ? s->texcoords.as<float2>() : nullptr;
+    v.tangents = any_tg ? s->tangents.as<float4>() : nullptr;
+    v.mat_tex = any_mat_tex ? s->mat_tex.as<unsigned long long>() : nullptr;
+    v.inst_xf = any_normal_tex ? s->inst_xf.as<float4>() : nullptr;
+    v.env_tex = d->env_map > 0 ? s->tex_objects[d->env_map - 1] : 0ull;
     s->camera_desc = d->camera;
     s->camera = make_camera(d->camera);
 
@@ -297,7 +408,8 @@ extern "C" srt_status srt_scene_create(const srt_scene_desc* d, srt_scene** out)
     I.num_lights = (int64_t)lights.size();
     I.device_bytes = (int64_t)(s->nodes.bytes() + s->tris.bytes() + s->tri_prim.bytes() + s->normals.bytes() +
                                s->insts.bytes() + s->mats.bytes() + s->lights.bytes() + s->light_cdf.bytes() +
-                               s->face_cdf.bytes() + s->light_tri.bytes());
+                               s->face_cdf.bytes() + s->light_tri.bytes() + s->texcoords.bytes() +
+                               s->tangents.bytes() + s->mat_tex.bytes() + s->inst_xf.bytes() + tex_bytes);
     I.bvh_depth = bvh.depth;
     I.build_ms = (float)std::chrono::duration<double, std::milli>(t1 - t0).count();
     I.light_weight_sum = wsum;
@@ -336,6 +448,12 @@ extern "C" srt_status srt_scene_prim_to_instance(const srt_scene* s, int64_t pri
     *instance = i;
     *face = (int32_t)(prim - s->inst_prim_base[i]);
     return SRT_OK;
+}
+
+srt_scene::~srt_scene()
+{
+    for (cudaTextureObject_t o : tex_objects) cudaDestroyTextureObject(o);
+    for (cudaArray_t a : tex_arrays) cudaFreeArray(a);
 }
 
 extern "C" void srt_scene_destroy(srt_scene* s) { delete s; }

@@ -10,6 +10,10 @@
 
 struct srt_scene {
     srt::DeviceBuffer nodes, tris, tri_prim, normals, insts, mats, lights, light_cdf, face_cdf, light_tri;
+    srt::DeviceBuffer texcoords, tangents, mat_tex, inst_xf;
+    std::vector<cudaArray_t> tex_arrays;              // Scene::build_gscene_textures (scene.cu:92-139)
+    std::vector<cudaTextureObject_t> tex_objects;
+    ~srt_scene();
     srt::SceneView view{};
     srt::CameraRec camera{};
     srt_camera_desc camera_desc{};

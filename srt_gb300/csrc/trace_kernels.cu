@@ -53,6 +53,17 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace_s
     if (overflow) atomicAdd(overflow_flag, 1);
 }
 
+// tex2D of one of the scene's textures at n normalised coordinates
+__global__ void __launch_bounds__(256) k_texture_lookup(cudaTextureObject_t tex, const float2* __restrict__ uv,
+                                                             int64_t n, float4* __restrict__ out)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float2 c = __ldg(uv + i);
+        out[i] = tex2D<float4>(tex, c.x, c.y);
+    }
+}
+
 struct QueryScratch {
     unsigned long long counter;
     int overflow;
@@ -104,4 +115,22 @@ extern "C" srt_status srt_trace_shadow(const srt_scene* s, const float* rays, in
                                        void* stream)
 {
     return run_query(s, rays, n, visible, true, stream);
+}
+
+extern "C" srt_status srt_scene_texture_lookup(const srt_scene* s, int32_t texture, const float* uv, int64_t n,
+                                               float* out, void* stream)
+{
+    clear_error();
+    if (!s || (n > 0 && (!uv || !out))) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (n < 0 || texture < 0 || texture >= (int32_t)s->tex_objects.size())
+        return set_error(SRT_ERR_ARG, "bad texture index or count");
+    if (reinterpret_cast<uintptr_t>(uv) % 8 || reinterpret_cast<uintptr_t>(out) % 16)
+        return set_error(SRT_ERR_ARG, "uv must be 8-byte and out 16-byte aligned");
+    if (n == 0) return SRT_OK;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 8);
+    k_texture_lookup<<<blocks, 256, 0, as_stream(stream)>>>(s->tex_objects[texture],
+                                                                 reinterpret_cast<const float2*>(uv), n,
+                                                                 reinterpret_cast<float4*>(out));
+    SRT_CUDA_TRY(cudaGetLastError());
+    return SRT_OK;
 }

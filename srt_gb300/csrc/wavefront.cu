@@ -162,6 +162,65 @@ struct LightSample {
     float pdf;
 };
 
+// texture coordinate of a hit (hit_info.h:36-38): the mesh's interpolated
+// texcoords, or the barycentric (u, v) when it has none
+__device__ __forceinline__ float2 hit_texcoord(const SceneView& S, int32_t attr, size_t tri, float u, float v)
+{
+    if (!(attr & kAttrTexcoords)) return make_float2(u, v);
+    const float2* t = S.texcoords + 3 * tri;
+    const float2 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
+    const float w = 1.0f - u - v;
+    return make_float2(a.x * w + b.x * u + c.x * v, a.y * w + b.y * u + c.y * v);
+}
+
+// EnvironmentLight::emission (light.h:27-41) of a "uvmap" environment: the
+// texture looked up by direction (world y up, math-space z up).
+__device__ __forceinline__ float3 env_map_radiance(unsigned long long tex, float3 d)
+{
+    const float3 m = make_float3(-d.x, d.z, d.y);
+    const float phi = atan2f(m.y, m.x), theta = acosf(m.z);  // cartesian_to_spherical_uv (basic.h:41-46)
+    const float u = phi * 0.5f * (float)M_1_PI + 0.5f, v = theta * (float)M_1_PI;
+    return f3(tex2D<float4>(tex, u, v));
+}
+
+__device__ __forceinline__ float3 env_radiance(const SceneView& S, float3 d)
+{
+    return S.env_tex ? env_map_radiance(S.env_tex, d) : S.env;
+}
+
+// GMaterial::surface_color / emission / shading_normal (gmaterial.h:35-56)
+// at a hit's texture coordinate: the colour texture replaces the base
+// colour (and the emission colour), the normal map's object-space normal,
+// turned by the instance (apply_onb), replaces the shading normal.
+__device__ __forceinline__ void apply_material_textures(const SceneView& S, int32_t attr, int32_t material, int32_t inst,
+                                                     int tri, float u, float v, float3& base_color, float4& em,
+                                                     float3& sn)
+{
+    const float2 tc = hit_texcoord(S, attr, (size_t)tri, u, v);
+    const unsigned long long ctex = __ldg(S.mat_tex + 2 * material);
+    const unsigned long long ntex = __ldg(S.mat_tex + 2 * material + 1);
+    if (ctex) {
+        base_color = f3(tex2D<float4>(ctex, tc.x, tc.y));
+        em = make_float4(base_color.x * em.w, base_color.y * em.w, base_color.z * em.w, em.w);
+    }
+    if (ntex) {
+        const float3 no = normalize(f3(tex2D<float4>(ntex, tc.x, tc.y)));
+        const float4* xr = S.inst_xf + 3 * (size_t)inst;
+        const float4 r0 = __ldg(xr), r1 = __ldg(xr + 1), r2 = __ldg(xr + 2);
+        sn = make_float3(r0.x * no.x + r0.y * no.y + r0.z * no.z, r1.x * no.x + r1.y * no.y + r1.z * no.z,
+                         r2.x * no.x + r2.y * no.y + r2.z * no.z);
+    }
+}
+
+// GMaterial::emission(texcoord) (gmaterial.h:35-41) of a light sample: the
+// colour texture times the intensity
+__device__ __forceinline__ float3 light_texture_emission(const SceneView& S, int32_t attr, int32_t material, int32_t t,
+                                                      float bu, float bv, float intensity)
+{
+    const float2 tc = hit_texcoord(S, attr, (size_t)t, bu, bv);
+    return f3(tex2D<float4>(__ldg(S.mat_tex + 2 * material), tc.x, tc.y)) * intensity;
+}
+
 // Light::sample + GInstance::sample (light.h:61-76, gmesh.h:45-85).
 __device__ __forceinline__ LightSample sample_light(const SceneView& S, float u1, float u2, bool fixed)
 {
@@ -182,7 +241,7 @@ __device__ __forceinline__ LightSample sample_light(const SceneView& S, float u1
     float3 n = normalize(cross(v1 - v0, v2 - v0));
     int32_t inst = __float_as_int(a.w);
     InstanceRec ir = S.insts[inst];
-    if (ir.has_normals) {
+    if (ir.attr & kAttrNormals) {
         const float4* np = S.normals + 3 * (size_t)t;
         float3 sn = f3(__ldg(np)) * (1.0f - bu - bv) + f3(__ldg(np + 1)) * bu + f3(__ldg(np + 2)) * bv;
         if (dot(n, sn) < 0.0f) n = -n;
@@ -190,6 +249,7 @@ __device__ __forceinline__ LightSample sample_light(const SceneView& S, float u1
     ls.normal = n;
     float4 em = __ldg(&S.mats[ir.material].m[4]);
     ls.emission = f3(em);
+    if (L.textured) ls.emission = light_texture_emission(S, ir.attr, ir.material, t, bu, bv, em.w);
     ls.pdf = L.pdf;
     return ls;
 }
@@ -208,6 +268,7 @@ __device__ __forceinline__ Bxdf unpack_bxdf(const MaterialRec* __restrict__ m, i
 constexpr int kMatSpecular = 1 << 8;
 constexpr int kMatTransmissive = 1 << 9;
 constexpr int kMatEmissive = 1 << 10;
+constexpr int kMatTextured = 1 << 11;
 
 __device__ __forceinline__ uint32_t pack_flags(int depth, bool specular, int job)
 {
@@ -388,7 +449,7 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
             terminate = true;
             if (tri < 0) {
                 // miss: environment light (path_tracer.cu:81-85)
-                L_add = beta * S.env;
+                L_add = beta * env_radiance(S, rd);
             } else {
                 const float4* tp = S.tris + 3 * (size_t)tri;
                 float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
@@ -403,10 +464,12 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                 float3 pos = v0 * (1.0f - u - v) + v1 * u + v2 * v;
                 float3 ng = normalize(cross(v1 - v0, v2 - v0));
                 float3 sn = ng;
-                if (ir.has_normals) {
+                if (ir.attr & kAttrNormals) {
                     const float4* np = S.normals + 3 * (size_t)tri;
                     sn = normalize(f3(__ldg(np)) * (1.0f - u - v) + f3(__ldg(np + 1)) * u + f3(__ldg(np + 2)) * v);
                 }
+                if (mflags & kMatTextured)
+                    apply_material_textures(S, ir.attr, ir.material, __float_as_int(a.w), tri, u, v, base_color, em, sn);
                 if (dot(ng, sn) < 0.0f) ng = -ng;
                 if (mflags & kMatEmissive) {
                     // emitter hit with MIS (path_tracer.cu:88-106)
@@ -456,6 +519,11 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                     Rng rng;
                     rng.load(ra, rb);
                     float3 tan = (fabsf(sn.x) > fabsf(sn.y)) ? make_float3(0.f, 1.f, 0.f) : make_float3(1.f, 0.f, 0.f);
+                    if (ir.attr & kAttrTangents) {
+                        // the mesh's interpolated tangent (hit_info.h:48-50)
+                        const float4* gp = S.tangents + 3 * (size_t)tri;
+                        tan = f3(__ldg(gp)) * (1.0f - u - v) + f3(__ldg(gp + 1)) * u + f3(__ldg(gp + 2)) * v;
+                    }
                     Frame fr = Frame::from_normal_tangent(sn, tan);
                     const bool transmissive = (mflags & kMatTransmissive) != 0;
                     // NEE with MIS (path_tracer.cu:113-142)

@@ -221,8 +221,10 @@ PBRT_HEAD = 'Film "rgb" "integer xresolution" [ 8 ] "integer yresolution" [ 8 ]\
 
 
 @pytest.mark.parametrize("name,text,status", [
-    ("tex.pbrt", PBRT_HEAD + 'WorldBegin\nTexture "checks" "spectrum" "imagemap" "string filename" "a.png"\n', 9),
-    ("texparam.pbrt", PBRT_HEAD + 'WorldBegin\nMaterial "diffuse" "texture reflectance" "checks"\n' + TRI, 9),
+    ("tex.pbrt", PBRT_HEAD + 'WorldBegin\nTexture "checks" "spectrum" "imagemap" "string filename" "a.png"\n', 1),
+    ("texclass.pbrt", PBRT_HEAD + 'WorldBegin\nTexture "c" "spectrum" "checkerboard" "float uscale" 4\n', 9),
+    ("uvsize.pbrt", PBRT_HEAD + 'WorldBegin\nMaterial "diffuse"\n'
+     'Shape "trianglemesh" "integer indices" [ 0 1 2 ] "point3 P" [ 0 0 0 1 0 0 0 1 0 ] "point2 uv" [ 0 0 1 ]\n', 8),
     ("token.pbrt", PBRT_HEAD + 'LookAt 0 0 0 0 0 1 0 1 0\nWorldBegin\n', 9),
     ("world.pbrt", PBRT_HEAD + 'WorldBegin\nMaterial "diffuse"\nShape "sphere" "float radius" 1\n', 9),
     ("mat.pbrt", PBRT_HEAD + 'WorldBegin\nMaterial "measured"\n', 9),
@@ -259,3 +261,63 @@ def test_renderer_needs_a_camera_for_obj(tmp_path):
     with pytest.raises(S.SrtError) as e:  # relative to the working directory, not the config's
         S.Renderer({"render": {"resolution": [8, 8]}, "passes": [], "scene": {"model": "t.obj"}})
     assert e.value.status == 1
+
+
+def _png(path, px):
+    """An RGBA8 PNG through the library's writer (values are 8-bit already)."""
+    h, w = px.shape[:2]
+    S.image_write(path, (px.astype(np.float32) / 255.0).reshape(-1, 4), w, h, flip=False)
+
+
+def test_pbrt_textures_uv_and_tangents(tmp_path):
+    rng = np.random.default_rng(5)
+    img = rng.integers(0, 256, size=(3, 4, 4), dtype=np.uint8)
+    (tmp_path / "tex").mkdir()
+    _png(tmp_path / "tex" / "wood.png", img)
+    hdr = np.abs(rng.random((2, 5, 4), dtype=np.float32))
+    S.image_write(tmp_path / "tex" / "sky.pfm", hdr.reshape(-1, 4), 5, 2, flip=False)
+    _write_ply_binary(tmp_path / "uv.ply", FLOOR_V, None, FLOOR_F, extra_uv=True)
+    (tmp_path / "t.pbrt").write_text(PBRT_HEAD + """WorldBegin
+Texture "wood" "spectrum" "imagemap" "string filename" [ "tex/wood.png" ]
+Texture "sky" "spectrum" "imagemap" "string filename" "tex/sky.pfm"
+Material "diffuse" "texture reflectance" "wood"
+Shape "trianglemesh" "integer indices" [ 0 1 2 ] "point3 P" [ 0 0 0 1 0 0 0 1 0 ]
+    "point2 uv" [ 0 0 1 0 0 1 ] "float3 tangent" [ 1 0 0 1 0 0 1 0 0 ]
+MakeNamedMaterial "m" "string type" "conductor" "texture reflectance" "sky"
+NamedMaterial "m"
+Shape "plymesh" "string filename" "uv.ply"
+Material "diffuse" "texture reflectance" "nosuch"
+""" + TRI)
+    s = S.import_scene(str(tmp_path / "t.pbrt"))
+    assert len(s.textures) == 2
+    # Image::load_from_file(path, false, true): rows flipped, columns kept
+    assert s.textures[0].dtype == np.uint8 and np.array_equal(s.textures[0], img[::-1])
+    assert s.textures[1].dtype == np.float32 and np.array_equal(s.textures[1][..., :3], hdr[..., :3])
+    assert s.material_textures == [(0, -1), (1, -1), (-1, -1)]
+    np.testing.assert_array_equal(s.meshes[0]["texcoords"], [[0, 0], [1, 0], [0, 1]])
+    np.testing.assert_array_equal(s.meshes[0]["tangents"], np.tile([1, 0, 0], (3, 1)))
+    np.testing.assert_array_equal(s.meshes[1]["texcoords"], np.tile([0.25, 0.75], (4, 1)))
+    assert s.meshes[2]["texcoords"] is None and s.env_map is None
+
+
+def test_obj_textures_and_flipped_uvs(tmp_path):
+    rng = np.random.default_rng(6)
+    img = rng.integers(0, 256, size=(2, 3, 4), dtype=np.uint8)
+    nrm = rng.integers(0, 256, size=(4, 2, 4), dtype=np.uint8)
+    (tmp_path / "maps").mkdir()
+    _png(tmp_path / "maps" / "albedo.png", img)
+    _png(tmp_path / "maps" / "normal.png", nrm)
+    (tmp_path / "m.mtl").write_text("newmtl a\nKd 1 1 1\nmap_Kd -s 1 1 1 maps\\albedo.png\nnorm maps/normal.png\n"
+                                    "newmtl b\nKd 0.5 0.5 0.5\nmap_Kd maps/albedo.png\nnewmtl c\nKd 0.2 0.2 0.2\n")
+    (tmp_path / "m.obj").write_text("mtllib m.mtl\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\n"
+                                    "vt 0 0\nvt 1 0\nvt 1 1\nvt 0.25 0.75\n"
+                                    "usemtl a\nf 1/1 2/2 3/3 4/4\nusemtl b\nf 1/4 2/4 3/4\nusemtl c\nf 1 2 3\n")
+    s = S.import_scene(str(tmp_path / "m.obj"))
+    # textures loaded once each, unflipped (load_from_file(filename))
+    assert len(s.textures) == 2
+    assert np.array_equal(s.textures[0], img) and np.array_equal(s.textures[1], nrm)
+    assert s.material_textures == [(0, 1), (0, -1), (-1, -1)]
+    # aiProcess_FlipUVs: v -> 1 - v
+    np.testing.assert_allclose(s.meshes[0]["texcoords"], [[0, 1], [1, 1], [1, 0], [0.25, 0.25]])
+    np.testing.assert_allclose(s.meshes[1]["texcoords"], np.tile([0.25, 0.25], (3, 1)))
+    assert s.meshes[2]["texcoords"] is None
