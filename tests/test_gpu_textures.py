@@ -160,7 +160,7 @@ def test_environment_map_vs_oracle(cuda):
     sa.textures = [sky.astype(np.float32)]
     sa.env_map = 0
     sa.camera.fov = 100.0
-    p = pt_params(4, 4, 3, 1, 1, 5)
+    p = pt_params(4, 4, 3, 0, 0, 5)  # no area light: no next-event estimation
     film, _ = _render(cuda, sa, w, h, p)
     of, _, _, _ = O.OracleScene(sa.desc()).render(w, h, p)
     assert np.abs(film[:, :3] - of[:, :3]).max() <= 0.01 * np.abs(sky).max() + 1e-6
