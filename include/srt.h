@@ -265,6 +265,17 @@ srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t height, srt_pt
  * Stream-ordered; returns after the frame has been enqueued and its
  * completion polled (the reference synchronises at the same point). */
 srt_status srt_pt_render(srt_pt* pt, float* film, const srt_pt_params* params, void* stream);
+/* LightTracer pass (src/passes/integrator/light_tracer.cu:13-33,
+ * src/shader/integrator/light_tracer.cu:57-175): clears `film`
+ * (float4[w*h], device) to (0, 0, 0, 1), then traces samples_per_pixel
+ * light paths per launch index w*h from that index's curand stream
+ * (seed + idx), connecting every non-specular vertex to the pinhole camera
+ * and adding the contribution to the pixel it lands on.  Uses
+ * samples_per_pixel, max_depth, rr_depth, seed and flags of `params`
+ * (curand streams only).  Perspective cameras only (Camera::get_xy).
+ * stats may be NULL. */
+srt_status srt_lt_render(const srt_scene* scene, int32_t width, int32_t height, float* film,
+                         const srt_pt_params* params, srt_pt_stats* stats, void* stream);
 srt_status srt_pt_get_stats(const srt_pt* pt, srt_pt_stats* stats);
 /* Profiling switch (PROFILE() scopes of src/utils/profiler.h:219 applied per
  * kernel).  enable = 1: the iteration graph carries event records between
@@ -505,7 +516,7 @@ srt_status srt_procedural_resolution(const srt_procedural* p, int32_t* width, in
 /* ------------------------------------------------------------------ */
 
 /* JSON config with "render", "passes", "scene" (example/example.json).
- * Passes registered: PathTracer, Wavefront, Accumulate, ToneMapping.
+ * Passes registered: PathTracer, Wavefront, LightTracer, Accumulate, ToneMapping, Measure.
  * scene.model: "procedural:cornell" | "procedural:spheres[:n[:subdiv[:seed]]]"
  * | a scene file (.pbrt, .obj, .ply). */
 typedef struct srt_renderer srt_renderer;

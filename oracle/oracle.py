@@ -59,6 +59,7 @@ def lib():
             "oracle_light_sample": (None, [_vp, _i64, _vp, C.c_int, _vp]),
             "oracle_hitinfo": (None, [_vp, _i64, _vp, _vp, _vp]),
             "oracle_texture_lookup": (None, [_vp, C.c_int, _i64, _vp, _vp]),
+            "oracle_light_trace": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp, _vp]),
             "oracle_render": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int,
                                         C.c_int, _vp, _vp, _vp, _vp]),
             "oracle_accumulate": (None, [_vp, _vp, _i64, C.c_int]),
@@ -187,6 +188,15 @@ class OracleScene:
         out = np.zeros((len(uv), 4), np.float32)
         lib().oracle_texture_lookup(self.h, int(texture), len(uv), _np(uv), _np(out))
         return out
+
+    def light_trace(self, w, h, params, threads=8):
+        film = np.zeros((w * h, 3), np.float64)
+        cnt = np.zeros(2, np.int64)
+        rc = lib().oracle_light_trace(self.h, w, h, C.cast(C.pointer(params), _vp), int(self.has_bvh), threads,
+                                      _np(film), _np(cnt))
+        if rc != 0:
+            raise ValueError(f"oracle_light_trace failed ({rc})")
+        return film, cnt
 
     def render(self, w, h, params, crop=None, threads=8):
         x0, y0, cw, ch = crop if crop else (0, 0, w, h)

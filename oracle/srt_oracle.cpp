@@ -1484,6 +1484,130 @@ int oracle_render(const oracle_scene* s, int w, int h, int x0, int y0, int cw, i
     return 0;
 }
 
+// LightTracer raygen (src/shader/integrator/light_tracer.cu:57-175) for
+// launch index `idx`; splats go to `film` (double RGB per pixel).
+void light_trace_index(const oracle_scene& s, int w, int h, int64_t idx, const srt_pt_params& p, bool use_bvh,
+                       double* film, int64_t* cnt)
+{
+    const bool fixed = (p.flags & SRT_PT_FIXED_CDF_REMAP) != 0;
+    const Camera& k = s.cam;
+    const float aspect = (float)w / (float)h;
+    Rng rng;
+    rng.mode = SRT_RNG_CURAND;
+    rng.init_curand(p.seed, (int)idx);
+    // Camera::get_xy (camera.h:142-148)
+    auto get_xy = [&](F3 dir, float& x, float& y) {
+        F3 m = dir * -1.0f;
+        F3 l(dot(m, k.x), dot(m, k.y), dot(m, k.z));
+        float px = l.x / l.z, py = l.y / l.z;
+        x = px / k.nw + 0.5f;
+        y = py / k.nh + 0.5f;
+    };
+    auto splat = [&](float x, float y, F3 v) {
+        int pix = (int)(x * (float)w) + (int)(y * (float)h) * w;
+        film[3 * pix] += v.x;
+        film[3 * pix + 1] += v.y;
+        film[3 * pix + 2] += v.z;
+    };
+    for (int i = 0; i < p.samples_per_pixel; ++i) {
+        float l1 = rng.next();
+        float l2 = rng.next();
+        LSample ls = light_sample(s, l1, l2, fixed);
+        float s1 = rng.next();
+        float s2 = rng.next();
+        float sz = 1.0f - 2.0f * s1;  // uniform_sample_sphere (basic.h:83-89)
+        float sr = std::sqrt(1.0f - sz * sz);
+        float phi = 2.0f * (float)M_PI * s2;
+        F3 wi = normalize(ls.normal + F3(sr * std::cos(phi), sr * std::sin(phi), sz));
+        F3 ro = ls.pos, rd = wi;
+        float cos_theta = dot(wi, ls.normal);
+        float pw = cos_theta * (float)M_1_PI;
+        F3 beta = ls.emission * cos_theta / ls.pdf;
+        bool specular = true;
+        for (int depth = 0; depth < p.max_depth; ++depth) {
+            cnt[0]++;
+            Hit hit = trace(s, ro, rd, 1e-3f, 1e16f, false, use_bvh);
+            HitInfo hi;
+            if (hit.prim >= 0) hi = hit_info(s, hit.prim, hit.u, hit.v);
+            if (specular) {
+                F3 to_cam = k.pos - ro;
+                float t = length(to_cam);
+                to_cam = to_cam / t;
+                if ((hit.prim < 0 || t < length(hi.pos - ro)) && dot(to_cam, rd) > 1.0f - 1e-6f) {
+                    float x, y;
+                    get_xy(rd, x, y);
+                    if (x >= 0.0f && x < 1.0f && y >= 0.0f && y < 1.0f) splat(x, y, beta / pw / (float)p.samples_per_pixel);
+                }
+            }
+            if (hit.prim < 0) break;
+            const srt_material& mat = s.mats[hi.mat];
+            if (mat.intensity > 0.0f) break;
+            Bx<float> bx = bx_of(mat.bxdf);
+            float cos_i = dot(rd * -1.0f, hi.normal);
+            if (cos_i < 0.0f) hi.normal = -hi.normal;
+            if (!is_specular(mat.bxdf)) {
+                F3 sd = normalize(k.pos - hi.pos);
+                float x, y;
+                get_xy(sd, x, y);
+                if (x >= 0.0f && x < 1.0f && y >= 0.0f && y < 1.0f) {
+                    float t = length(k.pos - hi.pos);
+                    cnt[1]++;
+                    Hit sh = trace(s, hi.pos, sd, 1e-3f, t - 1e-3f, true, use_bvh);
+                    if (sh.prim < 0) {
+                        F3 fv = mat_eval(bx, hi.onb, rd * -1.0f, sd, hi.color);
+                        F3 L = beta * aspect * fv * dot(sd, hi.normal) / t / t / pw;
+                        splat(x, y, L / (float)p.samples_per_pixel);
+                    }
+                }
+            }
+            float u1 = rng.next();
+            float u2 = rng.next();
+            BSample<float> ms = mat_sample(bx, hi.onb, rd * -1.0f, u1, u2, hi.color);
+            if (ms.pdf <= 1e-5f) break;
+            beta = beta * mat_eval(bx, hi.onb, rd * -1.0f, ms.wi, hi.color) * std::fabs(dot(ms.wi, hi.normal)) / pw;
+            pw = ms.pdf;
+            specular = is_specular(mat.bxdf);
+            ro = hi.pos;
+            rd = ms.wi;
+            if (depth >= p.rr_depth) {
+                float q = std::min(std::max(beta.x, std::max(beta.y, beta.z)), 0.95f);
+                if (rng.next() > q) break;
+                beta = beta / q;
+            }
+        }
+    }
+}
+
+// srt_lt_render's restatement: film (w*h RGB, double) is the sum of all
+// splats; counters[0] closest rays, [1] camera connections traced.
+int oracle_light_trace(const oracle_scene* s, int w, int h, const srt_pt_params* p, int use_bvh, int threads,
+                       double* film, int64_t* counters)
+{
+    if (!s || !p || w <= 0 || h <= 0) return 1;
+    if (s->light_inst.empty()) return 2;
+    const int64_t n = (int64_t)w * h;
+    const int nt = std::max(1, threads);
+    std::vector<std::vector<double>> part(nt, std::vector<double>(3 * (size_t)n, 0.0));
+    std::vector<int64_t> cnt(2 * (size_t)nt, 0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&, t]() {
+            for (int64_t idx = t; idx < n; idx += nt)
+                light_trace_index(*s, w, h, idx, *p, use_bvh != 0, part[t].data(), &cnt[2 * t]);
+        });
+    for (auto& th : pool) th.join();
+    for (int64_t i = 0; i < 3 * n; ++i) {
+        film[i] = 0.0;
+        for (int t = 0; t < nt; ++t) film[i] += part[t][i];
+    }
+    counters[0] = counters[1] = 0;
+    for (int t = 0; t < nt; ++t) {
+        counters[0] += cnt[2 * t];
+        counters[1] += cnt[2 * t + 1];
+    }
+    return 0;
+}
+
 // Accumulate::render (src/passes/postprocess/accumulate.cu:10-29)
 void oracle_accumulate(float* film, float* acc, int64_t n, int frame_count)
 {

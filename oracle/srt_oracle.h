@@ -71,6 +71,12 @@ void oracle_hitinfo(const oracle_scene* s, int64_t n, const int32_t* prim, const
  * scene's texture `texture` at n coordinates (uv n x 2 -> out n x 4). */
 void oracle_texture_lookup(const oracle_scene* s, int texture, int64_t n, const float* uv, float* out);
 
+/* LightTracer (src/shader/integrator/light_tracer.cu:57-175): film gets
+ * the sum of all splats (w*h x 3 doubles); counters[0] closest rays,
+ * counters[1] camera connections traced.  Returns 2 without lights. */
+int oracle_light_trace(const oracle_scene* s, int w, int h, const srt_pt_params* p, int use_bvh, int threads,
+                       double* film, int64_t* counters);
+
 /* Light::sample(u) -> pos, normal, emission, pdf (n x 10 floats). */
 void oracle_light_sample(const oracle_scene* s, int64_t n, const float* u2, int fixed_remap,
                          float* out);

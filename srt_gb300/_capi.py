@@ -145,6 +145,7 @@ _PROTOS = [
     ("srt_scene_texture_lookup", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("srt_pt_create", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     ("srt_pt_render", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PtParams), C.c_void_p]),
+    ("srt_lt_render", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(PtParams), C.POINTER(PtStats), C.c_void_p]),
     ("srt_pt_get_stats", C.c_int, [C.c_void_p, C.POINTER(PtStats)]),
     ("srt_pt_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
     ("srt_pt_destroy", None, [C.c_void_p]),

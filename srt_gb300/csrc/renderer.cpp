@@ -125,6 +125,35 @@ public:
 };
 RenderPassFactory::Register<Wavefront> Wavefront::reg("Wavefront");
 
+// ---- LightTracer (src/passes/integrator/light_tracer.{h,cu}) -----------------
+
+class LightTracer : public RenderPass {
+public:
+    explicit LightTracer(const Json& j)
+    {
+        if (j.is_null()) return;
+        samples_per_pixel = (int)j.number("samples_per_pixel", 1);
+        max_depth = (int)j.number("max_depth", 16);
+        rr_depth = (int)j.number("rr_depth", 4);
+    }
+    srt_status render(std::shared_ptr<Film> film) override
+    {
+        if (!enable) return SRT_OK;
+        srt_pt_params p{};
+        p.samples_per_pixel = samples_per_pixel;
+        p.max_depth = max_depth;
+        p.rr_depth = rr_depth;
+        p.seed = host_random_int(0, INT32_MAX);
+        p.rng_mode = SRT_RNG_CURAND;
+        return srt_lt_render(scene->handle, width, height, film->get_pixels(), &p, nullptr, nullptr);
+    }
+
+private:
+    int samples_per_pixel = 1, max_depth = 16, rr_depth = 4;
+    static RenderPassFactory::Register<LightTracer> reg;
+};
+RenderPassFactory::Register<LightTracer> LightTracer::reg("LightTracer");
+
 // ---- Accumulate (src/passes/postprocess/accumulate.{h,cu}) -----------------
 
 class Accumulate : public RenderPass {
