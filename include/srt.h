@@ -276,6 +276,44 @@ srt_status srt_pt_render(srt_pt* pt, float* film, const srt_pt_params* params, v
  * stats may be NULL. */
 srt_status srt_lt_render(const srt_scene* scene, int32_t width, int32_t height, float* film,
                          const srt_pt_params* params, srt_pt_stats* stats, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* NeuralRadiosity pass (src/passes/npr/neural_radiosity.{h,cu},       */
+/* src/shader/npr/nr_lhs.cu, nr_rhs.cu)                                */
+/* ------------------------------------------------------------------ */
+
+enum { SRT_NR_LHS = 0, SRT_NR_RHS = 1 };
+/* The pass's network in the reference's configuration: hash grid on the
+ * position (8 levels x 8 features, 2^19 entries, base resolution 16,
+ * scale 2, smoothstep), degree-3 spherical harmonics of direction and
+ * normal, the colour, padded with ones to 96; 96 -> 256 x 4 (ReLU) -> 16
+ * (3 used), no biases, BF16 with FP32 accumulation.  Parameters are one
+ * float vector: grid features level by level (entry-major, 8 per entry),
+ * then the layers' W[out][in].  Initialised from `seed` as tiny-cuda-nn
+ * initialises (grid U(-1e-4, 1e-4), layers U(+-sqrt(6/(in+out)))). */
+typedef struct srt_nr srt_nr;
+int64_t srt_nr_num_params(void);
+srt_status srt_nr_create(uint64_t seed, srt_nr** out);
+srt_status srt_nr_get_params(const srt_nr* nr, float* host_params);
+srt_status srt_nr_set_params(srt_nr* nr, const float* host_params);
+/* save_model / load_model in this library's own file format (a tiny-cuda-nn
+ * serialisation is not read). */
+srt_status srt_nr_save(const srt_nr* nr, const char* path);
+srt_status srt_nr_load(srt_nr* nr, const char* path);
+/* inputs: n x 12 floats (device), out: n x 16 floats (device; 3 used). */
+srt_status srt_nr_infer(srt_nr* nr, const float* inputs, int64_t n, float* out, void* stream);
+void srt_nr_destroy(srt_nr* nr);
+/* The LHS / RHS raygen of one sample with frame seed `seed` (curand stream
+ * seed + pixel): mask (w*h bytes: 1 = the pixel needs no network), base
+ * (w*h x 3), weight (w*h x 3, RHS only; may be NULL for LHS) and the
+ * network inputs (w*h x 12; zero where mask = 1), all device memory. */
+srt_status srt_nr_trace(const srt_scene* scene, int32_t width, int32_t height, int32_t type, int32_t seed,
+                        uint8_t* mask, float* base, float* weight, float* inputs, void* stream);
+/* NeuralRadiosity::render: `spp` samples with seeds[i], each traced,
+ * inferred and combined (LHS: mask ? base : net; RHS: base + weight * net
+ * where mask = 0), averaged into film (float4[w*h], device). */
+srt_status srt_nr_render(const srt_scene* scene, srt_nr* nr, int32_t width, int32_t height, int32_t type,
+                         int32_t spp, const int32_t* seeds, float* film, void* stream);
 srt_status srt_pt_get_stats(const srt_pt* pt, srt_pt_stats* stats);
 /* Profiling switch (PROFILE() scopes of src/utils/profiler.h:219 applied per
  * kernel).  enable = 1: the iteration graph carries event records between
@@ -516,7 +554,7 @@ srt_status srt_procedural_resolution(const srt_procedural* p, int32_t* width, in
 /* ------------------------------------------------------------------ */
 
 /* JSON config with "render", "passes", "scene" (example/example.json).
- * Passes registered: PathTracer, Wavefront, LightTracer, Accumulate, ToneMapping, Measure.
+ * Passes registered: PathTracer, Wavefront, LightTracer, NeuralRadiosity, Accumulate, ToneMapping, Measure.
  * scene.model: "procedural:cornell" | "procedural:spheres[:n[:subdiv[:seed]]]"
  * | a scene file (.pbrt, .obj, .ply). */
 typedef struct srt_renderer srt_renderer;

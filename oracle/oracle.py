@@ -60,6 +60,8 @@ def lib():
             "oracle_hitinfo": (None, [_vp, _i64, _vp, _vp, _vp]),
             "oracle_texture_lookup": (None, [_vp, C.c_int, _i64, _vp, _vp]),
             "oracle_light_trace": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp, _vp]),
+            "oracle_nr_trace": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp]),
+            "oracle_nr_infer": (None, [_vp, _i64, _vp, _vp, C.c_int]),
             "oracle_render": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int,
                                         C.c_int, _vp, _vp, _vp, _vp]),
             "oracle_accumulate": (None, [_vp, _vp, _i64, C.c_int]),
@@ -198,6 +200,18 @@ class OracleScene:
             raise ValueError(f"oracle_light_trace failed ({rc})")
         return film, cnt
 
+    def nr_trace(self, w, h, type_, seed):
+        n = w * h
+        mask = np.zeros(n, np.uint8)
+        base = np.zeros((n, 3), np.float32)
+        weight = np.zeros((n, 3), np.float32)
+        inputs = np.zeros((n, 12), np.float32)
+        rc = lib().oracle_nr_trace(self.h, w, h, int(type_), int(seed), int(self.has_bvh), _np(mask), _np(base),
+                                   _np(weight), _np(inputs))
+        if rc != 0:
+            raise ValueError(f"oracle_nr_trace failed ({rc})")
+        return mask, base, weight, inputs
+
     def render(self, w, h, params, crop=None, threads=8):
         x0, y0, cw, ch = crop if crop else (0, 0, w, h)
         film = np.zeros((ch * cw, 4), np.float32)
@@ -216,6 +230,14 @@ class OracleScene:
                 lib().oracle_scene_destroy(self.h)
         except Exception:
             pass
+
+
+def nr_infer(params, inputs, threads=8):
+    params = np.ascontiguousarray(params, np.float32)
+    inputs = np.ascontiguousarray(inputs, np.float32)
+    out = np.zeros((len(inputs), 3), np.float32)
+    lib().oracle_nr_infer(_np(params), len(inputs), _np(inputs), _np(out), threads)
+    return out
 
 
 def camera_rays(cam, xy):

@@ -1608,6 +1608,210 @@ int oracle_light_trace(const oracle_scene* s, int w, int h, const srt_pt_params*
     return 0;
 }
 
+// ---- NeuralRadiosity (src/shader/npr/nr_lhs.cu, nr_rhs.cu) -------------
+
+// the 12 network inputs of a hit (nr_lhs.cu:69-86)
+static void nr_input(float* in, F3 pos, F3 rd, F3 n, F3 c)
+{
+    F3 d = (rd * -1.0f + F3(1.0f)) * 0.5f;
+    F3 m = (n + F3(1.0f)) * 0.5f;
+    const float v[12] = {pos.x, pos.y, pos.z, d.x, d.y, d.z, m.x, m.y, m.z, c.x, c.y, c.z};
+    for (int k = 0; k < 12; ++k) in[k] = v[k];
+}
+
+// One sample of the LHS (type 0) or RHS (type 1) raygen for every pixel.
+int oracle_nr_trace(const oracle_scene* sp, int w, int h, int type, int seed, int use_bvh, uint8_t* mask, float* base,
+                    float* weight, float* inputs)
+{
+    const oracle_scene& s = *sp;
+    if (w <= 0 || h <= 0) return 1;
+    if (type == 1 && s.light_inst.empty()) return 2;
+    for (int64_t idx = 0; idx < (int64_t)w * h; ++idx) {
+        const int ix = (int)(idx % w), iy = (int)(idx / w);
+        F3 b(0.0f), wgt(0.0f);
+        uint8_t mk = 1;
+        float* in = inputs + 12 * idx;
+        for (int k = 0; k < 12; ++k) in[k] = 0.0f;
+        Rng rng;
+        rng.mode = SRT_RNG_CURAND;
+        rng.init_curand(seed, (int)idx);
+        float jx = rng.next();
+        float jy = rng.next();
+        F3 ro, rd;
+        camera_ray(s.cam, ((float)ix + jx) / (float)w, ((float)iy + jy) / (float)h, ro, rd);
+        Hit hit = trace(s, ro, rd, 1e-3f, 1e16f, false, use_bvh != 0);
+        if (hit.prim >= 0) {
+            HitInfo hi = hit_info(s, hit.prim, hit.u, hit.v);
+            const srt_material& mat = s.mats[hi.mat];
+            if (mat.intensity > 0.0f) {
+                b = hi.emission;
+            } else if (type == 0) {
+                mk = 0;
+                nr_input(in, hi.pos, rd, hi.normal, hi.color);
+            } else {
+                Bx<float> bx = bx_of(mat.bxdf);
+                const bool transmissive = is_transmissive(mat.bxdf);
+                if (!is_specular(mat.bxdf)) {
+                    float l1 = rng.next();
+                    float l2 = rng.next();
+                    LSample ls = light_sample(s, l1, l2, false);
+                    F3 sd = normalize(ls.pos - hi.pos);
+                    float cos_o = dot(hi.normal, sd);
+                    float cos_l = dot(ls.normal, sd * -1.0f);
+                    float t = length(ls.pos - hi.pos);
+                    if (cos_l > 1e-4f && ls.pdf > 1e-4f && t > 1e-3f && (cos_o > 0.0f || transmissive)) {
+                        Hit sh = trace(s, hi.pos, sd, 1e-3f, t - 1e-3f, true, use_bvh != 0);
+                        if (sh.prim < 0) {
+                            float lpdf = ls.pdf * t * t / cos_l;
+                            float mpdf = mat_pdf(bx, hi.onb, sd, rd * -1.0f, hi.color);
+                            float mis = lpdf / (lpdf + mpdf);
+                            b = mat_eval(bx, hi.onb, sd, rd * -1.0f, hi.color) * std::fabs(cos_o) * ls.emission * mis /
+                                lpdf;
+                        }
+                    }
+                }
+                float u1 = rng.next();
+                float u2 = rng.next();
+                BSample<float> ms = mat_sample(bx, hi.onb, rd * -1.0f, u1, u2, hi.color);
+                float cos_t = dot(ms.wi, hi.normal);
+                if (!(ms.pdf <= 1e-4f) && !(cos_t < 0.0f && !transmissive)) {
+                    F3 wv = ms.f / ms.pdf * (ms.delta ? 1.0f : std::fabs(cos_t));
+                    Hit h2 = trace(s, hi.pos, ms.wi, 1e-3f, 1e16f, false, use_bvh != 0);
+                    if (h2.prim >= 0) {
+                        HitInfo h2i = hit_info(s, h2.prim, h2.u, h2.v);
+                        const srt_material& m2 = s.mats[h2i.mat];
+                        if (m2.intensity > 0.0f) {
+                            float cos_i = dot(h2i.normal, ms.wi * -1.0f);
+                            if (cos_i > 1e-4f) {
+                                float t2 = dot(h2i.pos - hi.pos, h2i.pos - hi.pos);
+                                float lpdf = light_pdf_of(s, h2i.light_id) * t2 / cos_i;
+                                float mis = ms.pdf / (ms.pdf + lpdf);
+                                b = b + wv * h2i.emission * mis;
+                            }
+                        } else {
+                            mk = 0;
+                            wgt = wv;
+                            nr_input(in, h2i.pos, ms.wi, h2i.normal, h2i.color);
+                        }
+                    }
+                }
+            }
+        }
+        mask[idx] = mk;
+        base[3 * idx] = b.x;
+        base[3 * idx + 1] = b.y;
+        base[3 * idx + 2] = b.z;
+        if (weight) {
+            weight[3 * idx] = wgt.x;
+            weight[3 * idx + 1] = wgt.y;
+            weight[3 * idx + 2] = wgt.z;
+        }
+    }
+    return 0;
+}
+
+// float -> bfloat16 -> float, round to nearest even (NaN kept quiet)
+static float bf16_round(float x)
+{
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) {
+        u |= 0x00400000u;
+    } else {
+        u += 0x7fffu + ((u >> 16) & 1u);
+    }
+    u &= 0xffff0000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+
+// The network of the NeuralRadiosity pass, restated from its description
+// (hash grid after Mueller et al. 2022 with this library's layout; real
+// spherical harmonics; BF16 activations and weights, exact sums).
+void oracle_nr_infer(const float* params, int64_t n, const float* inputs, float* out, int threads)
+{
+    const int L = 8, F = 8, log2T = 19, W = 256, ENC = 96;
+    std::vector<int64_t> off(L + 1, 0), res(L), size(L);
+    for (int l = 0; l < L; ++l) {
+        res[l] = (int64_t)16 << l;
+        const int64_t r3 = res[l] * res[l] * res[l];
+        size[l] = r3 <= (1ll << log2T) ? r3 : (1ll << log2T);
+        off[l + 1] = off[l] + size[l];
+    }
+    const float* wts = params + off[L] * F;
+    const int in_dims[5] = {ENC, W, W, W, W}, out_dims[5] = {W, W, W, W, 16};
+    std::vector<int64_t> woff(6, 0);
+    for (int l = 0; l < 5; ++l) woff[l + 1] = woff[l] + (int64_t)in_dims[l] * out_dims[l];
+    std::vector<float> wb((size_t)woff[5]);
+    for (int64_t i = 0; i < woff[5]; ++i) wb[i] = bf16_round(wts[i]);
+    parallel_for(n, threads, [&](int64_t q) {
+        const float* in = inputs + 12 * q;
+        std::vector<float> x(ENC, 1.0f), y(W);
+        for (int l = 0; l < L; ++l) {
+            const float scale = (float)res[l] - 1.0f;
+            const bool dense = size[l] == res[l] * res[l] * res[l];
+            const float* g = params + off[l] * F;
+            int pi[3];
+            float w1[3];
+            for (int k = 0; k < 3; ++k) {
+                const float sv = in[k] * scale + 0.5f;
+                const float fl = std::floor(sv);
+                pi[k] = (int)fl;
+                const float fr = sv - fl;
+                w1[k] = fr * fr * (3.0f - 2.0f * fr);
+            }
+            float acc[8] = {};
+            for (int c = 0; c < 8; ++c) {
+                const int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+                const float wc = (dx ? w1[0] : 1.0f - w1[0]) * (dy ? w1[1] : 1.0f - w1[1]) * (dz ? w1[2] : 1.0f - w1[2]);
+                const uint32_t ux = (uint32_t)(pi[0] + dx), uy = (uint32_t)(pi[1] + dy), uz = (uint32_t)(pi[2] + dz);
+                int64_t e;
+                if (dense) {
+                    const int64_t r = res[l];
+                    e = (((int64_t)(int32_t)ux % r + r) % r) + (((int64_t)(int32_t)uy % r + r) % r) * r +
+                        (((int64_t)(int32_t)uz % r + r) % r) * r * r;
+                } else {
+                    e = (int64_t)((ux * 1u ^ uy * 2654435761u ^ uz * 805459861u) & ((1u << log2T) - 1u));
+                }
+                for (int k = 0; k < F; ++k) acc[k] += wc * g[e * F + k];
+            }
+            for (int k = 0; k < F; ++k) x[l * F + k] = bf16_round(acc[k]);
+        }
+        auto sh3 = [](float a, float b2, float c, float* o) {
+            o[0] = 0.28209479177387814f;
+            o[1] = -0.48860251190291987f * b2;
+            o[2] = 0.48860251190291987f * c;
+            o[3] = -0.48860251190291987f * a;
+            o[4] = 1.0925484305920792f * a * b2;
+            o[5] = -1.0925484305920792f * b2 * c;
+            o[6] = 0.94617469575755997f * c * c - 0.31539156525251999f;
+            o[7] = -1.0925484305920792f * a * c;
+            o[8] = 0.54627421529603959f * (a * a - b2 * b2);
+        };
+        float sd[9], sn[9];
+        sh3(in[3] * 2.0f - 1.0f, in[4] * 2.0f - 1.0f, in[5] * 2.0f - 1.0f, sd);
+        sh3(in[6] * 2.0f - 1.0f, in[7] * 2.0f - 1.0f, in[8] * 2.0f - 1.0f, sn);
+        for (int k = 0; k < 9; ++k) x[64 + k] = bf16_round(sd[k]);
+        for (int k = 0; k < 9; ++k) x[73 + k] = bf16_round(sn[k]);
+        for (int k = 0; k < 3; ++k) x[82 + k] = bf16_round(in[9 + k]);
+        std::vector<float> cur = x;
+        for (int l = 0; l < 5; ++l) {
+            std::vector<float> nxt((size_t)out_dims[l]);
+            for (int o = 0; o < out_dims[l]; ++o) {
+                double sacc = 0.0;
+                const float* wr = &wb[woff[l] + (int64_t)o * in_dims[l]];
+                for (int i = 0; i < in_dims[l]; ++i) sacc += (double)wr[i] * (double)cur[i];
+                float v = (float)sacc;
+                if (l < 4) v = bf16_round(std::max(v, 0.0f));
+                nxt[o] = v;
+            }
+            cur.swap(nxt);
+        }
+        for (int k = 0; k < 3; ++k) out[3 * q + k] = cur[k];
+    });
+}
+
 // Accumulate::render (src/passes/postprocess/accumulate.cu:10-29)
 void oracle_accumulate(float* film, float* acc, int64_t n, int frame_count)
 {

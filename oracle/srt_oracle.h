@@ -77,6 +77,13 @@ void oracle_texture_lookup(const oracle_scene* s, int texture, int64_t n, const 
 int oracle_light_trace(const oracle_scene* s, int w, int h, const srt_pt_params* p, int use_bvh, int threads,
                        double* film, int64_t* counters);
 
+/* NeuralRadiosity: one LHS (0) / RHS (1) sample of every pixel (mask,
+ * base, weight, inputs as srt_nr_trace), and the network on n inputs
+ * (params as srt_nr_get_params; out n x 3). */
+int oracle_nr_trace(const oracle_scene* s, int w, int h, int type, int seed, int use_bvh, uint8_t* mask, float* base,
+                    float* weight, float* inputs);
+void oracle_nr_infer(const float* params, int64_t n, const float* inputs, float* out, int threads);
+
 /* Light::sample(u) -> pos, normal, emission, pdf (n x 10 floats). */
 void oracle_light_sample(const oracle_scene* s, int64_t n, const float* u2, int fixed_remap,
                          float* out);

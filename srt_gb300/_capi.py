@@ -146,6 +146,18 @@ _PROTOS = [
     ("srt_pt_create", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     ("srt_pt_render", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PtParams), C.c_void_p]),
     ("srt_lt_render", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(PtParams), C.POINTER(PtStats), C.c_void_p]),
+    ("srt_nr_num_params", C.c_int64, []),
+    ("srt_nr_create", C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("srt_nr_get_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("srt_nr_set_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("srt_nr_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("srt_nr_load", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("srt_nr_infer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("srt_nr_destroy", None, [C.c_void_p]),
+    ("srt_nr_trace", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("srt_nr_render", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                C.c_void_p, C.c_void_p]),
     ("srt_pt_get_stats", C.c_int, [C.c_void_p, C.POINTER(PtStats)]),
     ("srt_pt_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
     ("srt_pt_destroy", None, [C.c_void_p]),

@@ -1,0 +1,613 @@
+// neural_radiosity.cu — the NeuralRadiosity pass (src/passes/npr/neural_radiosity.{h,cu},
+// src/shader/npr/nr_lhs.cu, nr_rhs.cu) on this library's BVH.
+//
+// Trace (one thread per pixel, single-ray traversal of trace.cuh):
+//   LHS  camera ray to the first hit; a miss or an emitter ends there
+//        (mask = 1, base = its emission), else the hit's network input.
+//   RHS  first hit with next-event estimation (MIS) into base, one BSDF
+//        sample to a second hit: an emitter adds its MIS-weighted emission,
+//        any other surface asks the network (mask = 0, weight = f cos / pdf).
+//   Network input per pixel, 12 floats: position, (-dir + 1) / 2,
+//   (normal + 1) / 2, surface colour.
+// Network (the reference's tiny-cuda-nn configuration, our own kernels and
+// parameter layout): a hash grid on the position (8 levels x 8 features,
+// 2^19 entries per level, base resolution 16, scale 2, smoothstep
+// interpolation; Mueller et al., "Instant Neural Graphics Primitives",
+// 2022), real spherical harmonics of degree 3 (9 terms) on the direction
+// and on the normal, the colour as is, padded with ones to 96 columns;
+// then 96 -> 256 -> 256 -> 256 -> 256 -> 16 (3 used), ReLU, no biases,
+// BF16 weights and activations with FP32 accumulation.  The encoding is a
+// CUDA kernel here; the five layers are plain GEMMs with a ReLU epilogue
+// and go to cuBLASLt.
+// Combine: LHS pixel = mask ? base : net; RHS pixel = base + weight * net
+// where the network was asked (mask = 0).  The reference's RHS combine
+// adds the network term where mask == 1, i.e. where this frame wrote no
+// network input and no weight; that reads the previous frames' buffers and
+// is not reproduced.
+#include <cublasLt.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <vector>
+
+#include "scene.h"
+#include "shading.cuh"
+#include "trace.cuh"
+
+namespace srt {
+
+namespace {
+
+constexpr int kNrThreads = 128;
+constexpr int kNrLevels = 8, kNrFeat = 8, kNrLog2T = 19, kNrBaseRes = 16;
+constexpr int kNrEncUsed = kNrLevels * kNrFeat + 9 + 9 + 3;  // 85
+constexpr int kNrEnc = 96, kNrWidth = 256, kNrOut = 16;
+constexpr int kNrLayers = 5;
+
+__host__ __device__ constexpr int64_t nr_level_res(int l) { return (int64_t)kNrBaseRes << l; }
+__host__ __device__ constexpr int64_t nr_level_size(int l)
+{
+    return nr_level_res(l) * nr_level_res(l) * nr_level_res(l) <= (1ll << kNrLog2T)
+               ? nr_level_res(l) * nr_level_res(l) * nr_level_res(l)
+               : (1ll << kNrLog2T);
+}
+__host__ __device__ constexpr int64_t nr_level_offset(int l)  // in entries
+{
+    return l == 0 ? 0 : nr_level_offset(l - 1) + nr_level_size(l - 1);
+}
+constexpr int64_t kNrGridEntries = nr_level_offset(kNrLevels);
+constexpr int64_t kNrGridParams = kNrGridEntries * kNrFeat;
+__host__ __device__ constexpr int nr_in(int l) { return l == 0 ? kNrEnc : kNrWidth; }
+__host__ __device__ constexpr int nr_out(int l) { return l == kNrLayers - 1 ? kNrOut : kNrWidth; }
+constexpr int64_t nr_w_offset(int l) { return l == 0 ? 0 : nr_w_offset(l - 1) + (int64_t)nr_in(l - 1) * nr_out(l - 1); }
+constexpr int64_t kNrWeights = nr_w_offset(kNrLayers);
+constexpr int64_t kNrParams = kNrGridParams + kNrWeights;
+
+// ---- trace -------------------------------------------------------------------
+
+struct NrArgs {
+    int32_t w, h, seed, rhs;
+    bool fixed;
+};
+
+struct HitSurf {
+    float3 pos, ng, base_color;
+    float4 em;
+    Frame fr;
+    Bxdf bx;
+    int mflags, light_id;
+};
+
+// get_hitinfo (hit_info.h:27-64): the normal is flipped to the shading
+// normal's side only, not to the viewer's
+__device__ __forceinline__ HitSurf surface_at(const SceneView& S, const Hit& h)
+{
+    HitSurf s;
+    const float4* tp = S.tris + 3 * (size_t)h.tri;
+    const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+    const float3 v0 = f3(ta), v1 = f3(tb), v2 = f3(tc);
+    const InstanceRec ir = S.insts[__float_as_int(ta.w)];
+    s.bx = unpack_bxdf(S.mats, ir.material, s.base_color, s.em, s.mflags);
+    s.light_id = ir.light_id;
+    s.pos = v0 * (1.0f - h.u - h.v) + v1 * h.u + v2 * h.v;
+    s.ng = normalize(cross(v1 - v0, v2 - v0));
+    float3 sn = s.ng;
+    if (ir.attr & kAttrNormals) {
+        const float4* np = S.normals + 3 * (size_t)h.tri;
+        sn = normalize(f3(__ldg(np)) * (1.0f - h.u - h.v) + f3(__ldg(np + 1)) * h.u + f3(__ldg(np + 2)) * h.v);
+    }
+    if (s.mflags & kMatTextured)
+        apply_material_textures(S, ir.attr, ir.material, __float_as_int(ta.w), h.tri, h.u, h.v, s.base_color, s.em,
+                                sn);
+    if (dot(s.ng, sn) < 0.0f) s.ng = -s.ng;
+    float3 tan = (fabsf(sn.x) > fabsf(sn.y)) ? make_float3(0.f, 1.f, 0.f) : make_float3(1.f, 0.f, 0.f);
+    if (ir.attr & kAttrTangents) {
+        const float4* gp = S.tangents + 3 * (size_t)h.tri;
+        tan = f3(__ldg(gp)) * (1.0f - h.u - h.v) + f3(__ldg(gp + 1)) * h.u + f3(__ldg(gp + 2)) * h.v;
+    }
+    s.fr = Frame::from_normal_tangent(sn, tan);
+    return s;
+}
+
+__device__ __forceinline__ void write_input(float* in, const float3& pos, const float3& rd, const float3& n,
+                                            const float3& c)
+{
+    const float3 d = (-1.0f * rd + make_float3(1.f, 1.f, 1.f)) * 0.5f;
+    const float3 m = (n + make_float3(1.f, 1.f, 1.f)) * 0.5f;
+    const float v[12] = {pos.x, pos.y, pos.z, d.x, d.y, d.z, m.x, m.y, m.z, c.x, c.y, c.z};
+    for (int k = 0; k < 12; ++k) in[k] = v[k];
+}
+
+__global__ void __launch_bounds__(kNrThreads) k_nr_trace(SceneView S, CameraRec cam, NrArgs a, uint8_t* mask,
+                                                         float* base, float* weight, float* inputs, int* overflow_flag)
+{
+    __shared__ uint2 stack_mem[kStackEntries * kNrThreads];
+    Stack st{stack_mem + threadIdx.x, kNrThreads, 0};
+    int overflow = 0;
+    const int64_t n = (int64_t)a.w * a.h;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(idx % a.w), iy = (int)(idx / a.w);
+        float3 b = make_float3(0.0f, 0.0f, 0.0f), wgt = b;
+        uint8_t mk = 1;
+        float* in = inputs + 12 * idx;
+        Rng rng;
+        curand_init(pixel_seed(a.seed, (int32_t)idx), 0ull, 0ull, &rng.s);
+        const float jx = rng.next();
+        const float jy = rng.next();
+        float3 ro, rd;
+        camera_ray(cam, ((float)ix + jx) / (float)a.w, ((float)iy + jy) / (float)a.h, ro, rd);
+        const Hit h = trace_closest(S, ro, rd, 1e-3f, 1e16f, st, overflow);
+        if (h.tri < 0) {
+            // a miss: no emission (the environment is not read here)
+        } else {
+            const HitSurf s = surface_at(S, h);
+            if (s.mflags & kMatEmissive) {
+                b = f3(s.em);
+            } else if (!a.rhs) {
+                mk = 0;
+                write_input(in, s.pos, rd, s.ng, s.base_color);
+            } else {
+                const bool transmissive = (s.mflags & kMatTransmissive) != 0;
+                // next-event estimation (nr_rhs.cu:83-107)
+                if (!(s.mflags & kMatSpecular)) {
+                    const float l1 = rng.next();
+                    const float l2 = rng.next();
+                    const LightSample ls = sample_light(S, l1, l2, a.fixed);
+                    const float3 sd = normalize(ls.pos - s.pos);
+                    const float cos_o = dot(s.ng, sd);
+                    const float cos_l = dot(ls.normal, -1.0f * sd);
+                    const float t = length(ls.pos - s.pos);
+                    if (cos_l > 1e-4f && ls.pdf > 1e-4f && t > 1e-3f && (cos_o > 0.0f || transmissive)) {
+                        if (!trace_any(S, s.pos, sd, 1e-3f, t - 1e-3f, st, overflow)) {
+                            const float lpdf = ls.pdf * t * t / cos_l;
+                            const float mpdf = material_pdf(s.bx, s.fr, sd, -1.0f * rd, s.base_color);
+                            const float mis = lpdf / (lpdf + mpdf);
+                            b = material_eval(s.bx, s.fr, sd, -1.0f * rd, s.base_color) * fabsf(cos_o) * ls.emission *
+                                mis / lpdf;
+                        }
+                    }
+                }
+                // one BSDF sample to the second hit (nr_rhs.cu:109-155)
+                const float u1 = rng.next();
+                const float u2 = rng.next();
+                const BxdfSample ms = material_sample(s.bx, s.fr, -1.0f * rd, make_float2(u1, u2), s.base_color);
+                const float cos_t = dot(ms.wi, s.ng);
+                if (!(ms.pdf <= 1e-4f) && !(cos_t < 0.0f && !transmissive)) {
+                    const float3 w = ms.f / ms.pdf * (ms.delta ? 1.0f : fabsf(cos_t));
+                    const Hit h2 = trace_closest(S, s.pos, ms.wi, 1e-3f, 1e16f, st, overflow);
+                    if (h2.tri >= 0) {
+                        const HitSurf s2 = surface_at(S, h2);
+                        if (s2.mflags & kMatEmissive) {
+                            const float cos_i = dot(s2.ng, -1.0f * ms.wi);
+                            if (cos_i > 1e-4f) {
+                                const float t2 = dot(s2.pos - s.pos, s2.pos - s.pos);
+                                const float lpdf = S.lights[s2.light_id].pdf * t2 / cos_i;
+                                const float mis = ms.pdf / (ms.pdf + lpdf);
+                                b = b + w * f3(s2.em) * mis;
+                            }
+                        } else {
+                            mk = 0;
+                            wgt = w;
+                            write_input(in, s2.pos, ms.wi, s2.ng, s2.base_color);
+                        }
+                    }
+                }
+            }
+        }
+        mask[idx] = mk;
+        base[3 * idx] = b.x;
+        base[3 * idx + 1] = b.y;
+        base[3 * idx + 2] = b.z;
+        if (weight) {
+            weight[3 * idx] = wgt.x;
+            weight[3 * idx + 1] = wgt.y;
+            weight[3 * idx + 2] = wgt.z;
+        }
+        if (mk) {
+            for (int k = 0; k < 12; ++k) in[k] = 0.0f;
+        }
+    }
+    if (overflow) atomicExch(overflow_flag, 1);
+}
+
+// ---- encoding ---------------------------------------------------------------------
+
+__device__ __forceinline__ void sh3(float x, float y, float z, float* o)
+{
+    // real spherical harmonics, bands 0..2
+    o[0] = 0.28209479177387814f;
+    o[1] = -0.48860251190291987f * y;
+    o[2] = 0.48860251190291987f * z;
+    o[3] = -0.48860251190291987f * x;
+    o[4] = 1.0925484305920792f * x * y;
+    o[5] = -1.0925484305920792f * y * z;
+    o[6] = 0.94617469575755997f * z * z - 0.31539156525251999f;
+    o[7] = -1.0925484305920792f * x * z;
+    o[8] = 0.54627421529603959f * (x * x - y * y);
+}
+
+// one thread per (query, level); level threads also write the other columns
+__global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inputs, int64_t n,
+                                                   const float* __restrict__ grid, __nv_bfloat16* __restrict__ out)
+{
+    const int64_t total = n * kNrLevels;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const int64_t q = t / kNrLevels;
+        const int l = (int)(t % kNrLevels);
+        const float* in = inputs + 12 * q;
+        __nv_bfloat16* o = out + kNrEnc * q;
+        const float scale = (float)nr_level_res(l) - 1.0f;
+        const int64_t res = nr_level_res(l);
+        const bool dense = nr_level_size(l) == res * res * res;
+        const float* g = grid + nr_level_offset(l) * kNrFeat;
+        int pi[3];
+        float w1[3];
+        for (int k = 0; k < 3; ++k) {
+            const float s = in[k] * scale + 0.5f;
+            const float f = floorf(s);
+            pi[k] = (int)f;
+            const float fr = s - f;
+            w1[k] = fr * fr * (3.0f - 2.0f * fr);  // smoothstep
+        }
+        float acc[kNrFeat] = {};
+        for (int c = 0; c < 8; ++c) {
+            const int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+            const float wc = (dx ? w1[0] : 1.0f - w1[0]) * (dy ? w1[1] : 1.0f - w1[1]) * (dz ? w1[2] : 1.0f - w1[2]);
+            const uint32_t x = (uint32_t)(pi[0] + dx), y = (uint32_t)(pi[1] + dy), z = (uint32_t)(pi[2] + dz);
+            int64_t e;
+            if (dense) {
+                const int64_t r = res;
+                e = (((int64_t)(int32_t)x % r + r) % r) + (((int64_t)(int32_t)y % r + r) % r) * r +
+                    (((int64_t)(int32_t)z % r + r) % r) * r * r;
+            } else {
+                e = (int64_t)((x * 1u ^ y * 2654435761u ^ z * 805459861u) & ((1u << kNrLog2T) - 1u));
+            }
+            const float4* p = reinterpret_cast<const float4*>(g + e * kNrFeat);
+            const float4 f0 = __ldg(p), f1 = __ldg(p + 1);
+            acc[0] += wc * f0.x;
+            acc[1] += wc * f0.y;
+            acc[2] += wc * f0.z;
+            acc[3] += wc * f0.w;
+            acc[4] += wc * f1.x;
+            acc[5] += wc * f1.y;
+            acc[6] += wc * f1.z;
+            acc[7] += wc * f1.w;
+        }
+        for (int k = 0; k < kNrFeat; ++k) o[l * kNrFeat + k] = __float2bfloat16_rn(acc[k]);
+        if (l == 0) {
+            float sd[9], sn[9];
+            sh3(in[3] * 2.0f - 1.0f, in[4] * 2.0f - 1.0f, in[5] * 2.0f - 1.0f, sd);
+            sh3(in[6] * 2.0f - 1.0f, in[7] * 2.0f - 1.0f, in[8] * 2.0f - 1.0f, sn);
+            const int b0 = kNrLevels * kNrFeat;
+            for (int k = 0; k < 9; ++k) o[b0 + k] = __float2bfloat16_rn(sd[k]);
+            for (int k = 0; k < 9; ++k) o[b0 + 9 + k] = __float2bfloat16_rn(sn[k]);
+            for (int k = 0; k < 3; ++k) o[b0 + 18 + k] = __float2bfloat16_rn(in[9 + k]);
+            for (int k = kNrEncUsed; k < kNrEnc; ++k) o[k] = __float2bfloat16_rn(1.0f);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_nr_to_bf16(const float* __restrict__ w, int64_t n, __nv_bfloat16* __restrict__ o)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) o[i] = __float2bfloat16_rn(w[i]);
+}
+
+__global__ void __launch_bounds__(256) k_nr_combine(const uint8_t* __restrict__ mask, const float* __restrict__ base,
+                                                    const float* __restrict__ weight, const float* __restrict__ net,
+                                                    int64_t n, int rhs, float4* __restrict__ film, float inv_spp,
+                                                    int last)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float3 b = make_float3(base[3 * i], base[3 * i + 1], base[3 * i + 2]);
+        const float3 y = make_float3(net[kNrOut * i], net[kNrOut * i + 1], net[kNrOut * i + 2]);
+        float3 r;
+        if (!rhs) {
+            r = mask[i] ? b : y;
+        } else {
+            r = b;
+            if (!mask[i]) r = r + make_float3(weight[3 * i], weight[3 * i + 1], weight[3 * i + 2]) * y;
+        }
+        float4 f = film[i];
+        f = make_float4(f.x + r.x, f.y + r.y, f.z + r.z, f.w + 1.0f);
+        if (last) f = make_float4(f.x * inv_spp, f.y * inv_spp, f.z * inv_spp, f.w * inv_spp);
+        film[i] = f;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_nr_clear(float4* film, int64_t n)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        film[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+int grid_for(int64_t n, int threads)
+{
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, (int64_t)device_sm_count() * 16));
+}
+
+// PCG32 (O'Neill, 2014) for the parameter initialisation
+struct Pcg {
+    uint64_t state, inc;
+    Pcg(uint64_t seed, uint64_t seq) : state(0), inc((seq << 1u) | 1u)
+    {
+        next();
+        state += seed;
+        next();
+    }
+    uint32_t next()
+    {
+        uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        uint32_t x = (uint32_t)(((old >> 18u) ^ old) >> 27u), r = (uint32_t)(old >> 59u);
+        return (x >> r) | (x << ((32 - r) & 31));
+    }
+    float uniform() { return (float)(next() >> 8) * (1.0f / 16777216.0f); }
+};
+
+}  // namespace
+
+}  // namespace srt
+
+using namespace srt;
+
+struct srt_nr {
+    DeviceBuffer params;   // fp32: grid | weights
+    DeviceBuffer w16;      // bf16 weights
+    DeviceBuffer act0, act1, out, work;
+    int64_t cap = 0;       // rows the activation buffers hold
+    cublasLtHandle_t lt = nullptr;
+    ~srt_nr()
+    {
+        if (lt) cublasLtDestroy(lt);
+    }
+};
+
+namespace {
+
+srt_status lt_check(cublasStatus_t s, const char* what)
+{
+    return s == CUBLAS_STATUS_SUCCESS ? SRT_OK
+                                      : set_error(SRT_ERR_CUDA, std::string("cuBLASLt ") + what + " failed (" +
+                                                                    std::to_string((int)s) + ")");
+}
+
+// D[n x out] = act(X[n x in] W^T), row-major, through cuBLASLt column-major views
+srt_status nr_gemm(srt_nr* nr, const __nv_bfloat16* W, int in, int outd, const __nv_bfloat16* X, void* D, int64_t n,
+                   bool relu, bool f32_out, cudaStream_t st)
+{
+    cublasLtMatmulDesc_t op = nullptr;
+    cublasLtMatrixLayout_t la = nullptr, lb = nullptr, ld = nullptr;
+    cublasLtMatmulPreference_t pref = nullptr;
+    srt_status s = lt_check(cublasLtMatmulDescCreate(&op, CUBLAS_COMPUTE_32F, CUDA_R_32F), "desc");
+    const cublasOperation_t ta = CUBLAS_OP_T, tb = CUBLAS_OP_N;
+    const cublasLtEpilogue_t epi = relu ? CUBLASLT_EPILOGUE_RELU : CUBLASLT_EPILOGUE_DEFAULT;
+    if (s == SRT_OK) s = lt_check(cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)), "transa");
+    if (s == SRT_OK) s = lt_check(cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)), "transb");
+    if (s == SRT_OK) s = lt_check(cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_EPILOGUE, &epi, sizeof(epi)), "epilogue");
+    if (s == SRT_OK) s = lt_check(cublasLtMatrixLayoutCreate(&la, CUDA_R_16BF, in, outd, in), "layout A");
+    if (s == SRT_OK) s = lt_check(cublasLtMatrixLayoutCreate(&lb, CUDA_R_16BF, in, (uint64_t)n, in), "layout B");
+    if (s == SRT_OK)
+        s = lt_check(cublasLtMatrixLayoutCreate(&ld, f32_out ? CUDA_R_32F : CUDA_R_16BF, outd, (uint64_t)n, outd),
+                     "layout D");
+    const size_t ws = nr->work.bytes();
+    if (s == SRT_OK) s = lt_check(cublasLtMatmulPreferenceCreate(&pref), "preference");
+    if (s == SRT_OK)
+        s = lt_check(cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &ws,
+                                                          sizeof(ws)),
+                     "workspace");
+    cublasLtMatmulHeuristicResult_t hr{};
+    int found = 0;
+    if (s == SRT_OK) s = lt_check(cublasLtMatmulAlgoGetHeuristic(nr->lt, op, la, lb, ld, ld, pref, 1, &hr, &found), "heuristic");
+    if (s == SRT_OK && found == 0) s = set_error(SRT_ERR_CUDA, "cuBLASLt found no algorithm for the network layer");
+    const float alpha = 1.0f, beta = 0.0f;
+    if (s == SRT_OK)
+        s = lt_check(cublasLtMatmul(nr->lt, op, &alpha, W, la, X, lb, &beta, D, ld, D, ld, &hr.algo, nr->work.get(), ws,
+                                    st),
+                     "matmul");
+    if (pref) cublasLtMatmulPreferenceDestroy(pref);
+    if (ld) cublasLtMatrixLayoutDestroy(ld);
+    if (lb) cublasLtMatrixLayoutDestroy(lb);
+    if (la) cublasLtMatrixLayoutDestroy(la);
+    if (op) cublasLtMatmulDescDestroy(op);
+    return s;
+}
+
+srt_status nr_reserve(srt_nr* nr, int64_t n)
+{
+    if (n <= nr->cap) return SRT_OK;
+    const int64_t c = std::max<int64_t>(n, 1 << 16);
+    SRT_TRY(nr->act0.alloc((size_t)c * kNrWidth * 2, "network activations"));
+    SRT_TRY(nr->act1.alloc((size_t)c * kNrWidth * 2, "network activations"));
+    SRT_TRY(nr->out.alloc((size_t)c * kNrOut * 4, "network output"));
+    nr->cap = c;
+    return SRT_OK;
+}
+
+srt_status nr_sync_weights(srt_nr* nr)
+{
+    k_nr_to_bf16<<<grid_for(kNrWeights, 256), 256>>>(nr->params.as<float>() + kNrGridParams, kNrWeights,
+                                                      nr->w16.as<__nv_bfloat16>());
+    SRT_CUDA_TRY(cudaGetLastError());
+    return SRT_OK;
+}
+
+}  // namespace
+
+extern "C" int64_t srt_nr_num_params(void) { return kNrParams; }
+
+extern "C" srt_status srt_nr_create(uint64_t seed, srt_nr** out)
+{
+    clear_error();
+    if (!out) return set_error(SRT_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    srt_nr* nr = new (std::nothrow) srt_nr();
+    if (!nr) return set_error(SRT_ERR_OOM, "host allocation failed");
+    auto fail = [&](srt_status st) {
+        delete nr;
+        return st;
+    };
+    srt_status st = nr->params.alloc((size_t)kNrParams * 4, "network parameters");
+    if (st == SRT_OK) st = nr->w16.alloc((size_t)kNrWeights * 2, "network weights");
+    if (st == SRT_OK) st = nr->work.alloc(32u << 20, "cuBLASLt workspace");
+    if (st != SRT_OK) return fail(st);
+    if (cublasLtCreate(&nr->lt) != CUBLAS_STATUS_SUCCESS) return fail(set_error(SRT_ERR_CUDA, "cublasLtCreate failed"));
+    // initialisation as tiny-cuda-nn does it: grid features U(-1e-4, 1e-4),
+    // layer weights U(-s, s) with s = sqrt(6 / (fan_in + fan_out))
+    std::vector<float> p((size_t)kNrParams);
+    Pcg rng(seed, 0x5eedull);
+    for (int64_t i = 0; i < kNrGridParams; ++i) p[i] = (rng.uniform() * 2.0f - 1.0f) * 1e-4f;
+    for (int l = 0; l < kNrLayers; ++l) {
+        const float s = std::sqrt(6.0f / (float)(nr_in(l) + nr_out(l)));
+        for (int64_t i = 0; i < (int64_t)nr_in(l) * nr_out(l); ++i)
+            p[kNrGridParams + nr_w_offset(l) + i] = (rng.uniform() * 2.0f - 1.0f) * s;
+    }
+    if ((st = srt_nr_set_params(nr, p.data())) != SRT_OK) return fail(st);
+    *out = nr;
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_nr_get_params(const srt_nr* nr, float* host)
+{
+    clear_error();
+    if (!nr || !host) return set_error(SRT_ERR_ARG, "NULL argument");
+    SRT_CUDA_TRY(cudaMemcpy(host, nr->params.get(), (size_t)kNrParams * 4, cudaMemcpyDeviceToHost));
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_nr_set_params(srt_nr* nr, const float* host)
+{
+    clear_error();
+    if (!nr || !host) return set_error(SRT_ERR_ARG, "NULL argument");
+    SRT_CUDA_TRY(cudaMemcpy(nr->params.get(), host, (size_t)kNrParams * 4, cudaMemcpyHostToDevice));
+    SRT_TRY(nr_sync_weights(nr));
+    SRT_CUDA_TRY(cudaDeviceSynchronize());
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_nr_save(const srt_nr* nr, const char* path)
+{
+    clear_error();
+    if (!nr || !path) return set_error(SRT_ERR_ARG, "NULL argument");
+    std::vector<float> p((size_t)kNrParams);
+    SRT_TRY(srt_nr_get_params(nr, p.data()));
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return set_error(SRT_ERR_ARG, std::string("cannot open ") + path);
+    const char magic[8] = {'S', 'R', 'T', 'N', 'R', '0', '1', '\n'};
+    const int64_t n = kNrParams;
+    f.write(magic, 8);
+    f.write(reinterpret_cast<const char*>(&n), 8);
+    f.write(reinterpret_cast<const char*>(p.data()), (std::streamsize)(p.size() * 4));
+    return f ? SRT_OK : set_error(SRT_ERR_ARG, std::string("write failed: ") + path);
+}
+
+extern "C" srt_status srt_nr_load(srt_nr* nr, const char* path)
+{
+    clear_error();
+    if (!nr || !path) return set_error(SRT_ERR_ARG, "NULL argument");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return set_error(SRT_ERR_ARG, std::string("Failed to open file: ") + path);
+    char magic[8];
+    int64_t n = 0;
+    f.read(magic, 8);
+    f.read(reinterpret_cast<char*>(&n), 8);
+    if (!f || std::string(magic, 8) != std::string("SRTNR01\n", 8) || n != kNrParams)
+        return set_error(SRT_ERR_PARSE, std::string(path) + ": not a network file of this architecture");
+    std::vector<float> p((size_t)kNrParams);
+    f.read(reinterpret_cast<char*>(p.data()), (std::streamsize)(p.size() * 4));
+    if (!f) return set_error(SRT_ERR_PARSE, std::string(path) + ": truncated");
+    return srt_nr_set_params(nr, p.data());
+}
+
+extern "C" void srt_nr_destroy(srt_nr* nr) { delete nr; }
+
+extern "C" srt_status srt_nr_infer(srt_nr* nr, const float* inputs, int64_t n, float* out, void* stream)
+{
+    clear_error();
+    if (!nr || (n > 0 && (!inputs || !out))) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (n < 0) return set_error(SRT_ERR_ARG, "negative count");
+    if (n == 0) return SRT_OK;
+    cudaStream_t st = as_stream(stream);
+    SRT_TRY(nr_reserve(nr, n));
+    __nv_bfloat16* a0 = nr->act0.as<__nv_bfloat16>();
+    __nv_bfloat16* a1 = nr->act1.as<__nv_bfloat16>();
+    k_nr_encode<<<grid_for(n * kNrLevels, 256), 256, 0, st>>>(inputs, n, nr->params.as<float>(), a0);
+    SRT_CUDA_TRY(cudaGetLastError());
+    const __nv_bfloat16* w = nr->w16.as<__nv_bfloat16>();
+    for (int l = 0; l < kNrLayers; ++l) {
+        const bool last = l == kNrLayers - 1;
+        SRT_TRY(nr_gemm(nr, w + nr_w_offset(l), nr_in(l), nr_out(l), a0, last ? (void*)out : (void*)a1, n, !last, last,
+                        st));
+        std::swap(a0, a1);
+    }
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_nr_trace(const srt_scene* s, int32_t width, int32_t height, int32_t type, int32_t seed,
+                                   uint8_t* mask, float* base, float* weight, float* inputs, void* stream)
+{
+    clear_error();
+    if (!s || !mask || !base || !inputs || (type == SRT_NR_RHS && !weight)) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (width <= 0 || height <= 0 || (type != SRT_NR_LHS && type != SRT_NR_RHS))
+        return set_error(SRT_ERR_ARG, "bad size or type");
+    if (type == SRT_NR_RHS && s->view.num_lights == 0)
+        return set_error(SRT_ERR_UNSUPPORTED, "the RHS pass samples area lights and the scene has none");
+    cudaStream_t st = as_stream(stream);
+    int* flag = nullptr;
+    SRT_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&flag), sizeof(int), st));
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+    const int64_t n = (int64_t)width * height;
+    NrArgs a{width, height, seed, type == SRT_NR_RHS ? 1 : 0, false};
+    if (e == cudaSuccess) {
+        k_nr_trace<<<grid_for(n, kNrThreads), kNrThreads, 0, st>>>(s->view, s->camera, a, mask, base,
+                                                                  type == SRT_NR_RHS ? weight : nullptr, inputs, flag);
+        e = cudaGetLastError();
+    }
+    int overflow = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&overflow, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(flag, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "srt_nr_trace");
+    if (overflow) return set_error(SRT_ERR_STACK, "traversal stack overflow");
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_nr_render(const srt_scene* s, srt_nr* nr, int32_t width, int32_t height, int32_t type,
+                                    int32_t spp, const int32_t* seeds, float* film, void* stream)
+{
+    clear_error();
+    if (!s || !nr || !film || (spp > 0 && !seeds)) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (width <= 0 || height <= 0 || spp < 0) return set_error(SRT_ERR_ARG, "bad size or sample count");
+    if (reinterpret_cast<uintptr_t>(film) % 16) return set_error(SRT_ERR_ARG, "film must be 16-byte aligned");
+    cudaStream_t st = as_stream(stream);
+    const int64_t n = (int64_t)width * height;
+    float4* f4 = reinterpret_cast<float4*>(film);
+    k_nr_clear<<<grid_for(n, 256), 256, 0, st>>>(f4, n);
+    SRT_CUDA_TRY(cudaGetLastError());
+    if (spp == 0) return SRT_OK;
+    DeviceBuffer mask, base, weight, inputs;
+    SRT_TRY(mask.alloc((size_t)n, "mask"));
+    SRT_TRY(base.alloc((size_t)n * 12, "base"));
+    SRT_TRY(weight.alloc((size_t)n * 12, "weight"));
+    SRT_TRY(inputs.alloc((size_t)n * 48, "network inputs"));
+    SRT_TRY(nr_reserve(nr, n));
+    for (int i = 0; i < spp; ++i) {
+        SRT_TRY(srt_nr_trace(s, width, height, type, seeds[i], mask.as<uint8_t>(), base.as<float>(), weight.as<float>(),
+                             inputs.as<float>(), stream));
+        SRT_TRY(srt_nr_infer(nr, inputs.as<float>(), n, nr->out.as<float>(), stream));
+        k_nr_combine<<<grid_for(n, 256), 256, 0, st>>>(mask.as<uint8_t>(), base.as<float>(), weight.as<float>(),
+                                                        nr->out.as<float>(), n, type == SRT_NR_RHS, f4,
+                                                        1.0f / (float)spp, i == spp - 1);
+        SRT_CUDA_TRY(cudaGetLastError());
+    }
+    SRT_CUDA_TRY(cudaStreamSynchronize(st));
+    return SRT_OK;
+}

@@ -154,6 +154,51 @@ private:
 };
 RenderPassFactory::Register<LightTracer> LightTracer::reg("LightTracer");
 
+// ---- NeuralRadiosity (src/passes/npr/neural_radiosity.{h,cu}) ----------------
+
+class NeuralRadiosity : public RenderPass {
+public:
+    explicit NeuralRadiosity(const Json& j)
+    {
+        if (j.is_null()) return;
+        type = j.string("type", "LHS") == "RHS" ? SRT_NR_RHS : SRT_NR_LHS;
+        samples_per_pixel = (int)j.number("samples_per_pixel", 1);
+        train_model = j.boolean("train_model", false);
+        model_path = j.string("model_path", "");
+    }
+    ~NeuralRadiosity() override
+    {
+        if (nr) srt_nr_destroy(nr);
+    }
+    srt_status init() override
+    {
+        SRT_TRY(srt_nr_create(0, &nr));
+        // load_model: a missing file leaves the initialised network (neural_radiosity.cu:60-70)
+        if (!model_path.empty()) {
+            std::ifstream probe(model_path, std::ios::binary);
+            if (probe) SRT_TRY(srt_nr_load(nr, model_path.c_str()));
+        }
+        return SRT_OK;
+    }
+    srt_status render(std::shared_ptr<Film> film) override
+    {
+        if (!enable) return SRT_OK;
+        if (train_model && !model_path.empty()) SRT_TRY(srt_nr_save(nr, model_path.c_str()));  // train() = save_model
+        std::vector<int32_t> seeds((size_t)std::max(samples_per_pixel, 0));
+        for (int32_t& s : seeds) s = host_random_int(0, INT32_MAX);
+        return srt_nr_render(scene->handle, nr, width, height, type, samples_per_pixel, seeds.data(),
+                             film->get_pixels(), nullptr);
+    }
+
+private:
+    srt_nr* nr = nullptr;
+    int type = SRT_NR_LHS, samples_per_pixel = 1;
+    bool train_model = false;
+    std::string model_path;
+    static RenderPassFactory::Register<NeuralRadiosity> reg;
+};
+RenderPassFactory::Register<NeuralRadiosity> NeuralRadiosity::reg("NeuralRadiosity");
+
 // ---- Accumulate (src/passes/postprocess/accumulate.{h,cu}) -----------------
 
 class Accumulate : public RenderPass {
