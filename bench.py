@@ -290,6 +290,10 @@ def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_s
     cp = S._capi.CacheParams(1 << 16, 4, 1e-2, 0.5, 16, 1)
     st = S._capi.CacheStats()
     accd = torch.zeros((w * h, 4), dtype=torch.float64, device="cuda")
+    # the first FP64 accumulate loads torch's kernels (over a second on a fresh process): not frame time
+    accd += film.double()
+    accd.zero_()
+    torch.cuda.synchronize()
     t_total, t_reach, curve = 0.0, None, []
     queries = fallback = 0
     for f in range(frames):
