@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -12,7 +13,14 @@ namespace srt {
 namespace {
 
 constexpr int kBins = 32;
-constexpr int kMaxLeaf = 3;
+#ifndef SRT_BVH_MAX_LEAF
+#define SRT_BVH_MAX_LEAF 3
+#endif
+constexpr int kMaxLeaf = SRT_BVH_MAX_LEAF;  // triangles per leaf child; 8 leaves fill the 32-bit leaf mask at 4
+// SAH cost of a triangle test relative to a node visit in the collapse
+#ifndef SRT_BVH_COST_PRIM
+#define SRT_BVH_COST_PRIM 1.5f
+#endif
 
 struct Box {
     float lo[3], hi[3];
@@ -47,8 +55,9 @@ struct Box {
 
 struct BinNode {
     Box box;
-    int32_t left, right;   // children (internal)
-    int32_t begin, count;  // prims (leaf, count > 0)
+    int32_t left, right;    // children (internal)
+    int32_t begin, count;   // prims (leaf, count > 0)
+    int32_t rbegin, rcount; // the subtree's prims: idx[rbegin, rbegin + rcount)
 };
 
 struct Builder {
@@ -79,6 +88,8 @@ struct Builder {
             cb.grow_pt(cent + 3 * (size_t)idx[i]);
         }
         nodes[ni].box = bb;
+        nodes[ni].rbegin = begin;
+        nodes[ni].rcount = end - begin;
         const int n = end - begin;
         if (n <= 1) {
             make_leaf(ni, begin, n);
@@ -219,6 +230,74 @@ void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& o
     }
     out.binary_depth = B.max_depth.load();
 
+    // SAH-optimal collapse of the binary tree into 8-wide nodes (Ylitie,
+    // Karras, Laine, HPG 2017, section 3.1): cost[n][i] is the least SAH cost
+    // of the subtree at n given as at most i children of a wide node, with a
+    // child either a leaf (at most kMaxLeaf triangles), or a wide node of its
+    // own, or its subtree distributed over several slots.
+    const int nn = B.nnodes.load();
+    constexpr float kCostNode = 1.0f, kCostPrim = SRT_BVH_COST_PRIM;
+    const float kInf = std::numeric_limits<float>::infinity();
+    std::vector<float> cost((size_t)nn * 8, kInf);
+    std::vector<uint8_t> dec((size_t)nn * 8, 0);  // [0]: 0 leaf / 1 wide node; [i]: 0 = as i, k = k slots left
+    std::vector<uint8_t> split8((size_t)nn, 1);   // left slots when the node's own wide node splits 8 ways
+    for (int ni = nn - 1; ni >= 0; --ni) {
+        const BinNode& bn = B.nodes[ni];
+        float* c = &cost[(size_t)ni * 8];
+        uint8_t* d = &dec[(size_t)ni * 8];
+        const float A = bn.box.area();
+        if (bn.count > 0 || bn.left < 0) {
+            for (int i = 0; i < 8; ++i) c[i] = A * (float)bn.count * kCostPrim;
+            continue;
+        }
+        const float* cl = &cost[(size_t)bn.left * 8];
+        const float* cr = &cost[(size_t)bn.right * 8];
+        float dist[9];
+        uint8_t kbest[9];
+        for (int j = 2; j <= 8; ++j) {
+            dist[j] = kInf;
+            kbest[j] = 1;
+            for (int k = 1; k < j; ++k) {
+                const float v = cl[k - 1] + cr[j - k - 1];
+                if (v < dist[j]) {
+                    dist[j] = v;
+                    kbest[j] = (uint8_t)k;
+                }
+            }
+        }
+        const float c_int = A * kCostNode + dist[8];
+        const float c_leaf = bn.rcount <= kMaxLeaf ? A * (float)bn.rcount * kCostPrim : kInf;
+        c[0] = std::min(c_leaf, c_int);
+        d[0] = c_leaf <= c_int ? 0 : 1;
+        split8[ni] = kbest[8];
+        for (int i = 2; i <= 8; ++i) {
+            if (dist[i] < c[i - 2]) {
+                c[i - 1] = dist[i];
+                d[i - 1] = kbest[i];
+            } else {
+                c[i - 1] = c[i - 2];
+                d[i - 1] = 0;
+            }
+        }
+    }
+    // children of the wide node made at binary node m given j slots
+    std::vector<std::pair<int, bool>> kids;  // (binary node, as a leaf)
+    std::function<void(int, int)> resolve = [&](int m, int j) {
+        const BinNode& bm = B.nodes[m];
+        if (bm.count > 0 || bm.left < 0) {
+            kids.push_back({m, true});
+            return;
+        }
+        while (j > 1 && dec[(size_t)m * 8 + j - 1] == 0) --j;
+        if (j == 1) {
+            kids.push_back({m, dec[(size_t)m * 8] == 0});
+            return;
+        }
+        const int k = dec[(size_t)m * 8 + j - 1];
+        resolve(bm.left, k);
+        resolve(bm.right, j - k);
+    };
+
     static const float dirs[8][3] = {{1, 1, 1},  {-1, 1, 1},  {1, -1, 1},  {-1, -1, 1},
                                      {1, 1, -1}, {-1, 1, -1}, {1, -1, -1}, {-1, -1, -1}};
     struct Pending {
@@ -235,30 +314,26 @@ void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& o
         depth = std::max(depth, p.depth);
         const BinNode& b = B.nodes[p.bin];
         int ch[8];
+        bool as_leaf[8] = {false, false, false, false, false, false, false, false};
         int nc = 0;
+        kids.clear();
         if (b.count > 0 || b.left < 0) {
-            if (b.count > 0) ch[nc++] = p.bin;
+            if (b.count > 0) kids.push_back({p.bin, true});
+        } else if (p.bin == 0 && dec[0] == 0) {
+            kids.push_back({0, true});  // the whole scene is one leaf
         } else {
-            ch[nc++] = b.left;
-            ch[nc++] = b.right;
-            while (nc < 8) {
-                int pick = -1;
-                float pa = -1.0f;
-                for (int i = 0; i < nc; ++i) {
-                    const BinNode& c = B.nodes[ch[i]];
-                    if (c.count == 0 && c.left >= 0 && c.box.area() > pa) {
-                        pa = c.box.area();
-                        pick = i;
-                    }
-                }
-                if (pick < 0) break;
-                int open = ch[pick];
-                ch[pick] = B.nodes[open].left;
-                ch[nc++] = B.nodes[open].right;
-            }
+            const int k = split8[p.bin];
+            resolve(b.left, k);
+            resolve(b.right, 8 - k);
+        }
+        for (const auto& kd : kids) {
+            ch[nc] = kd.first;
+            as_leaf[nc] = kd.second;
+            ++nc;
         }
         // octant slot assignment: slot s holds the child nearest along dirs[s]
         int slot_child[8];
+        bool slot_leaf[8] = {false, false, false, false, false, false, false, false};
         for (int s = 0; s < 8; ++s) slot_child[s] = -1;
         {
             float pc[3];
@@ -286,6 +361,7 @@ void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& o
                 if (used[cand[k].c] || slot_child[cand[k].s] >= 0) continue;
                 used[cand[k].c] = true;
                 slot_child[cand[k].s] = ch[cand[k].c];
+                slot_leaf[cand[k].s] = as_leaf[cand[k].c];
             }
         }
         WideNode wn;
@@ -296,8 +372,7 @@ void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& o
         for (int s = 0; s < 8; ++s) {
             int c = slot_child[s];
             if (c < 0) continue;
-            const BinNode& cn = B.nodes[c];
-            if (cn.count == 0 && cn.left >= 0) {
+            if (!slot_leaf[s]) {
                 wn.imask |= (uint8_t)(1u << s);
                 wn.meta[s] = (uint8_t)(0x80 | rank);
                 queue.push_back({(int32_t)(child_base + rank), c, p.depth + 1});
@@ -310,10 +385,11 @@ void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& o
             int c = slot_child[s];
             if (c < 0) continue;
             const BinNode& cn = B.nodes[c];
-            if (cn.count > 0) {
+            if (slot_leaf[s] && cn.rcount > 0) {
+                // a leaf: the triangles of the binary subtree (at most kMaxLeaf)
                 uint32_t off = (uint32_t)out.tri_order.size() - tri_base;
-                for (int i = 0; i < cn.count; ++i) out.tri_order.push_back(B.idx[cn.begin + i]);
-                wn.meta[s] = (uint8_t)((cn.count << 5) | off);
+                for (int i = 0; i < cn.rcount; ++i) out.tri_order.push_back(B.idx[cn.rbegin + i]);
+                wn.meta[s] = (uint8_t)((cn.rcount << 5) | off);
             }
         }
         wn.child_base = child_base;

@@ -17,10 +17,10 @@ struct WideBvh {
 };
 
 // Triangles given as 9 floats each (v0, v1, v2).  Binned SAH (32 bins,
-// leaves of at most 3 triangles), collapsed greedily to 8-wide nodes by
-// opening the largest-area internal child, slots assigned by the octant
-// ordering, boxes quantised to 16 bits per axis.  `threads` host threads
-// build independent subtrees.
+// leaves of at most 3 triangles), collapsed to 8-wide nodes by the
+// SAH-optimal dynamic programme of Ylitie, Karras and Laine (HPG 2017),
+// slots assigned by the octant ordering, boxes quantised to 16 bits per
+// axis.  `threads` host threads build independent subtrees.
 void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& out);
 
 }  // namespace srt
