@@ -9,6 +9,7 @@ OBJ + MTL: the reference's Assimp path (src/importer/assimp.cu:17-131) —
 one mesh per object and material run, one material copy per mesh,
 ai_convert's parameter mapping over the OBJ reader's defaults.
 """
+import os
 import struct
 
 import numpy as np
@@ -321,3 +322,25 @@ def test_obj_textures_and_flipped_uvs(tmp_path):
     np.testing.assert_allclose(s.meshes[0]["texcoords"], [[0, 1], [1, 1], [1, 0], [0.25, 0.25]])
     np.testing.assert_allclose(s.meshes[1]["texcoords"], np.tile([0.25, 0.25], (3, 1)))
     assert s.meshes[2]["texcoords"] is None
+
+
+REF_EXAMPLE = "/root/reference/example/cornell_box_obj/cornell_box.obj"
+
+
+@pytest.mark.skipif(not os.path.exists(REF_EXAMPLE), reason="the reference tree is not present")
+def test_reference_example_cornell_obj():
+    """The reference's own example model (example/cornell_box_obj): one mesh
+    per group as Assimp makes them, the MTL mapped by ai_convert, the lamp's
+    Ke (17, 12, 4) as intensity |Ke| with a unit colour."""
+    s = S.import_scene(REF_EXAMPLE)
+    assert len(s.meshes) == 8 and len(s.materials) == 8
+    kd = [list(np.round(m.base_color[:], 3)) for m in s.materials]
+    assert kd[:5] == [[0.725, 0.71, 0.68]] * 3 + [[0.14, 0.45, 0.091], [0.63, 0.065, 0.05]]
+    lights = [m for m in s.materials if m.intensity > 0]
+    assert len(lights) == 1
+    le = np.array(lights[0].emission_color[:]) * lights[0].intensity
+    np.testing.assert_allclose(le, [17, 12, 4], rtol=1e-6)
+    assert np.allclose(list(lights[0].base_color), [0.78] * 3)
+    assert [m.bxdf.ior for m in s.materials][:5] == [1.0, 1.0, 1.0, 1.5, 1.5]
+    # 2 triangles per wall quad, 12 per box, 2 for the lamp
+    assert [len(m["indices"]) for m in s.meshes] == [2, 2, 2, 2, 2, 12, 12, 2]
