@@ -594,8 +594,9 @@ srt_status srt_renderer_save(const srt_renderer* r, const char* path);
  * clamp(x,0,1)*255 truncated), .bmp (24-bit), .hdr (Radiance RGBE), .pfm
  * (float RGB), .exr (OpenEXR: channels B, G, R, A as half, no
  * compression, as the reference's save_exr writes them through tinyexr,
- * :69-130).  flip != 0 mirrors x and y first, as the reference does before
- * saving; PFM keeps its bottom-to-top rows.  Other extensions (.jpg)
+ * :69-130), .jpg (baseline JPEG at quality 100, as save_ldr asks
+ * stbi_write_jpg for).  flip != 0 mirrors x and y first, as the reference
+ * does before saving; PFM keeps its bottom-to-top rows.  Other extensions
  * return SRT_ERR_UNSUPPORTED. */
 srt_status srt_image_write(const char* path, int32_t width, int32_t height, const float* rgba, int32_t flip);
 /* Image::load_from_file for float images (texture.cu:170-217), by content:
@@ -613,9 +614,12 @@ enum { SRT_FLIP_NONE = 0, SRT_FLIP_XY = 1, SRT_FLIP_Y = 2 };
 srt_status srt_image_read(const char* path, int32_t* width, int32_t* height, float* rgba, int32_t flip);
 /* load_from_file's 8-bit branch (stbi_load(path, .., 4)): PNG (all colour
  * types and bit depths, palette and tRNS transparency, Adam7; 16-bit
- * samples cut to their high byte) and uncompressed 24 / 32-bit BMP into
- * RGBA8 (rgba: 4*w*h bytes, NULL for the size).  JPEG and other formats
- * return SRT_ERR_UNSUPPORTED.  flip as srt_image_read. */
+ * samples cut to their high byte), uncompressed 24 / 32-bit BMP and
+ * baseline JPEG (grey or YCbCr, any sampling, restart markers; decoded
+ * with an exact IDCT, so samples may differ from stbi_load's integer IDCT
+ * by a few levels) into RGBA8 (rgba: 4*w*h bytes, NULL for the size).
+ * Progressive JPEG and other formats return SRT_ERR_UNSUPPORTED.  flip as
+ * srt_image_read. */
 srt_status srt_image_read_rgba8(const char* path, int32_t* width, int32_t* height, uint8_t* rgba, int32_t flip);
 void srt_renderer_destroy(srt_renderer* r);
 /* Names of the registered passes, ';'-separated (print_registered_pass). */

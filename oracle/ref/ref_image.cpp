@@ -105,6 +105,12 @@ int ref_load_float_image(const char* path, int* w, int* h, float* out)
     return 0;
 }
 
+// stbi_write_jpg of 8-bit pixels (the reference's save_ldr uses quality 100)
+int ref_save_jpg(const char* path, int w, int h, int comp, const unsigned char* px, int quality)
+{
+    return stbi_write_jpg(path, w, h, comp, px, quality) ? 0 : -1;
+}
+
 // Image::load_from_file's 8-bit branch without the flip: stbi_load(.., 4).
 int ref_load_u8_image(const char* path, int* w, int* h, unsigned char* out)
 {

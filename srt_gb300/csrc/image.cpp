@@ -5,6 +5,7 @@
 //   .png  8-bit RGBA, channels clamp(x, 0, 1) * 255 truncated (Image::f_to_u,
 //         texture.cu:11-21); zlib stream of stored (uncompressed) deflate blocks
 //   .bmp  24-bit BGR, same 8-bit conversion
+//   .jpg  baseline JPEG at quality 100 (4:4:4), same 8-bit conversion
 //   .hdr  Radiance RGBE, flat (not run-length encoded) scanlines
 //   .pfm  float RGB
 //   .exr  OpenEXR scanline file, channels B, G, R, A stored as half, no
@@ -33,6 +34,7 @@
 
 #include "common.h"
 #include "inflate.h"
+#include "jpeg.h"
 
 using namespace srt;
 
@@ -749,8 +751,8 @@ extern "C" srt_status srt_image_write(const char* path, int32_t w, int32_t h, co
     clear_error();
     if (!path || !rgba || w <= 0 || h <= 0) return set_error(SRT_ERR_ARG, "bad image arguments");
     const std::string ext = extension(path);
-    if (ext != "png" && ext != "bmp" && ext != "hdr" && ext != "pfm" && ext != "exr")
-        return set_error(SRT_ERR_UNSUPPORTED, "unsupported image format: " + ext + " (png, bmp, hdr, pfm, exr)");
+    if (ext != "png" && ext != "bmp" && ext != "jpg" && ext != "jpeg" && ext != "hdr" && ext != "pfm" && ext != "exr")
+        return set_error(SRT_ERR_UNSUPPORTED, "unsupported image format: " + ext + " (png, bmp, jpg, hdr, pfm, exr)");
     // film pixel of the image's pixel (x, y), y counted from the first stored
     // row; mirror_y: the format stores rows top to bottom
     auto src = [&](int x, int y, bool mirror_y) -> const float* {
@@ -763,7 +765,7 @@ extern "C" srt_status srt_image_write(const char* path, int32_t w, int32_t h, co
     if (ext == "exr") {
         std::vector<uint8_t> exr = encode_exr(w, h, [&](int x, int y) { return src(x, y, true); });
         f.write(reinterpret_cast<const char*>(exr.data()), (std::streamsize)exr.size());
-    } else if (ext == "png" || ext == "bmp") {
+    } else if (ext == "png" || ext == "bmp" || ext == "jpg" || ext == "jpeg") {
         std::vector<uint8_t> px((size_t)w * h * 4);
         for (int y = 0; y < h; ++y)
             for (int x = 0; x < w; ++x) {
@@ -774,6 +776,10 @@ extern "C" srt_status srt_image_write(const char* path, int32_t w, int32_t h, co
         if (ext == "png") {
             std::vector<uint8_t> png = encode_png(w, h, px);
             f.write(reinterpret_cast<const char*>(png.data()), (std::streamsize)png.size());
+        } else if (ext == "jpg" || ext == "jpeg") {
+            // stbi_write_jpg(..., 100) in save_ldr (texture.cu:157-158)
+            std::vector<uint8_t> jpg = jpeg_encode(w, h, px.data(), 100);
+            f.write(reinterpret_cast<const char*>(jpg.data()), (std::streamsize)jpg.size());
         } else {
             const int row = (w * 3 + 3) & ~3;
             const uint32_t size = 54u + (uint32_t)row * (uint32_t)h;
@@ -874,8 +880,10 @@ extern "C" srt_status srt_image_read_rgba8(const char* path, int32_t* width, int
         SRT_TRY(read_png(b, path, w, h, px));
     } else if (b.size() >= 2 && b[0] == 'B' && b[1] == 'M') {
         SRT_TRY(read_bmp(b, path, w, h, px));
+    } else if (b.size() >= 3 && b[0] == 0xFF && b[1] == 0xD8 && b[2] == 0xFF) {
+        SRT_TRY(jpeg_decode(b, path, w, h, px));
     } else {
-        return set_error(SRT_ERR_UNSUPPORTED, std::string(path) + ": not an 8-bit image this library reads (png, bmp)");
+        return set_error(SRT_ERR_UNSUPPORTED, std::string(path) + ": not an 8-bit image this library reads (png, bmp, jpg)");
     }
     *width = w;
     *height = h;

@@ -311,6 +311,28 @@ def png_set():
     np.savez_compressed(os.path.join(OUT, "png.npz"), **out)
 
 
+def jpg_set():
+    """JPEG fixtures written by the reference's stb_image_write and what its
+    stbi_load(.., 4) decodes from them: quality 100 (4:4:4, what save_ldr
+    writes), 75 (4:2:0), grey at 90."""
+    L = _img_lib()
+    h, w = 29, 37
+    yy, xx = np.mgrid[0:h, 0:w]
+    img = np.stack([xx * 6 % 256, yy * 8 % 256, (xx + yy) * 3 % 256, np.full_like(xx, 255)], -1).astype(np.uint8)
+    img[5:12, 5:20] = np.random.default_rng(24).integers(0, 256, size=(7, 15, 4))
+    img[..., 3] = 255
+    out = {"src": img}
+    for name, comp, q in (("q100", 4, 100), ("q75", 3, 75), ("grey90", 1, 90)):
+        px = np.ascontiguousarray(img[..., :comp])
+        path = os.path.join(OUT, f"jpg_{name}.jpg")
+        assert L.ref_save_jpg(path.encode(), w, h, comp, px.ctypes.data_as(C.c_void_p), q) == 0
+        ww, hh = C.c_int(), C.c_int()
+        a = np.zeros((w * h, 4), np.uint8)
+        assert L.ref_load_u8_image(path.encode(), C.byref(ww), C.byref(hh), a.ctypes.data_as(C.c_void_p)) == 0
+        out[name] = a
+    np.savez_compressed(os.path.join(OUT, "jpg.npz"), **out)
+
+
 def _ref_load(L, path):
     w, h = C.c_int(), C.c_int()
     assert L.ref_load_float_image(path.encode(), C.byref(w), C.byref(h), None) == 0
@@ -380,5 +402,6 @@ if __name__ == "__main__":
     pbrt_camera_set()
     image_set()
     png_set()
+    jpg_set()
     scene_set()
     print("golden vectors written to", OUT)

@@ -232,9 +232,9 @@ def test_rgba8_reader_flips_and_own_writers(tmp_path):
     with pytest.raises(S.SrtError) as e:
         S.image_read_rgba8(_fixture("img_none.exr"))
     assert e.value.status == 9
-    (tmp_path / "x.jpg").write_bytes(b"\xff\xd8\xff\xe0" + bytes(64))
+    (tmp_path / "x.tga").write_bytes(bytes(64))
     with pytest.raises(S.SrtError) as e:
-        S.image_read_rgba8(tmp_path / "x.jpg")
+        S.image_read_rgba8(tmp_path / "x.tga")
     assert e.value.status == 9
 
 
@@ -252,3 +252,56 @@ def test_png_bmp_written_by_stb_read_like_stbi(tmp_path):
         assert R.ref_load_u8_image(p, C.byref(ww), C.byref(hh), ref.ctypes.data_as(C.c_void_p)) == 0
         ours, _, _ = S.image_read_rgba8(tmp_path / f"s.{ext}", flip=False)
         assert np.array_equal(ours, ref)
+
+
+@pytest.mark.parametrize("name", ["q100", "q75", "grey90"])
+def test_jpeg_decoder_close_to_stbi_load(name):
+    """Baseline JPEGs written by the reference's stb_image_write: our exact
+    IDCT and triangle chroma filter stay within 2 levels of stbi_load's
+    integer IDCT and upsampler."""
+    z = np.load(os.path.join(GOLDEN, "jpg.npz"))
+    px, w, h = S.image_read_rgba8(_fixture(f"jpg_{name}.jpg"), flip=False)
+    assert (w, h) == (37, 29)
+    d = np.abs(px.astype(int) - z[name].astype(int))
+    assert d.max() <= 2 and d.mean() < 0.5, (d.max(), d.mean())
+
+
+def test_jpeg_writer_round_trip(tmp_path):
+    """srt_image_write(.jpg) is save_ldr's stbi_write_jpg(.., 100): baseline,
+    4:4:4, Annex K tables at quality 100; it reads back within 2 levels."""
+    z = np.load(os.path.join(GOLDEN, "jpg.npz"))
+    src = z["src"]
+    h, w = src.shape[:2]
+    S.image_write(tmp_path / "o.jpg", (src / 255.0).astype(np.float32).reshape(-1, 4), w, h, flip=False)
+    data = (tmp_path / "o.jpg").read_bytes()
+    assert data[:2] == b"\xff\xd8" and data[-2:] == b"\xff\xd9" and b"\xff\xc0" in data
+    want = ((src / 255.0).astype(np.float32) * np.float32(255.0)).astype(np.uint8).reshape(-1, 4)
+    px, _, _ = S.image_read_rgba8(tmp_path / "o.jpg", flip=False)
+    assert np.abs(px[:, :3].astype(int) - want[:, :3]).max() <= 2
+    # progressive and truncated files
+    prog = bytearray(data)
+    k = prog.index(b"\xff\xc0")
+    prog[k + 1] = 0xC2
+    (tmp_path / "p.jpg").write_bytes(bytes(prog))
+    with pytest.raises(S.SrtError) as e:
+        S.image_read_rgba8(tmp_path / "p.jpg")
+    assert e.value.status == 9
+    (tmp_path / "t.jpg").write_bytes(data[:40])
+    with pytest.raises(S.SrtError) as e:
+        S.image_read_rgba8(tmp_path / "t.jpg")
+    assert e.value.status == 8
+
+
+@pytest.mark.skipif(not os.path.exists(REF_IMG), reason="reference image library not built here")
+def test_jpeg_writer_read_by_stbi(tmp_path):
+    R = C.CDLL(REF_IMG)
+    z = np.load(os.path.join(GOLDEN, "jpg.npz"))
+    src = z["src"]
+    h, w = src.shape[:2]
+    S.image_write(tmp_path / "o.jpg", (src / 255.0).astype(np.float32).reshape(-1, 4), w, h, flip=False)
+    ref = np.zeros((w * h, 4), np.uint8)
+    ww, hh = C.c_int(), C.c_int()
+    assert R.ref_load_u8_image(str(tmp_path / "o.jpg").encode(), C.byref(ww), C.byref(hh),
+                               ref.ctypes.data_as(C.c_void_p)) == 0
+    want = ((src / 255.0).astype(np.float32) * np.float32(255.0)).astype(np.uint8).reshape(-1, 4)
+    assert np.abs(ref[:, :3].astype(int) - want[:, :3]).max() <= 2
