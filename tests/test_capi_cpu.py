@@ -190,7 +190,7 @@ def test_image_write_hdr_pfm(tmp_path):
 
 def test_image_write_rejects_other_formats(tmp_path):
     film = _film(4, 4)
-    assert _write(tmp_path / "a.jpg", 4, 4, film, 1) == 9  # SRT_ERR_UNSUPPORTED
+    assert _write(tmp_path / "a.tga", 4, 4, film, 1) == 9  # SRT_ERR_UNSUPPORTED
     assert _write(tmp_path / "a.png", 0, 4, film, 1) == 1  # SRT_ERR_ARG
 
 
