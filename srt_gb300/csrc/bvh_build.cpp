@@ -374,7 +374,7 @@ void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& o
             if (c < 0) continue;
             if (!slot_leaf[s]) {
                 wn.imask |= (uint8_t)(1u << s);
-                wn.meta[s] = (uint8_t)(0x80 | rank);
+                wn.meta[s] = (uint8_t)(kMetaInternal | s);
                 queue.push_back({(int32_t)(child_base + rank), c, p.depth + 1});
                 ++rank;
             }
@@ -389,7 +389,7 @@ void build_wide_bvh(int64_t num_tris, const float* tri9, int threads, WideBvh& o
                 // a leaf: the triangles of the binary subtree (at most kMaxLeaf)
                 uint32_t off = (uint32_t)out.tri_order.size() - tri_base;
                 for (int i = 0; i < cn.rcount; ++i) out.tri_order.push_back(B.idx[cn.rbegin + i]);
-                wn.meta[s] = (uint8_t)((cn.rcount << 5) | off);
+                wn.meta[s] = (uint8_t)((((1u << cn.rcount) - 1u) << 5) | off);
             }
         }
         wn.child_base = child_base;

@@ -30,12 +30,17 @@ namespace srt {
 // 8-wide BVH node with 16-bit quantised child boxes, exactly 128 bytes.
 //   child box lo = origin + q_lo * 2^exp (per axis), hi likewise; the
 //   quantisation is conservative (floor for lo, ceil for hi).
-//   meta[i]: 0 = empty slot; bit 7 set = internal child, its node is
-//   child_base + (meta & 7); otherwise a leaf with count = meta >> 5
-//   (1..3) triangles starting at tri_base + (meta & 31).
+//   meta[i]: the bits slot i sets in the node's hit mask when its box is
+//   hit, as (meta >> 5) << (meta & 31): 0 = empty slot; a leaf of n (1..3)
+//   triangles starting at tri_base + off (off + n <= 24) is
+//   ((1 << n) - 1) << 5 | off (triangle bits 0..23); an internal child is
+//   kMetaInternal | i (bits 3 and 4 set, which no leaf offset has), and the
+//   traversal moves its bit to 24 + (i ^ octant).  Its node is child_base +
+//   the number of internal slots below i.
 // Children sit in slots ordered for octant traversal: a ray whose
 // direction-sign octant is `oct` visits slots in order k ^ oct, k = 0..7,
 // which approximates front-to-back (Ylitie, Karras, Laine, HPG 2017).
+constexpr uint8_t kMetaInternal = 0x38;
 struct alignas(128) WideNode {
     float origin[3];
     int8_t exp[3];

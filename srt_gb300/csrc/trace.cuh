@@ -195,24 +195,24 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     const float cnx = Cx - mx, cfx = Cx + mx;
     const float cny = Cy - my, cfy = Cy + my;
     const float cnz = Cz - mz, cfz = Cz + mz;
-    uint32_t ihits = 0;
-    uint32_t tm = 0;
+    // Each slot's meta byte holds the bits its child sets in the hit mask
+    // (bits 0..23 leaf triangles, 24..31 internal children in octant order),
+    // with internal children's slot index XORed with the octant here, four
+    // bytes at a time: bits 3 and 4 are both set only in internal bytes.
+    const uint32_t oct = r.oct();
+    const uint32_t mlo = w1.z ^ ((((w1.z & (w1.z << 1)) & 0x10101010u) >> 4) * oct);
+    const uint32_t mhi = w1.w ^ ((((w1.w & (w1.w << 1)) & 0x10101010u) >> 4) * oct);
+    uint32_t hitmask = 0;
     auto child = [&](int s, uint32_t wnx, uint32_t wfx, uint32_t wny, uint32_t wfy, uint32_t wnz, uint32_t wfz) {
-        uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * (s & 3))) & 0xffu;
+        const uint32_t meta = ((s < 4 ? mlo : mhi) >> (8 * (s & 3))) & 0xffu;
         int hi = s & 1;
         float nx = fmaf(q23(wnx, hi), Ax, cnx), fx = fmaf(q23(wfx, hi), Ax, cfx);
         float ny = fmaf(q23(wny, hi), Ay, cny), fy = fmaf(q23(wfy, hi), Ay, cfy);
         float nz = fmaf(q23(wnz, hi), Az, cnz), fz = fmaf(q23(wfz, hi), Az, cfz);
         float tn = fmax3(nx, ny, fmaxf(nz, tmin));
         float tf = fmin3(fx, fy, fminf(fz, tmax));
-        bool hit = meta != 0u && tn <= tf * 1.00000024f;
-        if (hit) {
-            if (meta & 0x80u) {
-                ihits |= 1u << (s ^ r.oct());
-            } else {
-                tm |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-            }
-        }
+        // (meta >> 5) << (meta & 31); an empty slot's byte is 0
+        if (tn <= tf * 1.00000024f) hitmask |= __funnelshift_l(0u, meta >> 5, meta);
     };
     const uint4 nqx = __ldg(np + 2 + 3 * ox), fqx = __ldg(np + 5 - 3 * ox);
     const uint4 nqy = __ldg(np + 3 + 3 * oy), fqy = __ldg(np + 6 - 3 * oy);
@@ -222,8 +222,8 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
         const int j = s >> 1;
         child(s, word4(nqx, j), word4(fqx, j), word4(nqy, j), word4(fqy, j), word4(nqz, j), word4(fqz, j));
     }
-    group = make_uint2(w1.x, imask | (ihits << 8));
-    tmask = tm;
+    group = make_uint2(w1.x, imask | ((hitmask >> 24) << 8));
+    tmask = hitmask & 0x00ffffffu;
     tri_base = w1.y;
 }
 
