@@ -1,0 +1,116 @@
+"""The benchmark frame at its full size on the GPU against the oracle's
+megakernel restatement (path_tracer.cu:50-169) with the same per-pixel curand
+streams (GPU only): 64 displaced icospheres of 81,920 triangles plus the
+ground and four quad lights (5,242,890 triangles), 1920x1080, depth 16,
+Russian roulette from depth 4, NEE with MIS.
+
+The GPU renders with its 8-wide quantised BVH and the streaming wavefront
+engine, the oracle with its own binary BVH and one path at a time; a path
+whose FP32 values differ by an ulp at a Russian-roulette or lobe decision
+diverges from there, so per-pixel equality is asked for most pixels, the
+ray counts within 1 %, and, at 256 spp on crops, every pixel's mean within
+3 standard errors of the oracle's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from srt_gb300 import pt_params
+
+pytestmark = pytest.mark.gpu
+
+W, H = 1920, 1080
+
+
+@pytest.fixture(scope="module")
+def frame_scene():
+    import srt_gb300 as S
+    sa = S.procedural("spheres", seed=1, n_spheres=64, subdiv=6)
+    sa.set_aspect(W / H)
+    osc = O.OracleScene(sa.desc(), bvh=True)
+    assert osc.num_triangles == 5_242_890
+    return sa, S.Scene(sa), osc
+
+
+def _render(cuda, sc, params, w=W, h=H):
+    import torch
+    import srt_gb300 as S
+    pt = S.PathTracer(sc, w, h)
+    film = torch.full((w * h, 4), -1.0, dtype=torch.float32, device=cuda)
+    pt.render(film, params)
+    torch.cuda.synchronize()
+    return film.cpu().numpy(), pt.stats()
+
+
+def test_full_frame_matches_oracle_streams(cuda, frame_scene):
+    sa, sc, osc = frame_scene
+    p = pt_params(2, 16, 4, 1, 1, 1)
+    film, st = _render(cuda, sc, p)
+    of, _, _, cnt = osc.render(W, H, p, threads=os.cpu_count() or 1)
+    assert np.all(film[:, 3] == 1.0) and np.all(np.isfinite(film)) and film[:, :3].min() >= 0.0
+    assert st["samples"] == W * H * 2 == cnt[0]
+    assert st["stack_overflows"] == 0
+    assert abs(st["closest_rays"] - cnt[1]) <= 0.01 * cnt[1]
+    assert abs(st["shadow_rays"] - cnt[2]) <= 0.01 * cnt[2]
+    d = np.abs(film[:, :3] - of[:, :3]).max(1)
+    same = d <= 1e-4 * np.maximum(1.0, np.abs(of[:, :3]).max(1))
+    print(f"full frame: {np.mean(same):.4f} of pixels equal to the oracle")
+    assert np.mean(same) > 0.95, np.mean(same)
+    # the frame's mean radiance: paths that diverged still sample the same integral
+    assert abs(film[:, :3].mean() - of[:, :3].mean()) <= 0.01 * of[:, :3].mean()
+
+
+@pytest.fixture(scope="module")
+def frame_256spp(cuda, frame_scene):
+    sa, sc, osc = frame_scene
+    p = pt_params(256, 16, 4, 1, 1, 99)
+    film, st = _render(cuda, sc, p)
+    assert st["samples"] == W * H * 256 and st["stack_overflows"] == 0
+    return film, p
+
+
+# crops of the frame: sphere silhouettes against the ground, a sphere cluster
+# and a mostly lit region (chosen from the oracle's hit counts per 64x64 tile)
+@pytest.mark.parametrize("crop", [(640, 128), (1152, 512), (1152, 768)])
+def test_frame_crops_256spp_within_3_standard_errors(frame_scene, frame_256spp, crop):
+    sa, sc, osc = frame_scene
+    film, p = frame_256spp
+    spp, cw = 256, 48
+    x0, y0 = crop
+    of, s1, s2, cnt = osc.render(W, H, p, crop=(x0, y0, cw, cw), threads=os.cpu_count() or 1)
+    g = film.reshape(H, W, 4)[y0:y0 + cw, x0:x0 + cw, :3].reshape(-1, 3).astype(np.float64)
+    mean = s1 / spp
+    var = np.maximum(s2 / spp - mean ** 2, 0.0)
+    se = np.sqrt(var / spp)
+    diff = np.abs(g - mean)
+    bound = 3.0 * se + 1e-5 * np.maximum(1.0, mean)
+    # identical streams: nearly every pixel is equal, the rest within the noise
+    z = np.where(se > 0, diff / np.where(se > 0, se, 1.0), 0.0)
+    print(f"crop {crop}: {np.mean(np.all(diff <= bound, axis=1)):.4f} within 3 SE, max {z.max():.2f} SE")
+    assert np.mean(np.all(diff <= bound, axis=1)) >= 0.999, z.max()
+    assert cnt[2] > 0  # the crop has lit surface points
+
+
+def test_full_scene_traversal_vs_oracle_bvh(cuda, frame_scene):
+    """Closest-hit and shadow rays through all 5,242,890 triangles: hit
+    triangles equal the oracle's except for rays within 1e-4 of an edge (or
+    ties in t), and visibility agrees away from edges."""
+    import torch
+    from test_gpu_kernels import _check_hits, _random_rays, _t
+    sa, sc, osc = frame_scene
+    rays = _random_rays(1 << 20, -12.0, 12.0, 17)
+    frac = _check_hits(sc, osc, rays, cuda)
+    print(f"full scene: primitive-id mismatch rate {frac:.2e}")
+    assert frac < 1e-3
+    rays[:, 7] = np.random.default_rng(18).uniform(0.1, 20.0, len(rays)).astype(np.float32)
+    vis = torch.zeros(len(rays), dtype=torch.int32, device=cuda)
+    sc.trace_shadow(_t(rays, cuda), vis)
+    torch.cuda.synchronize()
+    ov = osc.trace_shadow(rays)
+    _, edge = osc.trace_closest(rays)
+    safe = edge > 1e-4
+    v = vis.cpu().numpy()
+    assert 0.05 < np.mean(ov) < 0.95  # both outcomes occur
+    assert np.all(v[safe] == ov[safe])
