@@ -224,9 +224,6 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
     J.cam = sc->camera;
     J.film = reinterpret_cast<float4*>(film);
     J.lpath = p->lpath;
-    J.rng_a = p->rng_a;
-    J.rng_b = p->rng_b;
-    J.spp_done = p->spp_done;
     J.pixels_done = p->engine.pixels_done_slot(0);
     J.width = p->width;
     J.height = p->height;

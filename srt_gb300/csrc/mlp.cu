@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_cache_query(const JobRec* __res
                 float3 o = k ? o1 : o0;
                 float4* lp = J.lpath + __float_as_int(b.w);
                 float4 l = *lp;
-                *lp = make_float4(l.x + b.x * o.x, l.y + b.y * o.y, l.z + b.z * o.z, 0.0f);
+                *lp = make_float4(l.x + b.x * o.x, l.y + b.y * o.y, l.z + b.z * o.z, l.w);
             }
         }
     }

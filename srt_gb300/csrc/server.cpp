@@ -30,7 +30,7 @@ struct Job {
     int32_t state = SRT_JOB_QUEUED;
     int slot = -1;
     int64_t bytes = 0;          // job state + server-owned film
-    void* state_buf = nullptr;  // lpath | rng_a | rng_b | spp_done | frame_done
+    void* state_buf = nullptr;  // lpath | frame_done
     float* film = nullptr;
     bool own_film = false;
     double submit_s = 0, admit_s = -1, first_frame_s = -1, done_s = -1;
@@ -42,9 +42,9 @@ size_t frames_bytes(int spp) { return ((size_t)std::max(spp, 1) * 4 + 255) & ~(s
 
 size_t state_bytes(int64_t npix, int spp, bool cache)
 {
-    // lpath 16 + rng_a 16 + rng_b 8 + spp_done 4 per pixel (rounded), frame counters,
-    // and for a cached job its query records (64 B), throughputs (16 B) and counters
-    size_t b = (((size_t)npix * 44 + 255) & ~(size_t)255) + frames_bytes(spp);
+    // lpath 16 per pixel (rounded), frame counters, and for a cached job its
+    // query records (64 B), throughputs (16 B) and counters
+    size_t b = (((size_t)npix * 16 + 255) & ~(size_t)255) + frames_bytes(spp);
     if (cache) b += (size_t)npix * 80 + 256;
     return b;
 }
@@ -99,7 +99,7 @@ struct srt_server {
         }
         char* b = reinterpret_cast<char*>(j.state_buf);
         const size_t n = (size_t)j.npix;
-        const size_t px_bytes = ((size_t)n * 44 + 255) & ~(size_t)255;
+        const size_t px_bytes = ((size_t)n * 16 + 255) & ~(size_t)255;
         int32_t* frame_done = reinterpret_cast<int32_t*>(b + px_bytes);
         SRT_CUDA_TRY(cudaMemsetAsync(frame_done, 0, frames_bytes(spp), stream));
         j.frames_off = px_bytes;
@@ -110,9 +110,6 @@ struct srt_server {
         J.cam.nw = J.cam.nh * ((float)j.desc.width / (float)j.desc.height);
         J.film = reinterpret_cast<float4*>(j.film);
         J.lpath = reinterpret_cast<float4*>(b);
-        J.rng_a = reinterpret_cast<uint4*>(b + n * 16);
-        J.rng_b = reinterpret_cast<uint2*>(b + n * 32);
-        J.spp_done = reinterpret_cast<int32_t*>(b + n * 40);
         J.pixels_done = engine.pixels_done_slot(slot);
         J.frame_done = frame_done;
         J.width = j.desc.width;

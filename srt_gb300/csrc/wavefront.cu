@@ -116,8 +116,7 @@ __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ j
             camera_ray(J.cam, xx, yy, o, d);
             rng.store(ra, rb);
             J.film[pix] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-            J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            J.spp_done[pix] = 0;
+            J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0));  // no sample finished
             if (J.cache.w && (pix % J.cache.train_stride) == J.cache.train_phase)
                 J.cache.t_len[pix / J.cache.train_stride] = 0;
         }
@@ -225,7 +224,7 @@ template <bool kCache>
 __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(const JobRec* __restrict__ jobs, PathQueue q,
                                                     const float4* __restrict__ hits,
                                                     const int32_t* __restrict__ order, PathQueue qn, ShadowQueue sq,
-                                                    int2* __restrict__ done, Counters* ctr, int64_t capacity)
+                                                    DoneQueue done, Counters* ctr, int64_t capacity)
 {
     const int n = (int)min((int64_t)ctr->n_cur, capacity);
     const int stride = gridDim.x * blockDim.x;
@@ -317,7 +316,8 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                         qrec[2] = make_float4(wo.x, wo.y, wo.z, 0.0f);
                         qrec[3] = make_float4(base_color.x, base_color.y, base_color.z, 0.0f);
                     } else {
-                    if (train_pix && depth >= 1 && depth <= kTrainVertices && J.spp_done[pix] == 0) {
+                    if (train_pix && depth >= 1 && depth <= kTrainVertices &&
+                        __float_as_int(J.lpath[pix].w) == 0) {
                         // training vertex: features, arriving throughput, radiance gathered so far
                         int slot = (pix / Cc.train_stride) * kTrainVertices + depth - 1;
                         float4* tr = Cc.t_rec + 4 * (size_t)slot;
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
         if (valid && (L_add.x != 0.0f || L_add.y != 0.0f || L_add.z != 0.0f || !finite3(L_add))) {
             float4* lp = jobs[job].lpath + pix;
             float4 l = *lp;
-            *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, 0.0f);
+            *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, l.w);
         }
         int32_t slot = warp_append(&ctr->n_next, push_next);
         if (push_next) {
@@ -436,13 +436,12 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
         bool fin = valid && terminate;
         slot = warp_append(&ctr->n_done, fin);
         if (fin) {
-            JobRec const& J = jobs[job];
-            J.rng_a[pix] = ra;
-            J.rng_b[pix] = rb;
-            if (slot < capacity)
-                done[slot] = make_int2(job, pix);
-            else
+            if (slot < capacity) {
+                done.rec[2 * (size_t)slot] = ra;
+                done.rec[2 * (size_t)slot + 1] = make_uint4((uint32_t)job, (uint32_t)pix, rb.x, rb.y);
+            } else {
                 atomicAdd(&ctr->overflow_queue, 1);
+            }
         }
     }
 }
@@ -469,7 +468,7 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_shadow(
                 float4 o = sq.o[i], c = sq.c[i];
                 float4* lp = jobs[__float_as_int(c.w)].lpath + __float_as_int(o.w);
                 float4 l = *lp;
-                *lp = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.0f);
+                *lp = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
             }
         });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
@@ -481,7 +480,7 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_shadow(
 
 // Ends the samples of the done pixels (path_tracer.cu:164-165) and starts
 // their next sample (path_tracer.cu:64-68).
-__global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ jobs, const int2* __restrict__ done,
+__global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ jobs, DoneQueue done,
                                                     PathQueue qn, Counters* ctr, int64_t capacity)
 {
     const int n = (int)min((int64_t)ctr->n_done, capacity);
@@ -496,13 +495,14 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
         int32_t* frame_ctr = nullptr;  // progressive-frame counter of the finished sample
         int32_t* pixel_ctr = nullptr;  // finished-pixel counter, when the pixel's last sample ended
         if (i < n) {
-            int2 e = done[i];
-            job = e.x;
-            pix = e.y;
+            const uint4 e = done.rec[2 * (size_t)i + 1];
+            job = (int)e.x;
+            pix = (int)e.y;
             const JobRec& J = jobs[job];
             float4 l = J.lpath[pix];
+            const int spp_done = __float_as_int(l.w);
             const CacheRec& Cc = J.cache;
-            if (Cc.w && (pix % Cc.train_stride) == Cc.train_phase && J.spp_done[pix] == 0) {
+            if (Cc.w && (pix % Cc.train_stride) == Cc.train_phase && spp_done == 0) {
                 // targets of the recorded vertices: radiance gathered after the
                 // vertex divided by the throughput that arrived there
                 const int ts = pix / Cc.train_stride;
@@ -524,13 +524,12 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
                 float s = (float)J.spp;
                 J.film[pix] = make_float4(f.x + l.x / s, f.y + l.y / s, f.z + l.z / s, 1.0f);
             }
-            J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            int k = J.spp_done[pix] + 1;
-            J.spp_done[pix] = k;
+            const int k = spp_done + 1;
+            J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(k));
             if (J.frame_done) frame_ctr = J.frame_done + (k - 1);
             if (k < J.spp) {
                 Rng rng;
-                rng.load(J.rng_a[pix], J.rng_b[pix]);
+                rng.load(done.rec[2 * (size_t)i], make_uint2(e.z, e.w));
                 int ix = pix % J.width, iy = pix / J.width;
                 float xx = ((float)ix + rng.next()) / (float)J.width;
                 float yy = ((float)iy + rng.next()) / (float)J.height;
@@ -634,34 +633,36 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     capacity_ = capacity;
     max_jobs_ = max_jobs;
     const size_t C = (size_t)capacity;
-    size_t per_queue = align_up(C * 16) * 3 + align_up(C * 16) + align_up(C * 8);
-    size_t total = 2 * per_queue + align_up(C * 16) * 3 /*shadow*/ + align_up(C * 16) /*hits*/ +
-                   align_up(C * 4) /*order*/ + align_up(C * 8) /*done*/ + align_up(sizeof(Counters)) + align_up(sizeof(JobRec) * max_jobs) +
-                   align_up(4 * (size_t)max_jobs);
+    // one carve both sizes the buffer (base null) and places the arrays in it
+    auto carve = [&](char* base) {
+        size_t off = 0;
+        auto take = [&](size_t bytes) {
+            char* r = reinterpret_cast<char*>(reinterpret_cast<uintptr_t>(base) + off);
+            off += align_up(bytes);
+            return r;
+        };
+        for (int k = 0; k < 2; ++k) {
+            q_[k].o = (float4*)take(C * 16);
+            q_[k].d = (float4*)take(C * 16);
+            q_[k].beta = (float4*)take(C * 16);
+            q_[k].ra = (uint4*)take(C * 16);
+            q_[k].rb = (uint2*)take(C * 8);
+        }
+        sq_.o = (float4*)take(C * 16);
+        sq_.d = (float4*)take(C * 16);
+        sq_.c = (float4*)take(C * 16);
+        hits_ = (float4*)take(C * 16);
+        order_ = (int32_t*)take(C * 4);
+        done_.rec = (uint4*)take(C * 32);
+        counters_ = (Counters*)take(sizeof(Counters));
+        jobs_ = (JobRec*)take(sizeof(JobRec) * max_jobs);
+        pixels_done_ = (int32_t*)take(4 * (size_t)max_jobs);
+        return off;
+    };
+    const size_t total = carve(nullptr);
     SRT_TRY(buf_.alloc(total, "wavefront queues"));
     bytes_ = total;
-    char* p = buf_.as<char>();
-    auto take = [&](size_t bytes) {
-        char* r = p;
-        p += align_up(bytes);
-        return r;
-    };
-    for (int k = 0; k < 2; ++k) {
-        q_[k].o = (float4*)take(C * 16);
-        q_[k].d = (float4*)take(C * 16);
-        q_[k].beta = (float4*)take(C * 16);
-        q_[k].ra = (uint4*)take(C * 16);
-        q_[k].rb = (uint2*)take(C * 8);
-    }
-    sq_.o = (float4*)take(C * 16);
-    sq_.d = (float4*)take(C * 16);
-    sq_.c = (float4*)take(C * 16);
-    hits_ = (float4*)take(C * 16);
-    order_ = (int32_t*)take(C * 4);
-    done_ = (int2*)take(C * 8);
-    counters_ = (Counters*)take(sizeof(Counters));
-    jobs_ = (JobRec*)take(sizeof(JobRec) * max_jobs);
-    pixels_done_ = (int32_t*)take(4 * (size_t)max_jobs);
+    carve(buf_.as<char>());
     SRT_CUDA_TRY(cudaMemset(counters_, 0, sizeof(Counters)));
     SRT_CUDA_TRY(cudaMemset(jobs_, 0, sizeof(JobRec) * (size_t)max_jobs));  // unused slots read as plain, empty jobs
     SRT_CUDA_TRY(cudaMemset(pixels_done_, 0, 4 * (size_t)max_jobs));
@@ -967,16 +968,13 @@ extern "C" srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t hei
     p->height = height;
     const size_t npix = (size_t)width * height;
     srt_status st = p->engine.init((int64_t)npix, 1);
-    if (st == SRT_OK) st = p->job_buf.alloc(npix * (16 + 16 + 8 + 4) + 1024, "per-pixel path state");
+    if (st == SRT_OK) st = p->job_buf.alloc(npix * 16 + 1024, "per-pixel path state");
     if (st != SRT_OK) {
         delete p;
         return st;
     }
     char* b = p->job_buf.as<char>();
     p->lpath = (float4*)b;
-    p->rng_a = (uint4*)(b + npix * 16);
-    p->rng_b = (uint2*)(b + npix * 32);
-    p->spp_done = (int32_t*)(b + npix * 40);
     *out = p;
     return SRT_OK;
 }
@@ -1011,9 +1009,6 @@ extern "C" srt_status srt_pt_render(srt_pt* p, float* film, const srt_pt_params*
     J.cam = sc->camera;
     J.film = reinterpret_cast<float4*>(film);
     J.lpath = p->lpath;
-    J.rng_a = p->rng_a;
-    J.rng_b = p->rng_b;
-    J.spp_done = p->spp_done;
     J.pixels_done = p->engine.pixels_done_slot(0);
     J.width = p->width;
     J.height = p->height;

@@ -42,10 +42,8 @@ struct JobRec {
     SceneView scene;
     CameraRec cam;
     float4* film;        // caller film, float4[w*h], row-major idx = iy*w + ix
-    float4* lpath;       // per-pixel radiance of the sample in flight
-    uint4* rng_a;        // per-pixel XORWOW state v[0..3]
-    uint2* rng_b;        // per-pixel XORWOW state (v[4], d)
-    int32_t* spp_done;   // per-pixel finished samples
+    float4* lpath;       // per pixel: radiance of the sample in flight (xyz) and
+                         // the pixel's finished samples (w, int bits)
     int32_t* pixels_done;  // pixels that finished every sample (one int)
     int32_t* frame_done;   // [spp]: pixels that finished sample k (progressive frames), or null
     int32_t width, height, npix;
@@ -59,6 +57,13 @@ struct PathQueue {
     float4* beta;  // throughput, flags: depth bits 0-7, specular bit 8, job bits 16-31
     uint4* ra;     // rng state
     uint2* rb;
+};
+
+// A path that ended in this iteration: its pixel's RNG state travels with it
+// from k_shade to k_regen (stored as two 16-byte words: ra, then job, pixel,
+// rb.x, rb.y).
+struct DoneQueue {
+    uint4* rec;  // 2 per entry
 };
 
 struct ShadowQueue {
@@ -142,7 +147,7 @@ private:
     ShadowQueue sq_{};
     float4* hits_ = nullptr;
     int32_t* order_ = nullptr;  // queue indices in shading order (hits, then misses)
-    int2* done_ = nullptr;
+    DoneQueue done_{};
     Counters* counters_ = nullptr;
     JobRec* jobs_ = nullptr;
     int32_t* pixels_done_ = nullptr;
@@ -167,9 +172,6 @@ struct srt_pt {
     srt::Engine engine;
     srt::DeviceBuffer job_buf;
     float4* lpath = nullptr;
-    uint4* rng_a = nullptr;
-    uint2* rng_b = nullptr;
-    int32_t* spp_done = nullptr;
     srt_pt_stats stats{};
     srt::DeviceBuffer cache_buf;  // radiance-cache buffers, sized on first cached render
     int64_t cache_train = 0;
