@@ -21,7 +21,8 @@ per ray from a second frame of the same seed with the counting traversal
 kernels), `traffic` scaled from the DRAM bytes per ray of one ncu capture
 (profiles/<kernel>_dram.json); `cache` (learned-cache time to the plain
 tracer's 64-spp relMSE, 1280x720), `serving` (a 10 s Poisson run at 20
-jobs/s), `cpu_baseline`.  `--no-cache`, `--no-serving`,
+jobs/s), `bxdf` (the Disney BSDF batch of 2^20 points), `cornell` (the
+Cornell box at 512x512, 16 spp, depth 8), `cpu_baseline`.  `--no-cache`, `--no-serving`,
 `--no-cpu-baseline` skip those parts; `--profile-case` runs the short
 case the ncu captures use.
 """
@@ -245,6 +246,52 @@ def bxdf_eval_bench(S, n=1 << 20, launches=20, cpu=True):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": round(n / dt / 1e6, 2), "unit": "Mpoints/s", "cores": threads,
                                "kind": "port", "sample": "the same 2^20 points, oracle FP32 BxDF"}
+    return out
+
+
+def cornell_eval(S, steps=10, warmup=3, cpu=True):
+    """The Cornell box at 512x512, 16 spp, depth 8, Russian roulette from
+    depth 3, NEE with MIS: the small-scene configuration (36 triangles, the
+    BVH stays in L1/L2, so traversal is latency-bound).  Kernel time from CUDA
+    events around `steps` renders on the launching stream; the scene is tiny,
+    so there is no L2 flush.  CPU baseline: the oracle's megakernel
+    restatement on all host threads, whole frame."""
+    import torch
+    w = h = 512
+    spp, depth, rr = 16, 8, 3
+    arrays = S.procedural("cornell")
+    arrays.set_aspect(1.0)
+    scene = S.Scene(arrays)
+    pt = S.PathTracer(scene, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    p = S.pt_params(spp, depth, rr, 1, 1, SEED)
+    for i in range(warmup):
+        p.seed = SEED + 100 + i
+        pt.render(film, p, stream)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for i in range(steps):
+        p.seed = SEED + i
+        pt.render(film, p, stream)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    st = pt.stats()
+    out = {"workload": "Cornell box, 36 triangles, 512x512, 16 spp, depth 8, rr 3, NEE + MIS",
+           "msamples_per_s": round(w * h * spp / (ms / 1e3) / 1e6, 1), "ms_per_frame": round(ms, 3),
+           "closest_rays_per_frame": st["closest_rays"], "shadow_rays_per_frame": st["shadow_rays"]}
+    if cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        osc = O.OracleScene(arrays.desc(), bvh=True)
+        t0 = time.perf_counter()
+        osc.render(w, h, p, threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(w * h * spp / dt / 1e6, 3), "unit": "Msamples/s", "cores": threads,
+                               "kind": "port", "sample": "whole 512x512 frame at 16 spp, oracle CPU BVH"}
+    pt.close()
     return out
 
 
@@ -498,6 +545,7 @@ def main():
                               "iterations": st["iterations"]},
         }
         line["bxdf"] = bxdf_eval_bench(S, cpu=not args.no_cpu_baseline)
+        line["cornell"] = cornell_eval(S, cpu=not args.no_cpu_baseline)
         if not args.no_cache:
             line["cache"] = cache_eval(S, arrays, scene)
         if not args.no_serving:
