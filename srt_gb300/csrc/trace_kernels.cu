@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace_s
         n, counter, st, overflow, cnt,
         [&](int64_t i, TravState& s, Stack& stk) {
             float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
-            trav_init(s, S.nodes, S.tris, f3(a), f3(b), a.w, b.w, stk);
+            trav_init(s, S.nodes, S.tris, f3(a), f3(b), a.w, b.w, stk, SRT_SHADOW_FAR_FIRST != 0);
         },
         [&](int64_t i, const TravState& s, bool fin) {
             if (fin) visible[i] = s.tri >= 0 ? 0 : 1;

@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_shadow(
         [&](int64_t i, TravState& s, Stack& stk) {
             float4 o = sq.o[i], d = sq.d[i];
             const SceneView& S = jobs[__float_as_int(sq.c[i].w)].scene;
-            trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, d.w, stk);
+            trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, d.w, stk, SRT_SHADOW_FAR_FIRST != 0);
         },
         [&](int64_t i, const TravState& s, bool fin) {
             if (fin && s.tri < 0) {
