@@ -13,18 +13,21 @@ back to pinned host memory every step.
 Multi-GPU runs (torchrun) render independent replicas: each rank renders
 the full frame, value = all ranks' samples / max rank time (weak scaling).
 `--impl reference` times the reference's path-tracing algorithm on the
-host cores (the oracle's CPU restatement) on a bounded crop.
+host cores (the oracle's CPU restatement, which loads only the oracle
+library) on a seeded uniform sample of the frame's pixels at the full 64 spp.
 
 Extra keys: `roofline` for the kernel with the most device time in a
-timed profile frame (CUDA events around the production kernels; the work
-per ray from a second frame of the same seed with the counting traversal
-kernels), `traffic` scaled from the DRAM bytes per ray of one ncu capture
-(profiles/<kernel>_dram.json); `cache` (learned-cache time to the plain
-tracer's 64-spp relMSE, 1280x720), `serving` (a 10 s Poisson run at 20
-jobs/s), `bxdf` (the Disney BSDF batch of 2^20 points), `cornell` (the
-Cornell box at 512x512, 16 spp, depth 8), `cpu_baseline`.  `--no-cache`, `--no-serving`,
-`--no-cpu-baseline` skip those parts; `--profile-case` runs the short
-case the ncu captures use.
+timed profile frame (CUDA events around the production kernels): achieved =
+the per-ray bytes of the scope table (40 B ray + hit, plus the BVH traffic
+measured by ncu, profiles/<kernel>_dram.json) / launch time, with the
+logical node-and-triangle fetch figure beside it (`l2_level`) and the ncu
+counters that bound the kernel (`limiter`); `cache` (learned-cache time to
+the plain tracer's 64-spp relMSE, 1280x720), `serving` (Poisson arrivals at
+several rates under a 150 GB budget), `bxdf` (the Disney BSDF batch of 2^20
+points, with its FP64 parity), `cornell` (the Cornell box at 512x512, 16 spp,
+depth 8, with its roofline), `cpu_baseline`.  `--no-cache`, `--no-serving`,
+`--no-cpu-baseline` skip those parts; `--profile-case spheres|cornell` runs
+the short case the ncu captures use.
 """
 from __future__ import annotations
 
@@ -126,80 +129,115 @@ def build_scene(S):
     return arrays
 
 
-def cpu_baseline(arrays, steps=1, budget_s=20.0):
-    """The oracle's megakernel restatement on the host cores, on a crop of
-    the same frame (bounded to about `budget_s` seconds of CPU work)."""
+def cpu_baseline(steps=1, budget_s=20.0, warmup=0):
+    """The oracle's megakernel restatement (path_tracer.cu:50-169, own CPU
+    BVH) on all host cores, on a seeded uniform sample of the frame's pixels
+    at the full 64 spp and depth 16, so a sample's cost follows the frame's
+    mix of environment and surface pixels.  The scene is built inside the
+    oracle library from the same generator source: no CUDA library is
+    loaded.  About `budget_s` seconds of CPU work in all."""
+    import numpy as np
     from oracle import oracle as O
-    import srt_gb300 as S
     threads = os.cpu_count() or 1
-    osc = O.OracleScene(arrays.desc())
     t0 = time.perf_counter()
-    osc.build_bvh()
+    osc = O.OracleScene.procedural("spheres", seed=SEED, n_spheres=N_SPHERES, subdiv=SUBDIV, aspect=W / H, bvh=True)
     build_s = time.perf_counter() - t0
-    # calibrate on a small crop, then size the crop to the budget
-    cw = ch = 32
-    spp = 1
-    p = S.pt_params(spp, MAX_DEPTH, RR_DEPTH, 1, 1, SEED)
-    x0, y0 = (W - cw) // 2, (H - ch) // 2
+    order = np.random.default_rng(SEED).permutation(W * H).astype(np.int32)
+    # calibrate on 1024 pixels, then size the per-step sample to the budget
     t0 = time.perf_counter()
-    osc.render(W, H, p, crop=(x0, y0, cw, ch), threads=threads)
-    dt = max(time.perf_counter() - t0, 1e-3)
-    rate = cw * ch * spp / dt
-    target = rate * budget_s / max(1, steps)
-    side = int(max(32, min(512, (target / 4) ** 0.5)))
-    spp = 4
-    x0, y0 = (W - side) // 2, (H - side) // 2
-    p = S.pt_params(spp, MAX_DEPTH, RR_DEPTH, 1, 1, SEED)
+    osc.render_pixels(W, H, O.pt_params(SPP, MAX_DEPTH, RR_DEPTH, 1, 1, SEED), order[:1024], threads=threads)
+    rate = 1024 * SPP / max(time.perf_counter() - t0, 1e-3)
+    npix = int(max(1024, min(W * H, rate * budget_s / max(1, steps + warmup) / SPP)))
+    pix = np.sort(order[:npix])
+    for i in range(warmup):
+        osc.render_pixels(W, H, O.pt_params(SPP, MAX_DEPTH, RR_DEPTH, 1, 1, SEED + 2000 + i), pix, threads=threads)
     times = []
-    for _ in range(steps):
+    for i in range(steps):
         t0 = time.perf_counter()
-        osc.render(W, H, p, crop=(x0, y0, side, side), threads=threads)
+        osc.render_pixels(W, H, O.pt_params(SPP, MAX_DEPTH, RR_DEPTH, 1, 1, SEED + i), pix, threads=threads)
         times.append(time.perf_counter() - t0)
-    value = side * side * spp * len(times) / sum(times) / 1e6
+    value = npix * SPP * len(times) / sum(times) / 1e6
     return {"value": round(value, 4), "unit": "Msamples/s", "cores": threads, "kind": "port",
-            "sample": f"centre crop {side}x{side} of the {W}x{H} frame, {spp} spp, depth {MAX_DEPTH}, "
-                      f"oracle CPU BVH (build {build_s:.1f}s, not timed), {threads} threads"}
+            "sample": f"{npix} pixels drawn uniformly (seeded) from the {W}x{H} frame, {SPP} spp each, depth "
+                      f"{MAX_DEPTH}, per step; oracle CPU BVH (build {build_s:.1f}s, not timed), {threads} threads"}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle's CPU restatement of the path tracer on
+    the host cores, same metric and workload (a bounded pixel sample per
+    step).  Only rank 0 works; nothing of the CUDA library is loaded."""
     if rank != 0:
         return
-    import srt_gb300 as S
-    arrays = build_scene(S)
     steps = max(1, args.steps)
-    cb = cpu_baseline(arrays, steps=steps, budget_s=min(60.0, 12.0 * steps))
+    warmup = min(1, max(0, args.warmup))
+    cb = cpu_baseline(steps=steps, budget_s=min(120.0, 6.0 * (steps + warmup)), warmup=warmup)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "Msamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict(None), "cpu_baseline": cb,
+            "config": config_dict(), "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def config_dict(info):
-    d = {"workload": "5.2M-triangle synthetic scene (64 icospheres subdiv 6, value-noise displaced), "
-                     "plain wavefront PT FP32", "width": W, "height": H, "spp": SPP, "max_depth": MAX_DEPTH,
-         "rr_depth": RR_DEPTH, "nee": True, "mis": True, "rng": "curand XORWOW per pixel",
-         "l2": "scene larger than L2 (no flush between steps)"}
-    if info:
-        d["triangles"] = info["num_triangles"]
-        d["scene_mb"] = round(info["device_bytes"] / 2 ** 20, 1)
-        d["bvh_nodes"] = info["num_nodes"]
-        d["bvh_build_s"] = round(info["build_ms"] / 1000, 2)
-    return d
+def config_dict():
+    """The workload definition, identical in both arms."""
+    return {"workload": "5.2M-triangle synthetic scene (64 icospheres subdiv 6, value-noise displaced), "
+                        "plain wavefront PT FP32", "width": W, "height": H, "spp": SPP, "max_depth": MAX_DEPTH,
+            "rr_depth": RR_DEPTH, "nee": True, "mis": True, "rng": "curand XORWOW per pixel",
+            "l2": "scene larger than L2 (no flush between steps)"}
 
 
-def measured_traffic(kernel, rays_per_launch):
-    """DRAM bytes per launch of `kernel` scaled from one ncu capture: the
-    per-ray dram__bytes_read.sum + dram__bytes_write.sum of a captured launch
-    (profiles/<kernel>_dram.json, written from the capture) times the rays of
-    an average benchmark launch."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_dram.json")
+def scene_dict(info):
+    return {"triangles": info["num_triangles"], "scene_mb": round(info["device_bytes"] / 2 ** 20, 1),
+            "bvh_nodes": info["num_nodes"], "bvh_build_s": round(info["build_ms"] / 1000, 2)}
+
+
+def profile_record(name):
+    """One ncu capture's summary (profiles/<name>_dram.json): DRAM bytes per
+    ray (dram__bytes_read.sum + dram__bytes_write.sum of a captured launch /
+    its rays) and the counters that bound the kernel."""
+    path = os.path.join(ROOT, "profiles", f"{name}_dram.json")
     if not os.path.exists(path):
-        return None, None
+        return None
     with open(path) as f:
-        d = json.load(f)
-    return int(d["dram_bytes_per_ray"] * rays_per_launch), d["capture"]
+        return json.load(f)
+
+
+def bxdf_fp64_parity(S, O, normal, wo, color, params, rnd):
+    """The kernel's f and pdf at its own sampled direction against the FP64
+    evaluation of the same formulas (the oracle's FP64 restatement) on
+    device inputs: fraction of sampled points beyond 1e-5 relative and the
+    error quantiles; the reference's own FP32 formulas (the oracle's FP32
+    restatement, bit-identical to the reference's bxdf.h on the golden
+    vectors) measured the same way beside it."""
+    import numpy as np
+    import torch
+    n = normal.shape[0]
+    dev = normal.device
+    wi = torch.empty((n, 3), dtype=torch.float32, device=dev)
+    f = torch.empty((n, 3), dtype=torch.float32, device=dev)
+    pdf = torch.empty(n, dtype=torch.float32, device=dev)
+    delta = torch.empty(n, dtype=torch.int32, device=dev)
+    S.bxdf_sample(S.BXDF_DISNEY, normal, wo, color, params, rnd, wi, f, pdf, delta)
+    torch.cuda.synchronize()
+    h = [t.cpu().numpy() for t in (normal, wo, color, params, rnd, wi, f, pdf)]
+    nrm, w_o, col, prm, r2, wi_, f_, pdf_ = h
+
+    def rel(fa, pa, fb, pb):
+        ef = (np.abs(fa - fb) / np.maximum(np.abs(fb), 1e-20)).max(1)
+        return np.maximum(ef, np.abs(pa - pb) / np.maximum(np.abs(pb), 1e-20))
+
+    ok = pdf_ > 0
+    f64, p64 = O.bxdf_eval_pdf(64, S.BXDF_DISNEY, nrm, w_o, col, prm, wi_.astype(np.float64))
+    r = rel(f_[ok], pdf_[ok], f64[ok], p64[ok])
+    w32, f32, p32, _ = O.bxdf_sample(32, S.BXDF_DISNEY, nrm, w_o, col, prm, r2, threads=os.cpu_count() or 1)
+    ok32 = p32 > 0
+    f64b, p64b = O.bxdf_eval_pdf(64, S.BXDF_DISNEY, nrm, w_o, col, prm, w32)
+    rr = rel(f32[ok32], p32[ok32], f64b[ok32], p64b[ok32])
+    q = [0.5, 0.9, 0.99, 0.999]
+    return {"sampled_points": int(ok.sum()), "frac_beyond_1e-5": round(float(np.mean(r > 1e-5)), 5),
+            "rel_err_quantiles": {str(k): float(v) for k, v in zip(q, np.quantile(r, q))},
+            "reference_fp32_frac_beyond_1e-5": round(float(np.mean(rr > 1e-5)), 5)}
 
 
 def bxdf_eval_bench(S, n=1 << 20, launches=20, cpu=True):
@@ -208,9 +246,11 @@ def bxdf_eval_bench(S, n=1 << 20, launches=20, cpu=True):
     the config-0 definition; kernel time from CUDA events per launch with
     L2 flushed between launches.  Algorithmic bytes per point = inputs
     (normal, wo, colour: 36 B; 12 parameters: 48 B; 2 uniforms: 8 B) +
-    outputs (wi, f: 24 B; pdf, delta: 8 B) = 124 B.  CPU baseline: the
-    oracle's FP32 restatement (bit-identical to the reference's bxdf.h on
-    the golden vectors) on all host threads."""
+    outputs (wi, f: 24 B; pdf, delta: 8 B) = 124 B.  CPU leg: the oracle's
+    FP32 restatement (bit-identical to the reference's bxdf.h on the golden
+    vectors) on all host threads, and the FP64 parity of the kernel's
+    values on the same points (world frame) and with the shading frame
+    exact (normal = +z)."""
     import torch
     dev = torch.device("cuda")
     f32 = dict(dtype=torch.float32, device=dev)
@@ -238,6 +278,7 @@ def bxdf_eval_bench(S, n=1 << 20, launches=20, cpu=True):
                         "unit": "GB/s", "frac": round(gbs / peak, 4), "alg_bytes_per_point": 124},
            "l2": "flushed (256 MB write) before every launch"}
     if cpu:
+        import numpy as np
         from oracle import oracle as O
         threads = os.cpu_count() or 1
         nrm, w_o, col, prm, r4 = O.bxdf_inputs(0, n)
@@ -246,7 +287,47 @@ def bxdf_eval_bench(S, n=1 << 20, launches=20, cpu=True):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": round(n / dt / 1e6, 2), "unit": "Mpoints/s", "cores": threads,
                                "kind": "port", "sample": "the same 2^20 points, oracle FP32 BxDF"}
+        par = {"world_frame": bxdf_fp64_parity(S, O, normal, wo, color, params, rnd)}
+        # exact shading frame: normal = +z, wo uniform on the upper hemisphere
+        g = np.random.default_rng(11)
+        v = g.normal(size=(n, 3))
+        v[:, 2] = np.abs(v[:, 2]) + 1e-3
+        v = (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+        nz = torch.zeros((n, 3), **f32)
+        nz[:, 2] = 1.0
+        par["local_frame"] = bxdf_fp64_parity(S, O, nz, torch.from_numpy(v).to(dev), color, params, rnd)
+        out["fp64_parity"] = par
     return out
+
+
+KERNELS = ["k_closest", "k_shade", "k_shadow", "k_regen", "k_advance"]
+# queue bytes a closest-hit ray moves in k_closest (origin 16 B, direction 16 B,
+# job word 4 B in; hit record 16 B out)
+CLOSEST_QUEUE_BYTES = 52
+
+
+def kernel_bytes(st, hist, npix):
+    """Algorithmic bytes of one frame per kernel, from the frame's exact
+    counts and the queue layout (wavefront.cuh): R closest rays (H of them
+    hits), Sh shadow rays, N samples over npix pixels.
+      k_closest (+ k_order): ray 32 B + job word 4 B in, hit 16 B out; order
+        pass 4 B in, 4 B out (BVH nodes and triangles are not included: they
+        come from ncu's DRAM bytes where the scene exceeds L2)
+      k_shade: order index 4 B + hit 16 B + path state 72 B in per ray; per
+        hit the triangle 48 B, instance 16 B, material 80 B; per shadow ray
+        the light triangle 48 B in and the shadow record 48 B out; 72 B out
+        per continuing path, 32 B per ended sample, 32 B radiance update per
+        miss
+      k_shadow: 48 B in + 32 B radiance update per ray
+      k_regen: done record 32 B + radiance 32 B + film 32 B per sample, 72 B
+        per next-sample camera ray"""
+    R, Sh, N = st["closest_rays"], st["shadow_rays"], st["samples"]
+    Hh = int(hist[:, 1].sum())
+    return {"k_closest": R * (CLOSEST_QUEUE_BYTES + 8),
+            "k_shade": R * 92 + Hh * 144 + Sh * 96 + (R - N) * 72 + N * 32 + (R - Hh) * 32,
+            "k_shadow": Sh * 80,
+            "k_regen": N * 96 + (N - npix) * 72,
+            "k_advance": 0}
 
 
 def cornell_eval(S, steps=10, warmup=3, cpu=True):
@@ -254,8 +335,11 @@ def cornell_eval(S, steps=10, warmup=3, cpu=True):
     depth 3, NEE with MIS: the small-scene configuration (36 triangles, the
     BVH stays in L1/L2, so traversal is latency-bound).  Kernel time from CUDA
     events around `steps` renders on the launching stream; the scene is tiny,
-    so there is no L2 flush.  CPU baseline: the oracle's megakernel
-    restatement on all host threads, whole frame."""
+    so there is no L2 flush.  Roofline: the kernel with the most device time
+    in a timed profile frame (event timestamps around the production
+    kernels), achieved = its algorithmic bytes (kernel_bytes) / its time.
+    CPU baseline: the oracle's megakernel restatement on all host threads,
+    whole frame."""
     import torch
     w = h = 512
     spp, depth, rr = 16, 8, 3
@@ -279,9 +363,35 @@ def cornell_eval(S, steps=10, warmup=3, cpu=True):
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / steps
     st = pt.stats()
+    hist = pt.iteration_counts()
+    # one frame of the same seed with timestamps around the production kernels
+    p.seed = SEED
+    pt.set_profiling(2)
+    pt.render(film, p, stream)
+    kms = dict(zip(KERNELS, pt.stats()["kernel_ms"]))
+    pt.set_profiling(0)
+    top = max(kms, key=kms.get)
+    alg = kernel_bytes(st, hist, w * h)
+    peak, peak_kind = peaks()
+    achieved = alg[top] / (kms[top] / 1e3) / 1e9
+    iters = max(1, st["iterations"])
+    rec = profile_record(f"cornell_{top}")
+    traffic = None
+    if rec:
+        # DRAM bytes per algorithmic byte of the captured launch, scaled to the average launch
+        traffic = int(rec["dram_bytes_per_alg_byte"] * (alg[top] / iters))
     out = {"workload": "Cornell box, 36 triangles, 512x512, 16 spp, depth 8, rr 3, NEE + MIS",
            "msamples_per_s": round(w * h * spp / (ms / 1e3) / 1e6, 1), "ms_per_frame": round(ms, 3),
-           "closest_rays_per_frame": st["closest_rays"], "shadow_rays_per_frame": st["shadow_rays"]}
+           "closest_rays_per_frame": st["closest_rays"], "shadow_rays_per_frame": st["shadow_rays"],
+           "iterations": st["iterations"],
+           "profile_frame_kernel_ms": {k: round(v, 3) for k, v in kms.items()},
+           "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak,
+                        "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                        "traffic": traffic, "traffic_source": rec["capture"] if rec else None,
+                        "launches": iters, "per_launch_ms": round(kms[top] / iters, 5),
+                        "alg_bytes_per_launch": int(alg[top] / iters),
+                        "limiter": rec.get("limiter") if rec else None,
+                        "alg_bytes_per_sample": round(sum(alg.values()) / (w * h * spp), 1)}}
     if cpu:
         from oracle import oracle as O
         threads = os.cpu_count() or 1
@@ -372,28 +482,50 @@ def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_s
             "speedup_vs_plain64": None if t_reach is None else round(t_plain / t_reach, 3)}
 
 
-def serving_eval(S, scene_big, rate=20.0, duration=10.0):
-    """Short serving run (Poisson arrivals at `rate` jobs/s for `duration` s)."""
+def serving_eval(S, rates=(5.0, 20.0, 50.0), duration=30.0):
+    """Render serving (config 4): Poisson arrivals at each rate for
+    `duration` s under a 150 GB HBM budget, the job mix of serve_bench
+    (resolution, spp, scene, plain / cached); p50 / p99 job latency, first
+    progressive frame and frame interval, and Msamples/s per rate."""
     from srt_gb300 import serve_bench as SB
     scenes = SB.build_scenes(S, n_variants=1, cache_frames=30)
-    out = SB.run_rate(S, scenes, rate, duration)
-    out["mix"] = "res {256^2,512^2,1024^2,1920x1080} x spp {1,4,16,64} x {cornell, 5.2M spheres} x {plain, cached}"
-    return out
+    table = [SB.run_rate(S, scenes, r, duration) for r in rates]
+    return {"mix": "res {256^2,512^2,1024^2,1920x1080} x spp {1,4,16,64} x {cornell, 5.2M spheres} x "
+                   "{plain, cached (network trained beforehand, frozen)}",
+            "budget_gb": 150, "duration_s": duration, "rates": table}
 
 
-def profile_case():
-    """The benchmark scene (392 MB resident, larger than L2) at 1920x1080,
-    for ncu.  Frame A: 1 spp with max depth 2, so the first closest-hit
-    launch traces the 2,073,600 camera rays and the second the first-bounce
-    rays (their count is printed), the first shadow launch the NEE rays of
-    the primary hits.  Frame B: 1 spp at the benchmark's depth.  A few
-    hundred launches in all; run it with SRT_NO_GRAPH=1 so that ncu sees the
-    same kernels as separate launches."""
+def profile_case(which="spheres"):
+    """Short cases for ncu.  spheres: the benchmark scene (392 MB resident,
+    larger than L2) at 1920x1080.  Frame A: 1 spp with max depth 2, so the
+    first closest-hit launch traces the 2,073,600 camera rays and the second
+    the first-bounce rays (their count is printed), the first shadow launch
+    the NEE rays of the primary hits.  Frame B: 1 spp at the benchmark's
+    depth.  cornell: one frame of the Cornell workload (512x512, 16 spp,
+    depth 8).  Every kernel is launched directly (no graph), so ncu sees each
+    launch; a few hundred launches in all."""
     import torch
     import srt_gb300 as S
+    if which == "cornell":
+        arrays = S.procedural("cornell")
+        arrays.set_aspect(1.0)
+        scene = S.Scene(arrays)
+        pt = S.PathTracer(scene, 512, 512)
+        pt.set_launch_mode(S.LAUNCH_DIRECT)
+        film = torch.zeros((512 * 512, 4), dtype=torch.float32, device="cuda")
+        pt.render(film, S.pt_params(16, 8, 3, 1, 1, SEED))
+        torch.cuda.synchronize()
+        st = pt.stats()
+        hist = pt.iteration_counts()
+        print(json.dumps({"profile_case": "cornell 512x512x16spp", "closest_rays": st["closest_rays"],
+                          "shadow_rays": st["shadow_rays"], "iterations": st["iterations"],
+                          "per_iteration": hist[:8].tolist(),
+                          "kernel_bytes": kernel_bytes(st, hist, 512 * 512)}))
+        return
     arrays = build_scene(S)
     scene = S.Scene(arrays)
     pt = S.PathTracer(scene, W, H)
+    pt.set_launch_mode(S.LAUNCH_DIRECT)
     film = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
     pt.render(film, S.pt_params(1, 2, RR_DEPTH, 1, 1, 0))
     torch.cuda.synchronize()
@@ -416,12 +548,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cache", action="store_true", help="skip the learned-cache workload")
-    ap.add_argument("--no-serving", action="store_true", help="skip the short serving run")
-    ap.add_argument("--profile-case", action="store_true",
-                    help="short run of the same scene (1 spp, two frames) for ncu captures")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--serving-rates", default="5,20,50", help="Poisson arrival rates (jobs/s) of the sweep")
+    ap.add_argument("--serving-duration", type=float, default=30.0, help="seconds of arrivals per rate")
+    ap.add_argument("--profile-case", nargs="?", const="spheres", default=None, choices=["spheres", "cornell"],
+                    help="short run for ncu captures (direct launches)")
     args = ap.parse_args()
     if args.profile_case:
-        profile_case()
+        profile_case(args.profile_case)
         return
 
     rank = int(os.environ.get("RANK", "0"))
@@ -479,7 +613,7 @@ def main():
 
     # ---- end to end through the C ABI with host buffers -----------------
     host_film = torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True)
-    h2d = C_PARAM_BYTES = 32 + 48  # srt_pt_params + srt_camera_desc handed over per frame
+    h2d = 32 + 48  # srt_pt_params + srt_camera_desc handed over per frame
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
@@ -503,43 +637,54 @@ def main():
     pt.render(film, params, stream)
     st_t = pt.stats()
     pt.set_profiling(0)
-    names = ["k_closest", "k_shade", "k_shadow", "k_regen", "k_advance"]
-    kms = dict(zip(names, st_t["kernel_ms"]))
+    kms = dict(zip(KERNELS, st_t["kernel_ms"]))
     top = max(kms, key=kms.get)
-    # algorithmic bytes: per ray the ray (24 B) in and the hit (16 B) out, plus
-    # the BVH nodes (128 B) and triangles (48 B) the traversal fetches
-    if top == "k_shadow":
-        rays, nodes, tris = st["shadow_rays"], st["shadow_nodes"], st["shadow_tris"]
-        per_ray = 44
-    else:
-        rays, nodes, tris = st["closest_rays"], st["closest_nodes"], st["closest_tris"]
-        per_ray = 40
-    alg_bytes = rays * per_ray + nodes * 128 + tris * 48
     iters = max(1, st["iterations"])
-    traffic, traffic_src = measured_traffic(top, rays / iters)
-    achieved = alg_bytes / (kms[top] / 1e3) / 1e9 if kms[top] > 0 else 0.0
+    if top == "k_shadow":
+        rays, nodes, tris, per_ray = st["shadow_rays"], st["shadow_nodes"], st["shadow_tris"], 44
+        queue = 48
+    else:
+        rays, nodes, tris, per_ray = st["closest_rays"], st["closest_nodes"], st["closest_tris"], 40
+        queue = CLOSEST_QUEUE_BYTES
     peak, peak_kind = peaks()
+    # algorithmic bytes per ray (the scope table): the ray and its hit
+    # (per_ray) plus the BVH traffic ncu measured in DRAM per ray (its DRAM
+    # bytes per ray less the queue bytes the kernel moves per ray)
+    rec = profile_record(top)
+    launch_ms = kms[top] / iters
+    rays_per_launch = rays / iters
+    roof = {"bound": "hbm", "kernel": top, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "launches": iters, "per_launch_ms": round(launch_ms, 4)}
+    if rec:
+        alg_per_ray = per_ray + max(0.0, rec["dram_bytes_per_ray"] - queue)
+        achieved = alg_per_ray * rays_per_launch / (launch_ms / 1e3) / 1e9
+        roof.update({"achieved": round(achieved, 1), "frac": round(achieved / peak, 4),
+                     "traffic": int(rec["dram_bytes_per_ray"] * rays_per_launch),
+                     "traffic_source": rec["capture"], "alg_bytes_per_ray": round(alg_per_ray, 1),
+                     "alg_bytes_per_launch": int(alg_per_ray * rays_per_launch),
+                     "limiter": rec.get("limiter")})
+    # the logical figure: every node (128 B) and triangle (48 B) the traversal
+    # fetches, wherever it is served from (L1, L2 or DRAM)
+    logical = rays * per_ray + nodes * 128 + tris * 48
+    l2_gbs = logical / iters / (launch_ms / 1e3) / 1e9
+    roof["l2_level"] = {"alg_bytes_per_launch": int(logical / iters), "achieved": round(l2_gbs, 1),
+                        "frac_of_hbm_peak": round(l2_gbs / peak, 4),
+                        "nodes_per_ray": round(nodes / max(rays, 1), 2), "tris_per_ray": round(tris / max(rays, 1), 2),
+                        "shadow_nodes_per_ray": round(st["shadow_nodes"] / max(st["shadow_rays"], 1), 2),
+                        "shadow_tris_per_ray": round(st["shadow_tris"] / max(st["shadow_rays"], 1), 2)}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": config_dict(info),
+            "data": "synthetic", "config": config_dict(), "scene": scene_dict(info),
             "clocks": clocks,
             "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": W * H * 16},
             "gpu_launches": int(launches),
             "mrays_per_s": round((st["closest_rays"] + st["shadow_rays"]) / (ms / args.steps / 1e3) / 1e6, 1),
-            "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": traffic, "traffic_source": traffic_src, "launches": iters,
-                         "per_launch_ms": round(kms[top] / iters, 4),
-                         "alg_bytes_per_launch": int(alg_bytes / iters),
-                         "nodes_per_ray": round(nodes / max(rays, 1), 2),
-                         "tris_per_ray": round(tris / max(rays, 1), 2),
-                         "shadow_nodes_per_ray": round(st["shadow_nodes"] / max(st["shadow_rays"], 1), 2),
-                         "shadow_tris_per_ray": round(st["shadow_tris"] / max(st["shadow_rays"], 1), 2)},
+            "roofline": roof,
             "profile_frame": {"kernel_ms": {k: round(v, 2) for k, v in kms.items()},
                               "closest_rays": st["closest_rays"], "shadow_rays": st["shadow_rays"],
                               "iterations": st["iterations"]},
@@ -549,11 +694,16 @@ def main():
         if not args.no_cache:
             line["cache"] = cache_eval(S, arrays, scene)
         if not args.no_serving:
-            line["serving"] = serving_eval(S, scene)
-            line["p50_job_latency_s"] = line["serving"]["p50_job_s"]
-            line["p99_job_latency_s"] = line["serving"]["p99_job_s"]
+            rates = [float(x) for x in args.serving_rates.split(",") if x]
+            line["serving"] = serving_eval(S, rates, args.serving_duration)
+            # headline latencies: the lowest rate of the sweep at or above 20 jobs/s, else the highest
+            pick = [r for r in line["serving"]["rates"] if r["rate_jobs_per_s"] >= 20.0]
+            row = pick[0] if pick else line["serving"]["rates"][-1]
+            line["p50_job_latency_s"] = row["p50_job_s"]
+            line["p99_job_latency_s"] = row["p99_job_s"]
+            line["serving_latency_rate_jobs_per_s"] = row["rate_jobs_per_s"]
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(arrays, steps=1, budget_s=20.0)
+            line["cpu_baseline"] = cpu_baseline(steps=1, budget_s=20.0)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -323,6 +323,30 @@ srt_status srt_pt_get_stats(const srt_pt* pt, srt_pt_stats* stats);
  * to the unprofiled ones (their durations are the production kernels').
  * 0 turns profiling off.  Results land in srt_pt_stats. */
 srt_status srt_pt_set_profiling(srt_pt* pt, int32_t enable);
+
+/* How srt_pt_render issues a frame's wavefront iterations.  The reference
+ * issues one optixLaunch per frame (path_tracer.cu:13-33); here a frame is
+ * many short kernels per iteration.  SRT_LAUNCH_GRAPH (default): one launch
+ * of a captured CUDA graph whose conditional while-node iterates on the
+ * device.  SRT_LAUNCH_DIRECT: the same kernels launched one by one from the
+ * host, checked every few iterations (same results, more host work; lets
+ * kernel-level tools that do not look inside graphs see every kernel). */
+enum { SRT_LAUNCH_GRAPH = 0, SRT_LAUNCH_DIRECT = 1 };
+srt_status srt_pt_set_launch_mode(srt_pt* pt, int32_t mode);
+
+/* Queue counts of the last render's wavefront iterations (no counterpart in
+ * the reference's megakernel; these are the integer counts its per-pixel
+ * loop, path_tracer.cu:56-166, implies).  Iteration k holds, per pixel, the
+ * k-th path segment of its sample sequence, so the counts are a function of
+ * the per-pixel streams alone.  counts: host int32[5 * max_iterations]:
+ * closest-hit rays, of which hits, misses; shadow rays; samples ended.
+ * *n_iterations = the iterations recorded (the first 4096 of a render). */
+srt_status srt_pt_get_iteration_counts(const srt_pt* pt, int32_t* counts, int32_t max_iterations,
+                                       int32_t* n_iterations);
+/* Finished samples per pixel of the last render (host int32[w*h]); equal
+ * to samples_per_pixel everywhere after a complete frame (the reference's
+ * `for (i < samples_per_pixel)` loop, path_tracer.cu:64). */
+srt_status srt_pt_get_pixel_samples(const srt_pt* pt, int32_t* samples);
 void srt_pt_destroy(srt_pt* pt);
 
 /* curand tape: out[p * ndraws + k] = k-th draw of the pixel-p stream of
@@ -515,10 +539,11 @@ void srt_server_destroy(srt_server* s);
  * memory of up to 2,097,152 pixels (about 8 MB, held by every GPU that loads
  * the library until the process exits); larger n returns SRT_ERR_ARG.  It
  * allocates nothing.  The first call on a device looks the array's device
- * address up once (set-up), so make that first call before any stream
- * capture.  All calls on a device share the array: calls that overlap on
- * the GPU (different streams or host threads) race and must be serialised
- * by the caller. */
+ * address up (set-up), so make that first call before any stream capture;
+ * a context made anew on the device (after cudaDeviceReset) is looked up
+ * again by the next call, which is then a first call too.  All calls on a
+ * device share the array: calls that overlap on the GPU (different streams
+ * or host threads) race and must be serialised by the caller. */
 srt_status srt_film_metric_noalloc(const float* x, const float* ref, int64_t n, int32_t type,
                                    float discard, float* out, void* stream);
 

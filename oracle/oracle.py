@@ -64,6 +64,11 @@ def lib():
             "oracle_nr_infer": (None, [_vp, _i64, _vp, _vp, C.c_int]),
             "oracle_render": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int,
                                         C.c_int, _vp, _vp, _vp, _vp]),
+            "oracle_render_events": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp,
+                                               C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int]),
+            "oracle_render_pixels": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _i64, _vp, C.c_int, C.c_int, _vp, _vp,
+                                               _vp, _vp]),
+            "oracle_scene_create_procedural": (_vp, [C.c_char_p, C.c_uint64, C.c_int32, C.c_int32, C.c_float]),
             "oracle_accumulate": (None, [_vp, _vp, _i64, C.c_int]),
             "oracle_tonemap": (None, [_vp, _i64, C.c_int, C.c_float, C.c_int]),
             "oracle_metric": (C.c_double, [_vp, _vp, _i64, C.c_int, C.c_float, _vp]),
@@ -141,14 +146,34 @@ def bxdf_eval_pdf(precision, type_, normal, wo, color, params, wi):
     return f, pdf
 
 
+class PtParams(C.Structure):
+    """srt_pt_params of include/srt.h (the PathTracer JSON keys + frame seed)."""
+    _fields_ = [("samples_per_pixel", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
+                ("use_nee", C.c_int32), ("use_mis", C.c_int32), ("seed", C.c_int32), ("rng_mode", C.c_int32),
+                ("flags", C.c_int32)]
+
+
+def pt_params(spp=1, max_depth=16, rr_depth=4, use_nee=True, use_mis=True, seed=0, rng_mode=0, flags=0):
+    return PtParams(spp, max_depth, rr_depth, int(use_nee), int(use_mis), seed, rng_mode, flags)
+
+
 class OracleScene:
-    def __init__(self, desc, bvh=False):
-        self.h = lib().oracle_scene_create(C.cast(C.pointer(desc), _vp))
+    def __init__(self, desc, bvh=False, handle=None):
+        self.h = handle if handle else lib().oracle_scene_create(C.cast(C.pointer(desc), _vp))
         if not self.h:
             raise ValueError("oracle_scene_create failed")
         self.has_bvh = False
         if bvh:
             self.build_bvh()
+
+    @classmethod
+    def procedural(cls, name, seed=1, n_spheres=64, subdiv=6, aspect=1.0, bvh=False):
+        """The benchmark's procedural scene built inside the oracle library
+        (same generator source as the CUDA library's srt_procedural_create)."""
+        h = lib().oracle_scene_create_procedural(name.encode(), seed, n_spheres, subdiv, aspect)
+        if not h:
+            raise ValueError(f"oracle_scene_create_procedural({name}) failed")
+        return cls(None, bvh=bvh, handle=h)
 
     def build_bvh(self):
         lib().oracle_scene_build_bvh(self.h)
@@ -223,6 +248,50 @@ class OracleScene:
         if rc != 0:
             raise ValueError(f"oracle_render failed ({rc})")
         return film, s1, s2, cnt
+
+    def render_pixels(self, w, h, params, pixels, threads=8):
+        """The listed pixels (index iy*w + ix) of a w x h frame."""
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        n = len(pixels)
+        film = np.zeros((n, 4), np.float32)
+        s1 = np.zeros((n, 3), np.float64)
+        s2 = np.zeros((n, 3), np.float64)
+        cnt = np.zeros(4, np.int64)
+        rc = lib().oracle_render_pixels(self.h, w, h, _np(pixels), n, C.cast(C.pointer(params), _vp),
+                                        int(self.has_bvh), threads, _np(film), _np(s1), _np(s2), _np(cnt))
+        if rc != 0:
+            raise ValueError(f"oracle_render_pixels failed ({rc})")
+        return film, s1, s2, cnt
+
+    def render_timeline(self, w, h, params, threads=8):
+        """The whole frame plus its wavefront timeline: int64 [iterations, 5]
+        = closest rays, hits, misses, shadow rays, samples ended, where
+        iteration k holds segment k of every pixel's sample sequence (one
+        path per pixel in flight, the next sample started in the iteration
+        the previous one ends)."""
+        n = w * h
+        ev_max = max(1, params.samples_per_pixel * params.max_depth)
+        film = np.zeros((n, 4), np.float32)
+        s1 = np.zeros((n, 3), np.float64)
+        s2 = np.zeros((n, 3), np.float64)
+        cnt = np.zeros(4, np.int64)
+        ev = np.zeros((n, ev_max), np.uint8)
+        rc = lib().oracle_render_events(self.h, w, h, 0, 0, w, h, C.cast(C.pointer(params), _vp),
+                                        int(self.has_bvh), threads, _np(film), _np(s1), _np(s2), _np(cnt), _np(ev),
+                                        ev_max)
+        if rc != 0:
+            raise ValueError(f"oracle_render_events failed ({rc})")
+        traced = (ev & 1).astype(bool)
+        last = int(np.nonzero(traced.any(0))[0].max()) + 1 if traced.any() else 0
+        tl = np.zeros((last, 5), np.int64)
+        for k0 in range(0, last, 64):
+            blk = ev[:, k0:min(last, k0 + 64)]
+            tl[k0:k0 + blk.shape[1], 0] = (blk & 1).astype(bool).sum(0)
+            tl[k0:k0 + blk.shape[1], 1] = (blk & 2).astype(bool).sum(0)
+            tl[k0:k0 + blk.shape[1], 3] = (blk & 4).astype(bool).sum(0)
+            tl[k0:k0 + blk.shape[1], 4] = (blk & 8).astype(bool).sum(0)
+        tl[:, 2] = tl[:, 0] - tl[:, 1]
+        return film, s1, s2, cnt, tl
 
     def __del__(self):
         try:

@@ -1040,9 +1040,19 @@ F3 env_radiance(const oracle_scene& s, F3 d)
 }
 
 // Megakernel raygen loop (src/shader/integrator/path_tracer.cu:50-169).
+// ev (optional, ev_max bytes): one byte per traced path segment of the
+// pixel, in order across its samples: bit 0 traced, bit 1 the ray hit a
+// triangle, bit 2 a shadow ray was traced, bit 3 the sample ended there.
+// A wavefront that keeps one path per pixel in flight and starts the next
+// sample in the iteration the previous one ends traces segment k of every
+// pixel in its iteration k, so these bytes give its per-iteration counts.
 void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt_pt_params& p, bool use_bvh,
-                  float* film, double* sum, double* sumsq, int64_t* cnt)
+                  float* film, double* sum, double* sumsq, int64_t* cnt, uint8_t* ev = nullptr, int ev_max = 0)
 {
+    int seg = 0;
+    auto mark = [&](int k, uint8_t bits) {
+        if (ev && k >= 0 && k < ev_max) ev[k] |= bits;
+    };
     const int idx = iy * w + ix;
     const bool fixed = (p.flags & SRT_PT_FIXED_CDF_REMAP) != 0;
     Rng rng;
@@ -1064,6 +1074,7 @@ void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt
             cnt[1]++;
             cnt[3]++;
             Hit hit = trace(s, ro, rd, 1e-3f, 1e16f, false, use_bvh);
+            mark(seg++, hit.prim < 0 ? 1 : 3);
             if (hit.prim < 0) {
                 L = L + beta * env_radiance(s, rd);
                 break;
@@ -1098,6 +1109,7 @@ void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt
                 float t = length(ls.pos - hi.pos);
                 if (cos_l > 1e-4f && ls.pdf > 1e-4f && t > 1e-3f && (cos_o > 0.0f || is_transmissive(mat.bxdf))) {
                     cnt[2]++;
+                    mark(seg - 1, 4);
                     Hit sh = trace(s, hi.pos, sd, 1e-3f, t - 1e-3f, true, use_bvh);
                     if (sh.prim < 0) {
                         float mis = 1.0f;
@@ -1128,6 +1140,7 @@ void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt
                 beta = beta / q;
             }
         }
+        mark(seg - 1, 8);
         if (std::isfinite(L.x) && std::isfinite(L.y) && std::isfinite(L.z)) {
             result = result + L / (float)p.samples_per_pixel;
             s1[0] += L.x;
@@ -1468,20 +1481,51 @@ void oracle_light_sample(const oracle_scene* s, int64_t n, const float* u2, int 
     }
 }
 
-int oracle_render(const oracle_scene* s, int w, int h, int x0, int y0, int cw, int ch, const srt_pt_params* p,
-                  int use_bvh, int threads, float* film, double* sum, double* sumsq, int64_t* counters)
+// oracle_render with the per-pixel segment bytes of render_pixel (events:
+// uint8[cw * ch * ev_max], zeroed by the caller; may be null).
+int oracle_render_events(const oracle_scene* s, int w, int h, int x0, int y0, int cw, int ch,
+                         const srt_pt_params* p, int use_bvh, int threads, float* film, double* sum, double* sumsq,
+                         int64_t* counters, uint8_t* events, int ev_max)
 {
     if (!s || !p || w <= 0 || h <= 0 || x0 < 0 || y0 < 0 || x0 + cw > w || y0 + ch > h) return 1;
     if (s->light_inst.empty() && p->use_nee) return 2;
+    if (events && ev_max <= 0) return 1;
     std::vector<int64_t> cnt((size_t)cw * ch * 4, 0);
     parallel_for((int64_t)cw * ch, threads, [&](int64_t k) {
         int ix = x0 + (int)(k % cw), iy = y0 + (int)(k / cw);
-        render_pixel(*s, w, h, ix, iy, *p, use_bvh != 0, film + 4 * k, sum + 3 * k, sumsq + 3 * k, &cnt[4 * k]);
+        render_pixel(*s, w, h, ix, iy, *p, use_bvh != 0, film + 4 * k, sum + 3 * k, sumsq + 3 * k, &cnt[4 * k],
+                     events ? events + (size_t)k * ev_max : nullptr, events ? ev_max : 0);
     });
     for (int j = 0; j < 4; ++j) counters[j] = 0;
     for (size_t k = 0; k < (size_t)cw * ch; ++k)
         for (int j = 0; j < 4; ++j) counters[j] += cnt[4 * k + j];
     return 0;
+}
+
+int oracle_render_pixels(const oracle_scene* s, int w, int h, const int32_t* pixels, int64_t n,
+                         const srt_pt_params* p, int use_bvh, int threads, float* film, double* sum,
+                         double* sumsq, int64_t* counters)
+{
+    if (!s || !p || w <= 0 || h <= 0 || n < 0 || (n > 0 && !pixels)) return 1;
+    if (s->light_inst.empty() && p->use_nee) return 2;
+    for (int64_t k = 0; k < n; ++k)
+        if (pixels[k] < 0 || (int64_t)pixels[k] >= (int64_t)w * h) return 1;
+    std::vector<int64_t> cnt((size_t)n * 4, 0);
+    parallel_for(n, threads, [&](int64_t k) {
+        int ix = pixels[k] % w, iy = pixels[k] / w;
+        render_pixel(*s, w, h, ix, iy, *p, use_bvh != 0, film + 4 * k, sum + 3 * k, sumsq + 3 * k, &cnt[4 * k]);
+    });
+    for (int j = 0; j < 4; ++j) counters[j] = 0;
+    for (size_t k = 0; k < (size_t)n; ++k)
+        for (int j = 0; j < 4; ++j) counters[j] += cnt[4 * k + j];
+    return 0;
+}
+
+int oracle_render(const oracle_scene* s, int w, int h, int x0, int y0, int cw, int ch, const srt_pt_params* p,
+                  int use_bvh, int threads, float* film, double* sum, double* sumsq, int64_t* counters)
+{
+    return oracle_render_events(s, w, h, x0, y0, cw, ch, p, use_bvh, threads, film, sum, sumsq, counters, nullptr,
+                                0);
 }
 
 // LightTracer raygen (src/shader/integrator/light_tracer.cu:57-175) for

@@ -97,6 +97,22 @@ int oracle_render(const oracle_scene* s, int w, int h, int x0, int y0, int cw, i
                   const srt_pt_params* p, int use_bvh, int threads, float* film, double* sum,
                   double* sumsq, int64_t* counters);
 
+/* oracle_render plus one byte per traced path segment of each pixel
+ * (events: cw*ch*ev_max, zeroed by the caller): bit 0 traced, bit 1 hit,
+ * bit 2 shadow ray traced, bit 3 the sample ended there. */
+int oracle_render_events(const oracle_scene* s, int w, int h, int x0, int y0, int cw, int ch,
+                         const srt_pt_params* p, int use_bvh, int threads, float* film, double* sum,
+                         double* sumsq, int64_t* counters, uint8_t* events, int ev_max);
+/* oracle_render over an arbitrary list of pixels (index iy*w + ix) of a
+ * w x h film; film / sum / sumsq are per listed pixel. */
+int oracle_render_pixels(const oracle_scene* s, int w, int h, const int32_t* pixels, int64_t n,
+                         const srt_pt_params* p, int use_bvh, int threads, float* film, double* sum,
+                         double* sumsq, int64_t* counters);
+/* The procedural scene `name` ("cornell" | "spheres") of the benchmark
+ * built from the generator source (scene_inputs.cpp), camera aspect set. */
+oracle_scene* oracle_scene_create_procedural(const char* name, uint64_t seed, int32_t n_spheres,
+                                             int32_t subdiv, float aspect);
+
 /* Film passes. */
 void oracle_accumulate(float* film, float* acc, int64_t n, int frame_count);
 void oracle_tonemap(float* film, int64_t n, int type, float exposure, int use_gamma);

@@ -14,9 +14,9 @@ import numpy as np
 
 from . import _capi
 from ._capi import (BXDF_DIELECTRIC, BXDF_DIFFUSE, BXDF_DIFFUSE_TRANSMISSION, BXDF_DISNEY, CAMERA_ORTHOGRAPHIC,
-                    CAMERA_PERSPECTIVE, METRIC_MAPE, METRIC_MSE, METRIC_RELMSE, METRIC_SMAPE, PT_FIXED_CDF_REMAP,
-                    RNG_CURAND, RNG_HASH, TONE_ACES, TONE_CLAMP, TONE_NONE, TONE_REINHARD, TONE_UNCHARTED2,
-                    SrtError, check, lib)
+                    CAMERA_PERSPECTIVE, LAUNCH_DIRECT, LAUNCH_GRAPH, METRIC_MAPE, METRIC_MSE, METRIC_RELMSE,
+                    METRIC_SMAPE, PT_FIXED_CDF_REMAP, RNG_CURAND, RNG_HASH, TONE_ACES, TONE_CLAMP, TONE_NONE,
+                    TONE_REINHARD, TONE_UNCHARTED2, SrtError, check, lib)
 
 __all__ = [
     "SceneArrays", "Scene", "PathTracer", "procedural", "import_scene", "lib", "check", "SrtError", "bxdf_sample", "bxdf_eval",
@@ -274,6 +274,25 @@ class PathTracer:
     def set_profiling(self, mode):
         """0 off; 1 (or True) timestamps + traversal work counters; 2 timestamps only."""
         check(lib().srt_pt_set_profiling(self.handle, int(mode)))
+
+    def set_launch_mode(self, mode):
+        """LAUNCH_GRAPH (one graph launch per frame) or LAUNCH_DIRECT (the
+        same kernels launched one by one)."""
+        check(lib().srt_pt_set_launch_mode(self.handle, int(mode)))
+
+    def iteration_counts(self, max_iterations=4096):
+        """int32 [iterations, 5]: closest rays, hits, misses, shadow rays,
+        samples ended, per wavefront iteration of the last render."""
+        out = np.zeros((max_iterations, 5), np.int32)
+        n = C.c_int32()
+        check(lib().srt_pt_get_iteration_counts(self.handle, _ptr(out), max_iterations, C.byref(n)))
+        return out[: min(n.value, max_iterations)].copy()
+
+    def pixel_samples(self):
+        """int32 [w*h]: finished samples per pixel of the last render."""
+        out = np.zeros(self.width * self.height, np.int32)
+        check(lib().srt_pt_get_pixel_samples(self.handle, _ptr(out)))
+        return out
 
     def close(self):
         if self.handle:

@@ -23,6 +23,7 @@ CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC = 0, 1
 CAMERA_MIRROR_X = 0x100  # flag OR'd into CameraDesc.type (left-handed pbrt camera frame)
 RNG_CURAND, RNG_HASH = 0, 1
 PT_FIXED_CDF_REMAP = 1
+LAUNCH_GRAPH, LAUNCH_DIRECT = 0, 1
 TONE_NONE, TONE_CLAMP, TONE_REINHARD, TONE_UNCHARTED2, TONE_ACES = 0, 1, 2, 3, 4
 METRIC_MSE, METRIC_MAPE, METRIC_SMAPE, METRIC_RELMSE = 0, 1, 2, 3
 MEASURE_NONE, MEASURE_REFERENCE, MEASURE_ERROR = 0, 1, 2
@@ -160,6 +161,9 @@ _PROTOS = [
                                 C.c_void_p, C.c_void_p]),
     ("srt_pt_get_stats", C.c_int, [C.c_void_p, C.POINTER(PtStats)]),
     ("srt_pt_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
+    ("srt_pt_set_launch_mode", C.c_int, [C.c_void_p, C.c_int32]),
+    ("srt_pt_get_iteration_counts", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    ("srt_pt_get_pixel_samples", C.c_int, [C.c_void_p, C.c_void_p]),
     ("srt_pt_destroy", None, [C.c_void_p]),
     ("srt_rng_tape", C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]),
     ("srt_bxdf_sample", C.c_int, [C.POINTER(BxdfBatch), C.c_void_p]),

@@ -122,7 +122,7 @@ def build_cli() -> str:
 def build_oracle() -> str:
     """CPU oracle (test infrastructure): oracle/liboracle.so."""
     d = os.path.join(ROOT, "oracle")
-    for name in ("liboracle.so", "srt_oracle.o", "curand_host.o"):
+    for name in ("liboracle.so", "srt_oracle.o", "curand_host.o", "scene_inputs.o"):
         drop_foreign(os.path.join(d, name))
     r = subprocess.run(["make", "-s", "-C", d], capture_output=True, text=True)
     if r.returncode != 0:
@@ -130,10 +130,12 @@ def build_oracle() -> str:
     return os.path.join(d, "liboracle.so")
 
 
-def build_reference(ref_root: str = "/root/reference") -> str | None:
-    """Reference headers built for the host (oracle/_ref); only where the
-    reference tree exists."""
-    if not os.path.isdir(os.path.join(ref_root, "src", "device_include")):
+def build_reference(ref_root: str | None = None) -> str | None:
+    """Reference headers built for the host (oracle/_ref), from the reference
+    tree at `ref_root` or $SRT_REFERENCE_ROOT; skipped (None) when neither
+    names a reference tree."""
+    ref_root = ref_root or os.environ.get("SRT_REFERENCE_ROOT")
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src", "device_include")):
         return None
     d = os.path.join(ROOT, "oracle", "ref")
     r = subprocess.run(["make", "-s", "-C", d, f"REF={ref_root}"], capture_output=True, text=True)

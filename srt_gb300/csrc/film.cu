@@ -6,6 +6,8 @@
 // in the reference, measure.cu:46-49) it finds the exact cut value with a
 // three-pass radix select over the error bits (11 + 11 + 10 bits) and sums
 // everything below it.
+#include <cuda.h>  // CUcontext / CUresult types only (the driver call is looked up at run time)
+
 #include <mutex>
 
 #include "common.h"
@@ -285,6 +287,33 @@ extern "C" srt_status srt_film_measure_view(float* film, const float* ref, int64
     return SRT_OK;
 }
 
+namespace {
+
+// The Measure metric's launch sequence (measure.cu:35-49 with a radix select
+// in place of the sort) over a per-pixel error buffer `err` and select state
+// `sc`; returns the metric in *out once the stream has reached it.
+srt_status run_metric(const float* x, const float* ref, int64_t n, int32_t type, long long keep, float* err,
+                      MetricScratch* sc, cudaStream_t st, float* out)
+{
+    const int g = grid_for(n);
+    k_metric_init<<<1, 256, 0, st>>>(sc, keep);  // clears the histograms and the select state
+    k_metric_errors<<<g, kThreads, 0, st>>>(reinterpret_cast<const float4*>(x), reinterpret_cast<const float4*>(ref),
+                                            n, type, err);
+    const int shifts[3] = {21, 10, 0}, widths[3] = {11, 11, 10};
+    for (int p = 0; p < 3; ++p) {
+        k_metric_hist<<<g, kThreads, 0, st>>>(err, n, sc, shifts[p], widths[p]);
+        k_metric_select<<<1, 1, 0, st>>>(sc, shifts[p], widths[p], p == 2 ? 1 : 0);
+    }
+    SRT_CUDA_TRY(cudaGetLastError());
+    float res = 0.0f;
+    SRT_CUDA_TRY(cudaMemcpyAsync(&res, &sc->s.result, sizeof(float), cudaMemcpyDeviceToHost, st));
+    SRT_CUDA_TRY(cudaStreamSynchronize(st));
+    *out = res;
+    return SRT_OK;
+}
+
+}  // namespace
+
 extern "C" srt_status srt_film_metric(const float* x, const float* ref, int64_t n, int32_t type, float discard,
                                       void* scratch, float* out, void* stream)
 {
@@ -302,25 +331,10 @@ extern "C" srt_status srt_film_metric(const float* x, const float* ref, int64_t 
     if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(ref)) % 16 ||
         reinterpret_cast<uintptr_t>(scratch) % 256)
         return set_error(SRT_ERR_ARG, "films must be 16-byte aligned and scratch 256-byte aligned");
-    cudaStream_t st = as_stream(stream);
     float* err = reinterpret_cast<float*>(scratch);
     MetricScratch* sc = reinterpret_cast<MetricScratch*>(reinterpret_cast<char*>(scratch) +
                                                          ((size_t)n * 4 + 255) / 256 * 256);
-    int g = grid_for(n);
-    k_metric_init<<<1, 256, 0, st>>>(sc, keep);
-    k_metric_errors<<<g, kThreads, 0, st>>>(reinterpret_cast<const float4*>(x), reinterpret_cast<const float4*>(ref),
-                                            n, type, err);
-    const int shifts[3] = {21, 10, 0}, widths[3] = {11, 11, 10};
-    for (int p = 0; p < 3; ++p) {
-        k_metric_hist<<<g, kThreads, 0, st>>>(err, n, sc, shifts[p], widths[p]);
-        k_metric_select<<<1, 1, 0, st>>>(sc, shifts[p], widths[p], p == 2 ? 1 : 0);
-    }
-    SRT_CUDA_TRY(cudaGetLastError());
-    float res = 0.0f;
-    SRT_CUDA_TRY(cudaMemcpyAsync(&res, &sc->s.result, sizeof(float), cudaMemcpyDeviceToHost, st));
-    SRT_CUDA_TRY(cudaStreamSynchronize(st));
-    *out = res;
-    return SRT_OK;
+    return run_metric(x, ref, n, type, keep, err, sc, as_stream(stream), out);
 }
 
 // ---------------------------------------------------------------------------
@@ -340,24 +354,52 @@ constexpr size_t kStaticMetricErrBytes = ((size_t)kStaticMetricPixels * 4 + 255)
 // process exits; all calls on a device share it.
 static __device__ __align__(256) unsigned char g_metric_scratch[kStaticMetricErrBytes + sizeof(MetricScratch)];
 
-// Device address of g_metric_scratch on the current device, looked up once
-// per device (the array's host-side name is only a stand-in, never a device
-// address).
+// The calling thread's current CUDA context (the driver's cuCtxGetCurrent,
+// found through the runtime so the library needs no link to the driver
+// library), or null where it cannot be asked.
+CUcontext current_context()
+{
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    static GetCurrent fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<GetCurrent>(f);
+    }();
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
+// Device address of g_metric_scratch on the current device.  The array's
+// host-side name is only a stand-in, never a device address, so the address
+// is looked up with cudaGetSymbolAddress: once per device and context (a
+// context made anew, e.g. after cudaDeviceReset, places the array anew and
+// is looked up again; where the context cannot be told, every call looks
+// it up).
 srt_status static_metric_scratch(void** out)
 {
+    struct Entry {
+        CUcontext ctx;
+        void* ptr;
+    };
     static std::mutex mu;
-    static void* ptrs[128] = {};
+    static Entry cache[128] = {};
     int dev = 0;
     SRT_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 128) return set_error(SRT_ERR_ARG, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(mu);
-    if (!ptrs[dev]) {
+    const CUcontext ctx = current_context();
+    if (!cache[dev].ptr || !ctx || ctx != cache[dev].ctx) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_metric_scratch);
         if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_metric_scratch)");
-        ptrs[dev] = p;
+        cache[dev].ptr = p;
+        cache[dev].ctx = current_context();  // the lookup made the context current if it was not
     }
-    *out = ptrs[dev];
+    *out = cache[dev].ptr;
     return SRT_OK;
 }
 
@@ -383,22 +425,7 @@ extern "C" srt_status srt_film_metric_noalloc(const float* x, const float* ref, 
         return set_error(SRT_ERR_ARG, "films must be 16-byte aligned");
     void* base = nullptr;
     SRT_TRY(static_metric_scratch(&base));
-    cudaStream_t st = as_stream(stream);
     float* err = reinterpret_cast<float*>(base);
     MetricScratch* sc = reinterpret_cast<MetricScratch*>(reinterpret_cast<char*>(base) + kStaticMetricErrBytes);
-    int g = grid_for(n);
-    k_metric_init<<<1, 256, 0, st>>>(sc, keep);  // clears the histograms and the select state
-    k_metric_errors<<<g, kThreads, 0, st>>>(reinterpret_cast<const float4*>(x), reinterpret_cast<const float4*>(ref),
-                                            n, type, err);
-    const int shifts[3] = {21, 10, 0}, widths[3] = {11, 11, 10};
-    for (int p = 0; p < 3; ++p) {
-        k_metric_hist<<<g, kThreads, 0, st>>>(err, n, sc, shifts[p], widths[p]);
-        k_metric_select<<<1, 1, 0, st>>>(sc, shifts[p], widths[p], p == 2 ? 1 : 0);
-    }
-    SRT_CUDA_TRY(cudaGetLastError());
-    float res = 0.0f;
-    SRT_CUDA_TRY(cudaMemcpyAsync(&res, &sc->s.result, sizeof(float), cudaMemcpyDeviceToHost, st));
-    SRT_CUDA_TRY(cudaStreamSynchronize(st));
-    *out = res;
-    return SRT_OK;
+    return run_metric(x, ref, n, type, keep, err, sc, as_stream(stream), out);
 }

@@ -562,9 +562,19 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
 // decides whether the loop runs again (paths in flight, no overflow, and the
 // launch's iteration bound not reached: the loop always terminates).
 template <bool kCond>
-__global__ void k_advance(Counters* c, const JobRec* __restrict__ jobs, int max_jobs,
+__global__ void k_advance(Counters* c, IterCount* history, const JobRec* __restrict__ jobs, int max_jobs,
                           cudaGraphConditionalHandle cond)
 {
+    if (c->iterations < kIterHistory) {
+        IterCount h;
+        h.closest = c->n_cur;
+        h.hits = c->n_hit;
+        h.misses = c->n_miss;
+        h.shadow = c->n_shadow;
+        h.done = c->n_done;
+        h.pad[0] = h.pad[1] = h.pad[2] = 0;
+        history[c->iterations] = h;
+    }
     for (int j = 0; j < max_jobs; ++j)
         if (jobs[j].cache.q_count) {
             jobs[j].cache.q_count[4] += jobs[j].cache.q_count[0];  // queries of the frame
@@ -655,6 +665,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
         order_ = (int32_t*)take(C * 4);
         done_.rec = (uint4*)take(C * 32);
         counters_ = (Counters*)take(sizeof(Counters));
+        history_ = (IterCount*)take(sizeof(IterCount) * kIterHistory);
         jobs_ = (JobRec*)take(sizeof(JobRec) * max_jobs);
         pixels_done_ = (int32_t*)take(4 * (size_t)max_jobs);
         return off;
@@ -746,9 +757,9 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     mark(3, 1);
     mark(4, 0);
     if (cond)
-        k_advance<true><<<1, 1, 0, st>>>(counters_, jobs_, max_jobs_, *cond);
+        k_advance<true><<<1, 1, 0, st>>>(counters_, history_, jobs_, max_jobs_, *cond);
     else
-        k_advance<false><<<1, 1, 0, st>>>(counters_, jobs_, max_jobs_, 0);
+        k_advance<false><<<1, 1, 0, st>>>(counters_, history_, jobs_, max_jobs_, 0);
     mark(4, 1);
 }
 
@@ -821,14 +832,24 @@ srt_status Engine::read_counters(Counters& c, cudaStream_t st)
     return SRT_OK;
 }
 
+srt_status Engine::read_history(IterCount* host, int n)
+{
+    if (n <= 0) return SRT_OK;
+    n = std::min(n, kIterHistory);
+    SRT_CUDA_TRY(cudaMemcpy(host, history_, sizeof(IterCount) * (size_t)n, cudaMemcpyDeviceToHost));
+    return SRT_OK;
+}
+
 srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, long long budget_iters)
 {
     const bool prof = profile_;
-    // SRT_NO_GRAPH=1 launches the iteration kernels directly (diagnostics)
-    static const bool no_graph = [] {
+    // direct launches: the handle's launch mode, or SRT_NO_GRAPH=1 for every
+    // engine of the process (diagnostics)
+    static const bool env_no_graph = [] {
         const char* v = std::getenv("SRT_NO_GRAPH");
         return v && v[0] == '1';
     }();
+    const bool no_graph = env_no_graph || direct_;
     if (prof && !ev_[0][0][0]) {
         for (auto& a : ev_)
             for (auto& b : a)
@@ -1060,6 +1081,49 @@ extern "C" srt_status srt_pt_get_stats(const srt_pt* p, srt_pt_stats* s)
     clear_error();
     if (!p || !s) return set_error(SRT_ERR_ARG, "NULL argument");
     *s = p->stats;
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_pt_set_launch_mode(srt_pt* p, int32_t mode)
+{
+    clear_error();
+    if (!p) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (mode != SRT_LAUNCH_GRAPH && mode != SRT_LAUNCH_DIRECT)
+        return set_error(SRT_ERR_ARG, "launch mode must be SRT_LAUNCH_GRAPH or SRT_LAUNCH_DIRECT");
+    p->engine.set_direct(mode == SRT_LAUNCH_DIRECT);
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_pt_get_iteration_counts(const srt_pt* p, int32_t* counts, int32_t max_iterations,
+                                                  int32_t* n_iterations)
+{
+    clear_error();
+    if (!p || !n_iterations || max_iterations < 0 || (max_iterations > 0 && !counts))
+        return set_error(SRT_ERR_ARG, "bad arguments");
+    const int recorded = (int)std::min<int64_t>(p->stats.iterations, kIterHistory);
+    *n_iterations = recorded;
+    const int n = std::min(recorded, (int)max_iterations);
+    if (n <= 0) return SRT_OK;
+    std::vector<IterCount> h((size_t)n);
+    SRT_TRY(const_cast<srt_pt*>(p)->engine.read_history(h.data(), n));
+    for (int i = 0; i < n; ++i) {
+        counts[5 * i + 0] = h[i].closest;
+        counts[5 * i + 1] = h[i].hits;
+        counts[5 * i + 2] = h[i].misses;
+        counts[5 * i + 3] = h[i].shadow;
+        counts[5 * i + 4] = h[i].done;
+    }
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_pt_get_pixel_samples(const srt_pt* p, int32_t* samples)
+{
+    clear_error();
+    if (!p || !samples) return set_error(SRT_ERR_ARG, "NULL argument");
+    const size_t npix = (size_t)p->width * p->height;
+    // the w word of each pixel's 16-byte radiance record counts its finished samples
+    SRT_CUDA_TRY(cudaMemcpy2D(samples, 4, reinterpret_cast<const char*>(p->lpath) + 12, 16, 4, npix,
+                              cudaMemcpyDeviceToHost));
     return SRT_OK;
 }
 

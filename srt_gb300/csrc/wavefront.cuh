@@ -82,6 +82,18 @@ struct Counters {
     long long run_iters, run_limit;  // iterations of the current graph launch and its bound
 };
 
+// Queue counts of one wavefront iteration (written by k_advance for the
+// first kIterHistory iterations of a run).
+struct IterCount {
+    int32_t closest;   // rays through the closest-hit kernel
+    int32_t hits;      // of those, rays that hit a triangle
+    int32_t misses;    // of those, rays that left the scene
+    int32_t shadow;    // rays through the shadow kernel
+    int32_t done;      // samples that ended in the iteration
+    int32_t pad[3];
+};
+constexpr int kIterHistory = 4096;
+
 // Per-kernel device time gathered in profiling mode.
 struct KernelTimes {
     double ms[5] = {0, 0, 0, 0, 0};  // closest, shade, shadow, regen, advance
@@ -109,6 +121,8 @@ public:
     srt_status run(cudaStream_t st, long long max_iters, bool until_idle, long long budget_iters);
     srt_status reset_counters(cudaStream_t st);
     srt_status read_counters(Counters& c, cudaStream_t st);
+    // Copies the first n recorded iterations' counts to host memory.
+    srt_status read_history(IterCount* host, int n);
     int32_t* pixels_done_slot(int job) const { return pixels_done_ + job; }
     const int32_t* pixels_done_all() const { return pixels_done_; }
     // mode 0: off; 1: timestamps between the kernels and traversal work
@@ -130,6 +144,11 @@ public:
         }
     }
     bool profiling() const { return profile_; }
+    // direct = true: every iteration's kernels are launched one by one from
+    // the host instead of through the captured graph (same kernels, same
+    // results)
+    void set_direct(bool direct) { direct_ = direct; }
+    bool direct() const { return direct_; }
     KernelTimes& times() { return times_; }
 
 private:
@@ -149,6 +168,7 @@ private:
     int32_t* order_ = nullptr;  // queue indices in shading order (hits, then misses)
     DoneQueue done_{};
     Counters* counters_ = nullptr;
+    IterCount* history_ = nullptr;  // [kIterHistory]
     JobRec* jobs_ = nullptr;
     int32_t* pixels_done_ = nullptr;
     Counters* host_counters_ = nullptr;
@@ -158,6 +178,7 @@ private:
     bool profile_ = false;
     bool count_ = true;
     bool cache_ = false;
+    bool direct_ = false;
     KernelTimes times_;
     int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0, grid_shade_ = 0, grid_order_ = 0;
 };

@@ -324,7 +324,9 @@ def test_obj_textures_and_flipped_uvs(tmp_path):
     assert s.meshes[2]["texcoords"] is None
 
 
-REF_EXAMPLE = "/root/reference/example/cornell_box_obj/cornell_box.obj"
+# the reference's own example model, where $SRT_REFERENCE_ROOT names a reference tree
+REF_EXAMPLE = os.path.join(os.environ.get("SRT_REFERENCE_ROOT") or "/nonexistent",
+                           "example", "cornell_box_obj", "cornell_box.obj")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_EXAMPLE), reason="the reference tree is not present")
