@@ -411,6 +411,62 @@ def relmse(S, x, ref):
     return S.film_metric(torch.from_numpy(x).cuda(), torch.from_numpy(ref).cuda(), S.METRIC_RELMSE, 0.1)
 
 
+def cache_bound(S, scene, ref, w, h, frames=128):
+    """Upper bound on the time-to-quality speedup of ANY cache that ends
+    paths at the second vertex, measured on this scene.  A perfect cache
+    returns the exact expected radiance at the second vertex: it removes
+    the variance of everything after it and the cost of tracing it, but
+    keeps the variance of the path prefix (camera ray, emission and NEE at
+    the first vertex: the estimator with max depth 1, its terms assumed not
+    negatively correlated with the rest) and costs at least the prefix.
+    Per-pixel variances from `frames` independent 1-spp frames of the full
+    estimator and of the prefix; their trimmed (largest 0.1 % dropped) mean
+    relMSE contribution per sample against the FP64 reference gives the
+    variance ratio r, so the perfect cache needs 64 r samples to reach the
+    plain 64-spp relMSE; cost per sample from 64-spp frames at max depth 16
+    (plain) and 1 (prefix, optimistic: the second-vertex ray is not even
+    traced).  Bound = (t_plain / t_prefix per sample) / r."""
+    import numpy as np
+    import torch
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    pt = S.PathTracer(scene, w, h)
+    refd = torch.from_numpy(ref[:, :3]).cuda().double()
+    den = (refd + 1e-6) ** 2
+
+    def rel_per_sample(depth):
+        s1 = torch.zeros((w * h, 3), dtype=torch.float64, device="cuda")
+        s2 = torch.zeros_like(s1)
+        for f in range(frames):
+            pt.render(film, S.pt_params(1, depth, RR_DEPTH, 1, 1, 30000 + f))
+            x = film[:, :3].double()
+            s1 += x
+            s2 += x * x
+        var = (s2 - s1 * s1 / frames) / (frames - 1)
+        e = (var / den).mean(1)
+        keep = int(e.numel() * 0.999)
+        return float(torch.sort(e).values[:keep].mean())
+
+    def per_sample_ms(depth):
+        pt.render(film, S.pt_params(64, depth, RR_DEPTH, 1, 1, 777))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(3):
+            pt.render(film, S.pt_params(64, depth, RR_DEPTH, 1, 1, 778 + i))
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / 3 / 64 * 1e3
+
+    e_full, e_prefix = rel_per_sample(MAX_DEPTH), rel_per_sample(1)
+    t_full, t_prefix, t_prefix2 = per_sample_ms(MAX_DEPTH), per_sample_ms(1), per_sample_ms(2)
+    r = e_prefix / e_full
+    pt.close()
+    return {"frames_for_variance": frames, "relmse_per_sample_plain": e_full, "relmse_per_sample_prefix": e_prefix,
+            "variance_ratio_prefix_over_plain": round(r, 4),
+            "samples_a_perfect_cache_needs": round(64 * r, 1),
+            "ms_per_sample_plain_depth16": round(t_full, 4), "ms_per_sample_prefix_depth1": round(t_prefix, 4),
+            "ms_per_sample_depth2": round(t_prefix2, 4),
+            "max_speedup_any_second_vertex_cache": round((t_full / t_prefix) / r, 3)}
+
+
 def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_spp=64):
     """Learned-cache workload: 1280x720, 1 spp per frame for `frames` frames
     with online training on 2^16 paths per frame; relMSE of the accumulated
@@ -470,6 +526,7 @@ def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_s
             if t_reach is None and r <= rel_plain:
                 t_reach = t_total
     S.lib().srt_mlp_destroy(mlp)
+    bound = cache_bound(S, scene, ref, w, h)
     arrays.set_aspect(W / H)
     S.check(S.lib().srt_scene_set_camera(scene.handle, C.byref(arrays.camera)))
     return {"workload": f"{w}x{h}, 1 spp/frame x {frames} frames, online training on 2^16 paths/frame",
@@ -479,7 +536,8 @@ def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_s
                        "relmse_curve": curve,
                        "fallback_fraction": round(fallback / max(1, queries + fallback), 4)},
             "time_to_plain64_relmse_s": None if t_reach is None else round(t_reach, 4),
-            "speedup_vs_plain64": None if t_reach is None else round(t_plain / t_reach, 3)}
+            "speedup_vs_plain64": None if t_reach is None else round(t_plain / t_reach, 3),
+            "bound": bound}
 
 
 def serving_eval(S, rates=(5.0, 20.0, 50.0), duration=30.0):

@@ -238,6 +238,7 @@ extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_
     J.rng_mode = prm->rng_mode;
     CacheRec& C = J.cache;
     C.w = mlp->wb;
+    C.wpack = mlp->wpack;
     C.box = mlp->box;
     C.q_rec = b.q_rec;
     C.q_beta = b.q_beta;

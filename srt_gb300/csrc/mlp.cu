@@ -1,6 +1,7 @@
 // mlp.cu — fused BF16 tensor-core kernels of the radiance-cache network
-// (see mlp.cuh): inference, forward+backward-data for training, weight
-// gradients, Adam.  The reference's learned part (tiny-cuda-nn HashGrid +
+// (see mlp.cuh): inference (tcgen05.mma with TMEM accumulators, the fused
+// kernel of umma_mlp.cuh: standalone and the tracer's cache queries),
+// forward+backward-data for training, weight gradients (mma.sync), Adam.  The reference's learned part (tiny-cuda-nn HashGrid +
 // CutlassMLP, src/passes/npr/neural_radiosity.cu:6-52) is an un-vendored
 // library; the network here is a plain fully fused MLP.
 //
@@ -19,6 +20,7 @@
 
 #include "common.h"
 #include "mlp.cuh"
+#include "umma_mlp.cuh"
 #include "wavefront.cuh"
 
 namespace srt {
@@ -210,46 +212,6 @@ __device__ __forceinline__ void forward_tile(const __nv_bfloat16* ws, const uint
 }
 
 __device__ __forceinline__ float safe_exp(float z) { return __expf(fminf(z, 15.0f)); }
-
-// RGB of rows g (out0) and g+8 (out1), valid in lanes with t == 0
-__device__ __forceinline__ void output_rgb(const float (&z)[2][4], float3& out0, float3& out1)
-{
-    const unsigned full = 0xffffffffu;
-    float b0 = __shfl_down_sync(full, z[0][0], 1);  // column 2 (t = 1, c0) of row g
-    float b1 = __shfl_down_sync(full, z[0][2], 1);  // column 2 of row g+8
-    out0 = make_float3(safe_exp(z[0][0]), safe_exp(z[0][1]), safe_exp(b0));
-    out1 = make_float3(safe_exp(z[0][2]), safe_exp(z[0][3]), safe_exp(b1));
-}
-
-__global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(const __nv_bfloat16* __restrict__ w, MlpBox box,
-                                                           const float4* __restrict__ rec, int64_t n,
-                                                           float4* __restrict__ out)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16* ws = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    load_weights(w, ws, nullptr);
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int warp = threadIdx.x >> 5;
-    const int64_t tiles = (n + 15) / 16;
-    for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < tiles; tile += (int64_t)gridDim.x * 4) {
-        int64_t r0 = tile * 16 + g, r1 = r0 + 8;
-        bool v0 = r0 < n, v1 = r1 < n;
-        float4 q0[4], q1[4];
-        load_record(rec, r0, v0, q0);
-        load_record(rec, r1, v1, q1);
-        uint32_t a0[6][4];
-        input_fragments(q0, q1, v0, v1, box, a0);
-        float z[2][4];
-        uint32_t masks[5];
-        forward_tile<false>(ws, a0, z, masks, nullptr);
-        float3 o0, o1;
-        output_rgb(z, o0, o1);
-        if (t == 0) {
-            if (v0) out[r0] = make_float4(o0.x, o0.y, o0.z, 0.0f);
-            if (v1) out[r1] = make_float4(o1.x, o1.y, o1.z, 0.0f);
-        }
-    }
-}
 
 // Forward + relative-L2 loss + backward-data for one 16-row tile per warp.
 // Stores the input of every layer (act) and dL/dz of every layer (dz) as
@@ -466,53 +428,90 @@ __global__ void k_to_bf16(const float* __restrict__ wf, __nv_bfloat16* __restric
     if (i < n) wb[i] = __float2bfloat16(wf[i]);
 }
 
-// Radiance-cache queries of one job per blockIdx.y: network output times the
-// path throughput is added to the pixel's in-flight radiance (one path per
-// pixel in flight, so a plain read-modify-write).
-__global__ void __launch_bounds__(kMlpThreads) k_cache_query(const JobRec* __restrict__ jobs)
+size_t train_smem() { return (size_t)(kWSmem + kWtSmem) * 2; }
+
+// The 96 input features of one query record (feature_pair) as row r of a
+// 128-row A tile in the canonical layout (K = 96): twelve 16-byte stores.
+__device__ __forceinline__ void write_features(const float4 (&q)[4], bool valid, const MlpBox& box, uint8_t* a, int r)
 {
-    const JobRec& J = jobs[blockIdx.y];
-    const CacheRec& C = J.cache;
-    if (!C.w) return;  // uniform over the block
-    const int64_t n = min((int64_t)C.q_count[0], (int64_t)J.npix);
-    if (n == 0) return;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16* ws = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    load_weights(C.w, ws, nullptr);
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int warp = threadIdx.x >> 5;
-    const int64_t tiles = (n + 15) / 16;
-    for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < tiles; tile += (int64_t)gridDim.x * 4) {
-        int64_t r0 = tile * 16 + g, r1 = r0 + 8;
-        bool v0 = r0 < n, v1 = r1 < n;
-        float4 q0[4], q1[4];
-        load_record(C.q_rec, r0, v0, q0);
-        load_record(C.q_rec, r1, v1, q1);
-        uint32_t a0[6][4];
-        input_fragments(q0, q1, v0, v1, C.box, a0);
-        float z[2][4];
-        uint32_t masks[5];
-        forward_tile<false>(ws, a0, z, masks, nullptr);
-        float3 o0, o1;
-        output_rgb(z, o0, o1);
-        if (t == 0) {
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                if (!(k ? v1 : v0)) continue;
-                float4 b = C.q_beta[k ? r1 : r0];
-                float3 o = k ? o1 : o0;
-                float4* lp = J.lpath + __float_as_int(b.w);
-                float4 l = *lp;
-                *lp = make_float4(l.x + b.x * o.x, l.y + b.y * o.y, l.z + b.z * o.z, l.w);
-            }
+    for (int j = 0; j < kMlpIn / 8; ++j) {
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float2 f = valid ? feature_pair(q, box, 8 * j + 2 * e) : make_float2(0.0f, 0.0f);
+            w[e] = pack2_bf16(f.x, f.y);
         }
+        *reinterpret_cast<uint4*>(a + canon_off(r, 8 * j, kMlpIn)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 
-size_t infer_smem() { return (size_t)kWSmem * 2; }
-size_t train_smem() { return (size_t)(kWSmem + kWtSmem) * 2; }
-
 }  // namespace
+
+// The network's shape as a fused tensor-core task (umma_mlp.cuh): all six
+// layers' packed weights (46 KB) resident in shared memory, the input tile
+// built by the threads from the query records, ReLU after the hidden layers.
+struct MlpTaskShape {
+    static constexpr int kLayers = kMlpLayers;
+    static constexpr bool kResident = true;
+    static constexpr bool kInputBulk = false;
+    __host__ __device__ static constexpr int in(int l) { return mlp_in(l); }
+    __host__ __device__ static constexpr int out(int l) { return mlp_out(l); }
+    __host__ __device__ static constexpr bool relu(int l) { return l + 1 < kMlpLayers; }
+    __host__ __device__ static constexpr uint32_t w_off(int l) { return (uint32_t)mlp_offset(l) * 2u; }
+    __device__ const void* input_tile(int64_t) const { return nullptr; }
+};
+
+// srt_mlp_infer: records in, RGB radiance (exp of the first three outputs) out.
+struct MlpInferTask : MlpTaskShape {
+    const float4* rec;
+    float4* y;
+    int64_t n;
+    MlpBox box;
+    const __nv_bfloat16* w;
+    __device__ int64_t rows() const { return n; }
+    __device__ const uint8_t* weights() const { return reinterpret_cast<const uint8_t*>(w); }
+    __device__ void make_input(int64_t row, bool valid, uint8_t* a, int r) const
+    {
+        float4 q[4];
+        load_record(rec, row, valid, q);
+        write_features(q, valid, box, a, r);
+    }
+    __device__ void store(int64_t row, const float (&o)[kMlpOut]) const
+    {
+        y[row] = make_float4(safe_exp(o[0]), safe_exp(o[1]), safe_exp(o[2]), 0.0f);
+    }
+};
+
+// The tracer's radiance-cache queries of job blockIdx.y: the network's
+// output times the path throughput is added to the pixel's in-flight
+// radiance (one path per pixel in flight, so a plain read-modify-write).
+struct CacheQueryTask : MlpTaskShape {
+    const JobRec* jobs;
+    __device__ const JobRec& job() const { return jobs[blockIdx.y]; }
+    __device__ int64_t rows() const
+    {
+        const JobRec& J = job();
+        if (!J.cache.wpack) return 0;  // a plain job
+        return min((int64_t)J.cache.q_count[0], (int64_t)J.npix);
+    }
+    __device__ const uint8_t* weights() const { return reinterpret_cast<const uint8_t*>(job().cache.wpack); }
+    __device__ void make_input(int64_t row, bool valid, uint8_t* a, int r) const
+    {
+        const CacheRec& C = job().cache;
+        float4 q[4];
+        load_record(C.q_rec, row, valid, q);
+        write_features(q, valid, C.box, a, r);
+    }
+    __device__ void store(int64_t row, const float (&o)[kMlpOut]) const
+    {
+        const JobRec& J = job();
+        const float4 b = J.cache.q_beta[row];
+        float4* lp = J.lpath + __float_as_int(b.w);
+        const float4 l = *lp;
+        *lp = make_float4(l.x + b.x * safe_exp(o[0]), l.y + b.y * safe_exp(o[1]), l.z + b.z * safe_exp(o[2]), l.w);
+    }
+};
 
 }  // namespace srt
 
@@ -535,8 +534,6 @@ srt_status configure_smem()
 {
     static bool done = false;
     if (done) return SRT_OK;
-    SRT_CUDA_TRY(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
-    SRT_CUDA_TRY(cudaFuncSetAttribute(k_cache_query, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
     SRT_CUDA_TRY(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
     done = true;
     return SRT_OK;
@@ -553,14 +550,24 @@ int grid_rows(int64_t n)
 
 namespace srt {
 
-// launches the fused inference kernel (also used by the tracer's cache path)
+srt_status mlp_pack(srt_mlp* p, cudaStream_t st)
+{
+    for (int l = 0; l < kMlpLayers; ++l)
+        SRT_TRY(umma_pack_layer(p->wf + mlp_offset(l), mlp_in(l), mlp_out(l), p->wpack + mlp_offset(l), st));
+    return SRT_OK;
+}
+
+// the fused tensor-core inference (the tracer's cache path uses the same kernel)
 srt_status mlp_infer_launch(const srt_mlp* p, const float4* rec, int64_t n, float4* out, cudaStream_t st)
 {
-    SRT_TRY(configure_smem());
     if (n <= 0) return SRT_OK;
-    k_mlp_infer<<<grid_rows(n), kMlpThreads, infer_smem(), st>>>(p->wb, p->box, rec, n, out);
-    SRT_CUDA_TRY(cudaGetLastError());
-    return SRT_OK;
+    MlpInferTask t{};
+    t.rec = rec;
+    t.y = out;
+    t.n = n;
+    t.box = p->box;
+    t.w = p->wpack;
+    return umma_mlp_launch(t, n, 1, st);
 }
 
 srt_status mlp_train_launch(srt_mlp* p, const float4* rec, const float4* target, int64_t n, float lr, bool update,
@@ -584,6 +591,8 @@ srt_status mlp_train_launch(srt_mlp* p, const float4* rec, const float4* target,
         float c1 = 1.0f - std::pow(p->b1, (float)p->step), c2 = 1.0f - std::pow(p->b2, (float)p->step);
         k_adam<<<(kMlpParams + 255) / 256, 256, 0, st>>>(p->wf, p->wb, p->m, p->v, p->grad, kMlpParams, lr, p->b1,
                                                          p->b2, p->eps, c1, c2);
+        SRT_CUDA_TRY(cudaGetLastError());
+        SRT_TRY(mlp_pack(p, st));
     }
     SRT_CUDA_TRY(cudaGetLastError());
     return SRT_OK;
@@ -593,9 +602,20 @@ MlpView mlp_view(const srt_mlp* p) { return MlpView{p->wb, p->box}; }
 
 void launch_cache_queries(const JobRec* jobs, int max_jobs, cudaStream_t st)
 {
-    configure_smem();
-    dim3 grid((unsigned)device_sm_count(), (unsigned)max_jobs);
-    k_cache_query<<<grid, kMlpThreads, infer_smem(), st>>>(jobs);
+    // the query count is read on the device: launch the resident CTAs
+    CacheQueryTask t{};
+    t.jobs = jobs;
+    umma_mlp_launch(t, (int64_t)1 << 40, (unsigned)max_jobs, st);
+}
+
+srt_status mlp_prepare_kernels()
+{
+    SRT_TRY(umma_prepare());
+    SRT_TRY(configure_smem());
+    // kernel attributes of both fused tasks, outside any stream capture
+    SRT_TRY(umma_mlp_launch(MlpInferTask{}, 0, 1, 0));
+    SRT_TRY(umma_mlp_launch(CacheQueryTask{}, 0, 1, 0));
+    return SRT_OK;
 }
 
 }  // namespace srt
@@ -607,8 +627,9 @@ extern "C" srt_status srt_mlp_create(uint64_t seed, srt_mlp** out)
     *out = nullptr;
     srt_mlp* p = new (std::nothrow) srt_mlp();
     if (!p) return set_error(SRT_ERR_OOM, "host allocation failed");
-    size_t bytes = (size_t)kMlpParams * (4 + 2 + 4 + 4 + 4) + 64;
-    srt_status st = p->params.alloc(bytes, "mlp parameters");
+    size_t bytes = (size_t)kMlpParams * (4 + 2 + 4 + 4 + 4) + 64 + 256 + (size_t)kMlpParams * 2;
+    srt_status st = mlp_prepare_kernels();
+    if (st == SRT_OK) st = p->params.alloc(bytes, "mlp parameters");
     if (st != SRT_OK) {
         delete p;
         return st;
@@ -620,6 +641,8 @@ extern "C" srt_status srt_mlp_create(uint64_t seed, srt_mlp** out)
     p->grad = p->v + kMlpParams;
     p->loss = p->grad + kMlpParams;
     p->wb = reinterpret_cast<__nv_bfloat16*>(p->loss + 16);
+    // 256-byte aligned: the kernels bulk-copy it into shared memory
+    p->wpack = reinterpret_cast<__nv_bfloat16*>((reinterpret_cast<uintptr_t>(p->wb + kMlpParams) + 255) & ~(uintptr_t)255);
     // He-uniform initialisation from a seeded 64-bit LCG; padded rows/columns are zero
     std::vector<float> w(kMlpParams, 0.0f);
     uint64_t s = seed * 6364136223846793005ULL + 1442695040888963407ULL;
@@ -643,6 +666,7 @@ extern "C" srt_status srt_mlp_create(uint64_t seed, srt_mlp** out)
         k_to_bf16<<<(kMlpParams + 255) / 256, 256>>>(p->wf, p->wb, kMlpParams);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess && mlp_pack(p, 0) != SRT_OK) e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         delete p;
@@ -679,6 +703,7 @@ extern "C" srt_status srt_mlp_set_params(srt_mlp* p, const float* host)
     SRT_CUDA_TRY(cudaMemcpy(p->wf, host, (size_t)kMlpParams * 4, cudaMemcpyHostToDevice));
     k_to_bf16<<<(kMlpParams + 255) / 256, 256>>>(p->wf, p->wb, kMlpParams);
     SRT_CUDA_TRY(cudaGetLastError());
+    SRT_TRY(mlp_pack(p, 0));
     SRT_CUDA_TRY(cudaDeviceSynchronize());
     p->step = 0;
     SRT_CUDA_TRY(cudaMemset(p->m, 0, (size_t)kMlpParams * 4 * 3));

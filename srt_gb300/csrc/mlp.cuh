@@ -1,8 +1,8 @@
 // mlp.cuh — the radiance-cache network: 96 -> 64 -> 64 -> 64 -> 64 -> 64 -> 16
 // (five hidden ReLU layers of width 64, RGB output through exp), BF16
 // weights and activations, FP32 accumulation on the tensor cores
-// (mma.sync m16n8k16), no biases (a constant-1 input feature plays the
-// first layer's bias).
+// (tcgen05.mma for inference, mma.sync m16n8k16 for training), no biases
+// (a constant-1 input feature plays the first layer's bias).
 //
 // Inputs of one query (16 floats, four float4): position (3), roughness,
 // shading normal (3), -, outgoing direction (3), -, albedo (3), -.  The
@@ -56,9 +56,10 @@ struct MlpView {
 
 // Network state: FP32 master weights, BF16 copy, Adam moments, gradient.
 struct srt_mlp {
-    srt::DeviceBuffer params;  // fp32 master | adam m | adam v | grad | loss | bf16 copy
+    srt::DeviceBuffer params;  // fp32 master | adam m | adam v | grad | loss | bf16 copy | bf16 packed
     float* wf = nullptr;
     __nv_bfloat16* wb = nullptr;
+    __nv_bfloat16* wpack = nullptr;  // bf16 weights in the tensor cores' canonical layout (umma.cuh)
     float* m = nullptr;
     float* v = nullptr;
     float* grad = nullptr;
@@ -72,6 +73,8 @@ struct srt_mlp {
 };
 
 namespace srt {
+// refreshes the packed weights from the FP32 master weights
+srt_status mlp_pack(srt_mlp* p, cudaStream_t st);
 srt_status mlp_infer_launch(const srt_mlp* p, const float4* rec, int64_t n, float4* out, cudaStream_t st);
 srt_status mlp_train_launch(srt_mlp* p, const float4* rec, const float4* target, int64_t n, float lr, bool update,
                             cudaStream_t st);

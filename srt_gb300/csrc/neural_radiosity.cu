@@ -16,15 +16,16 @@
 // 2022), real spherical harmonics of degree 3 (9 terms) on the direction
 // and on the normal, the colour as is, padded with ones to 96 columns;
 // then 96 -> 256 -> 256 -> 256 -> 256 -> 16 (3 used), ReLU, no biases,
-// BF16 weights and activations with FP32 accumulation.  The encoding is a
-// CUDA kernel here; the five layers are plain GEMMs with a ReLU epilogue
-// and go to cuBLASLt.
+// BF16 weights and activations with FP32 accumulation.  The encoding
+// kernel writes each 128-row tile in the tensor cores' canonical
+// shared-memory layout; the five layers run fused in one tcgen05 kernel
+// (umma_mlp.cuh): per 128-row tile, bulk-copied input and layer weights,
+// accumulators in tensor memory, activations kept on chip between layers.
 // Combine: LHS pixel = mask ? base : net; RHS pixel = base + weight * net
 // where the network was asked (mask = 0).  The reference's RHS combine
 // adds the network term where mask == 1, i.e. where this frame wrote no
 // network input and no weight; that reads the previous frames' buffers and
 // is not reproduced.
-#include <cublasLt.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -37,6 +38,7 @@
 #include "scene.h"
 #include "shading.cuh"
 #include "trace.cuh"
+#include "umma_mlp.cuh"
 
 namespace srt {
 
@@ -63,7 +65,10 @@ constexpr int64_t kNrGridEntries = nr_level_offset(kNrLevels);
 constexpr int64_t kNrGridParams = kNrGridEntries * kNrFeat;
 __host__ __device__ constexpr int nr_in(int l) { return l == 0 ? kNrEnc : kNrWidth; }
 __host__ __device__ constexpr int nr_out(int l) { return l == kNrLayers - 1 ? kNrOut : kNrWidth; }
-constexpr int64_t nr_w_offset(int l) { return l == 0 ? 0 : nr_w_offset(l - 1) + (int64_t)nr_in(l - 1) * nr_out(l - 1); }
+__host__ __device__ constexpr int64_t nr_w_offset(int l)
+{
+    return l == 0 ? 0 : nr_w_offset(l - 1) + (int64_t)nr_in(l - 1) * nr_out(l - 1);
+}
 constexpr int64_t kNrWeights = nr_w_offset(kNrLayers);
 constexpr int64_t kNrParams = kNrGridParams + kNrWeights;
 
@@ -231,9 +236,16 @@ __device__ __forceinline__ void sh3(float x, float y, float z, float* o)
     o[8] = 0.54627421529603959f * (x * x - y * y);
 }
 
+// byte offset of encoded column `col` of query q: 128-query tiles, each in
+// the tensor cores' canonical K-major layout (umma.cuh) with K = 96
+__device__ __forceinline__ size_t nr_enc_off(int64_t q, int col)
+{
+    return (size_t)(q / kUmmaRows) * (kUmmaRows * kNrEnc * 2) + canon_off((int)(q % kUmmaRows), col, kNrEnc);
+}
+
 // one thread per (query, level); level threads also write the other columns
 __global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inputs, int64_t n,
-                                                   const float* __restrict__ grid, __nv_bfloat16* __restrict__ out)
+                                                   const float* __restrict__ grid, uint8_t* __restrict__ out)
 {
     const int64_t total = n * kNrLevels;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -241,7 +253,9 @@ __global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inp
         const int64_t q = t / kNrLevels;
         const int l = (int)(t % kNrLevels);
         const float* in = inputs + 12 * q;
-        __nv_bfloat16* o = out + kNrEnc * q;
+        auto put = [&](int col, float v) {
+            *reinterpret_cast<__nv_bfloat16*>(out + nr_enc_off(q, col)) = __float2bfloat16_rn(v);
+        };
         const float scale = (float)nr_level_res(l) - 1.0f;
         const int64_t res = nr_level_res(l);
         const bool dense = nr_level_size(l) == res * res * res;
@@ -279,24 +293,24 @@ __global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inp
             acc[6] += wc * f1.z;
             acc[7] += wc * f1.w;
         }
-        for (int k = 0; k < kNrFeat; ++k) o[l * kNrFeat + k] = __float2bfloat16_rn(acc[k]);
+        // the level's 8 features are one 16-byte row of a core matrix
+        uint4 q8;
+        q8.x = pack2_bf16(acc[0], acc[1]);
+        q8.y = pack2_bf16(acc[2], acc[3]);
+        q8.z = pack2_bf16(acc[4], acc[5]);
+        q8.w = pack2_bf16(acc[6], acc[7]);
+        *reinterpret_cast<uint4*>(out + nr_enc_off(q, l * kNrFeat)) = q8;
         if (l == 0) {
             float sd[9], sn[9];
             sh3(in[3] * 2.0f - 1.0f, in[4] * 2.0f - 1.0f, in[5] * 2.0f - 1.0f, sd);
             sh3(in[6] * 2.0f - 1.0f, in[7] * 2.0f - 1.0f, in[8] * 2.0f - 1.0f, sn);
             const int b0 = kNrLevels * kNrFeat;
-            for (int k = 0; k < 9; ++k) o[b0 + k] = __float2bfloat16_rn(sd[k]);
-            for (int k = 0; k < 9; ++k) o[b0 + 9 + k] = __float2bfloat16_rn(sn[k]);
-            for (int k = 0; k < 3; ++k) o[b0 + 18 + k] = __float2bfloat16_rn(in[9 + k]);
-            for (int k = kNrEncUsed; k < kNrEnc; ++k) o[k] = __float2bfloat16_rn(1.0f);
+            for (int k = 0; k < 9; ++k) put(b0 + k, sd[k]);
+            for (int k = 0; k < 9; ++k) put(b0 + 9 + k, sn[k]);
+            for (int k = 0; k < 3; ++k) put(b0 + 18 + k, in[9 + k]);
+            for (int k = kNrEncUsed; k < kNrEnc; ++k) put(k, 1.0f);
         }
     }
-}
-
-__global__ void __launch_bounds__(256) k_nr_to_bf16(const float* __restrict__ w, int64_t n, __nv_bfloat16* __restrict__ o)
-{
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) o[i] = __float2bfloat16_rn(w[i]);
 }
 
 __global__ void __launch_bounds__(256) k_nr_combine(const uint8_t* __restrict__ mask, const float* __restrict__ base,
@@ -355,88 +369,64 @@ struct Pcg {
 
 }  // namespace
 
+// The network as a fused tensor-core task (umma_mlp.cuh): the encoded input
+// tiles are bulk-copied, the layers' packed weights streamed layer by layer
+// (256 x 256 BF16 = 128 KB each), ReLU after every hidden layer, the 16
+// outputs of each row stored as FP32.
+struct NrNetTask {
+    const uint8_t* x;   // encoded inputs, 128-row canonical tiles (k_nr_encode)
+    const uint8_t* w;   // packed weights, layer l at w_off(l)
+    float* y;           // n x 16 outputs
+    int64_t n;
+    static constexpr int kLayers = kNrLayers;
+    static constexpr bool kResident = false;
+    static constexpr bool kInputBulk = true;
+    __host__ __device__ static constexpr int in(int l) { return nr_in(l); }
+    __host__ __device__ static constexpr int out(int l) { return nr_out(l); }
+    __host__ __device__ static constexpr bool relu(int l) { return l + 1 < kNrLayers; }
+    __host__ __device__ static constexpr uint32_t w_off(int l) { return (uint32_t)(nr_w_offset(l) * 2); }
+    __device__ int64_t rows() const { return n; }
+    __device__ const uint8_t* weights() const { return w; }
+    __device__ const void* input_tile(int64_t t) const { return x + (size_t)t * (kUmmaRows * kNrEnc * 2); }
+    __device__ void make_input(int64_t, bool, uint8_t*, int) const {}
+    __device__ void store(int64_t row, const float (&o)[kNrOut]) const
+    {
+        float4* p = reinterpret_cast<float4*>(y + (size_t)kNrOut * row);
+#pragma unroll
+        for (int k = 0; k < kNrOut / 4; ++k) p[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+    }
+};
+
 }  // namespace srt
 
 using namespace srt;
 
 struct srt_nr {
     DeviceBuffer params;   // fp32: grid | weights
-    DeviceBuffer w16;      // bf16 weights
-    DeviceBuffer act0, act1, out, work;
-    int64_t cap = 0;       // rows the activation buffers hold
-    cublasLtHandle_t lt = nullptr;
-    ~srt_nr()
-    {
-        if (lt) cublasLtDestroy(lt);
-    }
+    DeviceBuffer wpack;    // bf16 weights in the canonical layout, layer after layer
+    DeviceBuffer enc, out; // encoded inputs (128-row tiles), network outputs
+    int64_t cap = 0;       // rows the buffers hold (a multiple of 128)
 };
 
 namespace {
 
-srt_status lt_check(cublasStatus_t s, const char* what)
-{
-    return s == CUBLAS_STATUS_SUCCESS ? SRT_OK
-                                      : set_error(SRT_ERR_CUDA, std::string("cuBLASLt ") + what + " failed (" +
-                                                                    std::to_string((int)s) + ")");
-}
-
-// D[n x out] = act(X[n x in] W^T), row-major, through cuBLASLt column-major views
-srt_status nr_gemm(srt_nr* nr, const __nv_bfloat16* W, int in, int outd, const __nv_bfloat16* X, void* D, int64_t n,
-                   bool relu, bool f32_out, cudaStream_t st)
-{
-    cublasLtMatmulDesc_t op = nullptr;
-    cublasLtMatrixLayout_t la = nullptr, lb = nullptr, ld = nullptr;
-    cublasLtMatmulPreference_t pref = nullptr;
-    srt_status s = lt_check(cublasLtMatmulDescCreate(&op, CUBLAS_COMPUTE_32F, CUDA_R_32F), "desc");
-    const cublasOperation_t ta = CUBLAS_OP_T, tb = CUBLAS_OP_N;
-    const cublasLtEpilogue_t epi = relu ? CUBLASLT_EPILOGUE_RELU : CUBLASLT_EPILOGUE_DEFAULT;
-    if (s == SRT_OK) s = lt_check(cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)), "transa");
-    if (s == SRT_OK) s = lt_check(cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)), "transb");
-    if (s == SRT_OK) s = lt_check(cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_EPILOGUE, &epi, sizeof(epi)), "epilogue");
-    if (s == SRT_OK) s = lt_check(cublasLtMatrixLayoutCreate(&la, CUDA_R_16BF, in, outd, in), "layout A");
-    if (s == SRT_OK) s = lt_check(cublasLtMatrixLayoutCreate(&lb, CUDA_R_16BF, in, (uint64_t)n, in), "layout B");
-    if (s == SRT_OK)
-        s = lt_check(cublasLtMatrixLayoutCreate(&ld, f32_out ? CUDA_R_32F : CUDA_R_16BF, outd, (uint64_t)n, outd),
-                     "layout D");
-    const size_t ws = nr->work.bytes();
-    if (s == SRT_OK) s = lt_check(cublasLtMatmulPreferenceCreate(&pref), "preference");
-    if (s == SRT_OK)
-        s = lt_check(cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &ws,
-                                                          sizeof(ws)),
-                     "workspace");
-    cublasLtMatmulHeuristicResult_t hr{};
-    int found = 0;
-    if (s == SRT_OK) s = lt_check(cublasLtMatmulAlgoGetHeuristic(nr->lt, op, la, lb, ld, ld, pref, 1, &hr, &found), "heuristic");
-    if (s == SRT_OK && found == 0) s = set_error(SRT_ERR_CUDA, "cuBLASLt found no algorithm for the network layer");
-    const float alpha = 1.0f, beta = 0.0f;
-    if (s == SRT_OK)
-        s = lt_check(cublasLtMatmul(nr->lt, op, &alpha, W, la, X, lb, &beta, D, ld, D, ld, &hr.algo, nr->work.get(), ws,
-                                    st),
-                     "matmul");
-    if (pref) cublasLtMatmulPreferenceDestroy(pref);
-    if (ld) cublasLtMatrixLayoutDestroy(ld);
-    if (lb) cublasLtMatrixLayoutDestroy(lb);
-    if (la) cublasLtMatrixLayoutDestroy(la);
-    if (op) cublasLtMatmulDescDestroy(op);
-    return s;
-}
-
 srt_status nr_reserve(srt_nr* nr, int64_t n)
 {
     if (n <= nr->cap) return SRT_OK;
-    const int64_t c = std::max<int64_t>(n, 1 << 16);
-    SRT_TRY(nr->act0.alloc((size_t)c * kNrWidth * 2, "network activations"));
-    SRT_TRY(nr->act1.alloc((size_t)c * kNrWidth * 2, "network activations"));
+    const int64_t c = (std::max<int64_t>(n, 1 << 16) + kUmmaRows - 1) / kUmmaRows * kUmmaRows;
+    SRT_TRY(nr->enc.alloc((size_t)c * kNrEnc * 2, "network inputs"));
     SRT_TRY(nr->out.alloc((size_t)c * kNrOut * 4, "network output"));
+    // rows of the last tile beyond n are computed and not stored: keep them finite
+    SRT_CUDA_TRY(cudaMemset(nr->enc.get(), 0, (size_t)c * kNrEnc * 2));
     nr->cap = c;
     return SRT_OK;
 }
 
 srt_status nr_sync_weights(srt_nr* nr)
 {
-    k_nr_to_bf16<<<grid_for(kNrWeights, 256), 256>>>(nr->params.as<float>() + kNrGridParams, kNrWeights,
-                                                      nr->w16.as<__nv_bfloat16>());
-    SRT_CUDA_TRY(cudaGetLastError());
+    for (int l = 0; l < kNrLayers; ++l)
+        SRT_TRY(umma_pack_layer(nr->params.as<float>() + kNrGridParams + nr_w_offset(l), nr_in(l), nr_out(l),
+                                nr->wpack.as<__nv_bfloat16>() + nr_w_offset(l), 0));
     return SRT_OK;
 }
 
@@ -455,11 +445,10 @@ extern "C" srt_status srt_nr_create(uint64_t seed, srt_nr** out)
         delete nr;
         return st;
     };
-    srt_status st = nr->params.alloc((size_t)kNrParams * 4, "network parameters");
-    if (st == SRT_OK) st = nr->w16.alloc((size_t)kNrWeights * 2, "network weights");
-    if (st == SRT_OK) st = nr->work.alloc(32u << 20, "cuBLASLt workspace");
+    srt_status st = umma_prepare();
+    if (st == SRT_OK) st = nr->params.alloc((size_t)kNrParams * 4, "network parameters");
+    if (st == SRT_OK) st = nr->wpack.alloc((size_t)kNrWeights * 2, "network weights");
     if (st != SRT_OK) return fail(st);
-    if (cublasLtCreate(&nr->lt) != CUBLAS_STATUS_SUCCESS) return fail(set_error(SRT_ERR_CUDA, "cublasLtCreate failed"));
     // initialisation as tiny-cuda-nn does it: grid features U(-1e-4, 1e-4),
     // layer weights U(-s, s) with s = sqrt(6 / (fan_in + fan_out))
     std::vector<float> p((size_t)kNrParams);
@@ -535,20 +524,14 @@ extern "C" srt_status srt_nr_infer(srt_nr* nr, const float* inputs, int64_t n, f
     if (!nr || (n > 0 && (!inputs || !out))) return set_error(SRT_ERR_ARG, "NULL argument");
     if (n < 0) return set_error(SRT_ERR_ARG, "negative count");
     if (n == 0) return SRT_OK;
+    if (reinterpret_cast<uintptr_t>(out) % 16) return set_error(SRT_ERR_ARG, "out must be 16-byte aligned");
     cudaStream_t st = as_stream(stream);
     SRT_TRY(nr_reserve(nr, n));
-    __nv_bfloat16* a0 = nr->act0.as<__nv_bfloat16>();
-    __nv_bfloat16* a1 = nr->act1.as<__nv_bfloat16>();
-    k_nr_encode<<<grid_for(n * kNrLevels, 256), 256, 0, st>>>(inputs, n, nr->params.as<float>(), a0);
+    uint8_t* enc = nr->enc.as<uint8_t>();
+    k_nr_encode<<<grid_for(n * kNrLevels, 256), 256, 0, st>>>(inputs, n, nr->params.as<float>(), enc);
     SRT_CUDA_TRY(cudaGetLastError());
-    const __nv_bfloat16* w = nr->w16.as<__nv_bfloat16>();
-    for (int l = 0; l < kNrLayers; ++l) {
-        const bool last = l == kNrLayers - 1;
-        SRT_TRY(nr_gemm(nr, w + nr_w_offset(l), nr_in(l), nr_out(l), a0, last ? (void*)out : (void*)a1, n, !last, last,
-                        st));
-        std::swap(a0, a1);
-    }
-    return SRT_OK;
+    NrNetTask task{enc, nr->wpack.as<uint8_t>(), out, n};
+    return umma_mlp_launch(task, n, 1, st);
 }
 
 extern "C" srt_status srt_nr_trace(const srt_scene* s, int32_t width, int32_t height, int32_t type, int32_t seed,
@@ -609,5 +592,5 @@ extern "C" srt_status srt_nr_render(const srt_scene* s, srt_nr* nr, int32_t widt
         SRT_CUDA_TRY(cudaGetLastError());
     }
     SRT_CUDA_TRY(cudaStreamSynchronize(st));
-    return SRT_OK;
+    return umma_take_error();
 }

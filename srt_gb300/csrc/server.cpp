@@ -128,6 +128,7 @@ struct srt_server {
             char* cb = b + px_bytes + frames_bytes(spp);
             CacheRec& C = J.cache;
             C.w = j.desc.cache->wb;
+            C.wpack = j.desc.cache->wpack;
             C.box = j.desc.cache->box;
             C.q_rec = reinterpret_cast<float4*>(cb);
             C.q_beta = reinterpret_cast<float4*>(cb + n * 64);

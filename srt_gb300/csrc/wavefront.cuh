@@ -24,6 +24,7 @@ namespace srt {
 // records up to 8 vertices whose targets are computed when it ends.
 struct CacheRec {
     const __nv_bfloat16* w;   // network weights (bf16); null = plain job
+    const __nv_bfloat16* wpack;  // the same weights in the tensor cores' canonical layout
     MlpBox box;
     float4* q_rec;            // [npix * 4] query records
     float4* q_beta;           // [npix] throughput (rgb), pixel (int bits)
