@@ -25,7 +25,8 @@ counters that bound the kernel (`limiter`); `cache` (learned-cache time to
 the plain tracer's 64-spp relMSE, 1280x720), `serving` (Poisson arrivals at
 several rates under a 150 GB budget), `bxdf` (the Disney BSDF batch of 2^20
 points, with its FP64 parity), `cornell` (the Cornell box at 512x512, 16 spp,
-depth 8, with its roofline), `cpu_baseline`.  `--no-cache`, `--no-serving`,
+depth 8, with its roofline), `mlp` (the two networks' tcgen05 kernels on
+2,073,600 rows against the measured bf16 GEMM rate), `cpu_baseline`.  `--no-cache`, `--no-serving`,
 `--no-cpu-baseline` skip those parts; `--profile-case spheres|cornell` runs
 the short case the ncu captures use.
 """
@@ -55,6 +56,15 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def tensor_peak():
+    """Dense bf16 TFLOP/s of a cuBLAS GEMM timed alone (burst)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
 
 
 class Clocks:
@@ -300,6 +310,65 @@ def bxdf_eval_bench(S, n=1 << 20, launches=20, cpu=True):
     return out
 
 
+def mlp_eval(S, n=1920 * 1080, reps=10):
+    """The two networks' tensor-core kernels (tcgen05.mma, accumulators in
+    tensor memory) on n rows.  NeuralRadiosity's network 96 -> 256 x 4 -> 16
+    (srt_nr_infer: the encoding kernel and the fused five-layer kernel, each
+    timed with the handle's profiling events) and the radiance cache's
+    96 -> 64 x 5 -> 16 (srt_mlp_infer, features built in the kernel; CUDA
+    events).  FLOPs per row = 2 * sum(in * out) over the layers; roofline
+    against the measured dense bf16 GEMM rate."""
+    import ctypes as C
+    import torch
+    L = S.lib()
+    peak, kind = tensor_peak()
+    dev = torch.device("cuda")
+    out = {}
+    nr = C.c_void_p()
+    S.check(L.srt_nr_create(7, C.byref(nr)))
+    x = torch.rand((n, 12), device=dev)
+    y = torch.empty((n, 16), device=dev)
+    S.check(L.srt_nr_set_profiling(nr, 1))
+    st = S._capi.NrStats()
+    enc, net = [], []
+    for i in range(reps + 3):
+        S.check(L.srt_nr_infer(nr, C.c_void_p(x.data_ptr()), n, C.c_void_p(y.data_ptr()), None))
+        S.check(L.srt_nr_get_stats(nr, C.byref(st)))
+        if i >= 3:
+            enc.append(st.encode_ms)
+            net.append(st.network_ms)
+    L.srt_nr_destroy(nr)
+    flops = 2.0 * n * (96 * 256 + 3 * 256 * 256 + 256 * 16)
+    ms = statistics.median(net)
+    tf = flops / (ms / 1e3) / 1e12
+    out["neural_radiosity"] = {"rows": n, "network_ms": round(ms, 4), "encode_ms": round(statistics.median(enc), 4),
+                               "roofline": {"bound": "tensor", "kernel": "k_umma_mlp_stream<NrNetTask>", "achieved": round(tf, 1),
+                                            "peak": peak, "peak_kind": kind, "unit": "TFLOP/s",
+                                            "frac": round(tf / peak, 4), "flops_per_row": flops / n}}
+    mlp = C.c_void_p()
+    S.check(L.srt_mlp_create(3, C.byref(mlp)))
+    rec = torch.rand((n, 16), device=dev)
+    o4 = torch.empty((n, 4), device=dev)
+    call = lambda: S.check(L.srt_mlp_infer(mlp, C.c_void_p(rec.data_ptr()), n, C.c_void_p(o4.data_ptr()), None))
+    for _ in range(3):
+        call()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, b in evs:
+        a.record()
+        call()
+        b.record()
+    torch.cuda.synchronize()
+    L.srt_mlp_destroy(mlp)
+    ms2 = statistics.median(a.elapsed_time(b) for a, b in evs)
+    flops2 = 2.0 * n * (96 * 64 + 4 * 64 * 64 + 64 * 16)
+    tf2 = flops2 / (ms2 / 1e3) / 1e12
+    out["radiance_cache"] = {"rows": n, "kernel_ms": round(ms2, 4),
+                             "roofline": {"bound": "tensor", "kernel": "k_umma_mlp<MlpInferTask>", "achieved": round(tf2, 1),
+                                          "peak": peak, "peak_kind": kind, "unit": "TFLOP/s",
+                                          "frac": round(tf2 / peak, 4), "flops_per_row": flops2 / n}}
+    return out
+
+
 KERNELS = ["k_closest", "k_shade", "k_shadow", "k_regen", "k_advance"]
 # queue bytes a closest-hit ray moves in k_closest (origin 16 B, direction 16 B,
 # job word 4 B in; hit record 16 B out)
@@ -455,16 +524,20 @@ def cache_bound(S, scene, ref, w, h, frames=128):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) / 3 / 64 * 1e3
 
-    e_full, e_prefix = rel_per_sample(MAX_DEPTH), rel_per_sample(1)
-    t_full, t_prefix, t_prefix2 = per_sample_ms(MAX_DEPTH), per_sample_ms(1), per_sample_ms(2)
-    r = e_prefix / e_full
+    e_full, e1, e2 = rel_per_sample(MAX_DEPTH), rel_per_sample(1), rel_per_sample(2)
+    t_full, t1, t2 = per_sample_ms(MAX_DEPTH), per_sample_ms(1), per_sample_ms(2)
+    r1, r2 = e1 / e_full, e2 / e_full
     pt.close()
-    return {"frames_for_variance": frames, "relmse_per_sample_plain": e_full, "relmse_per_sample_prefix": e_prefix,
-            "variance_ratio_prefix_over_plain": round(r, 4),
-            "samples_a_perfect_cache_needs": round(64 * r, 1),
-            "ms_per_sample_plain_depth16": round(t_full, 4), "ms_per_sample_prefix_depth1": round(t_prefix, 4),
-            "ms_per_sample_depth2": round(t_prefix2, 4),
-            "max_speedup_any_second_vertex_cache": round((t_full / t_prefix) / r, 3)}
+    # the prefix a second-vertex cache keeps lies between depth 1 (no emission
+    # at the second vertex) and depth 2 (also its next-event estimate, which
+    # the cache replaces); its cost lies between theirs as well
+    return {"frames_for_variance": frames, "relmse_per_sample_plain": e_full,
+            "relmse_per_sample_depth1": e1, "relmse_per_sample_depth2": e2,
+            "variance_ratio_depth1": round(r1, 4), "variance_ratio_depth2": round(r2, 4),
+            "samples_a_perfect_cache_needs": [round(64 * r1, 1), round(64 * r2, 1)],
+            "ms_per_sample_plain_depth16": round(t_full, 4), "ms_per_sample_depth1": round(t1, 4),
+            "ms_per_sample_depth2": round(t2, 4),
+            "max_speedup_any_second_vertex_cache": [round((t_full / t2) / r2, 3), round((t_full / t1) / r1, 3)]}
 
 
 def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_spp=64):
@@ -564,6 +637,35 @@ def profile_case(which="spheres"):
     launch; a few hundred launches in all."""
     import torch
     import srt_gb300 as S
+    if which == "cache":
+        # radiance-cache frames of the learned-cache workload (1280x720, 1 spp,
+        # online training on 2^16 paths per frame), every kernel launched directly
+        import ctypes as C
+        import numpy as np
+        w, h = 1280, 720
+        arrays = build_scene(S)
+        arrays.set_aspect(w / h)
+        scene = S.Scene(arrays)
+        verts = np.concatenate([m["vertices"] for m in arrays.meshes])
+        lo, hi = verts.min(0) - 0.05, verts.max(0) + 0.05
+        mlp = C.c_void_p()
+        S.check(S.lib().srt_mlp_create(1, C.byref(mlp)))
+        S.check(S.lib().srt_mlp_set_box(mlp, (C.c_float * 3)(*lo), (C.c_float * 3)(*hi)))
+        pt = S.PathTracer(scene, w, h)
+        pt.set_launch_mode(S.LAUNCH_DIRECT)
+        film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+        cp = S._capi.CacheParams(1 << 16, 4, 1e-2, 0.5, 16, 1)
+        st = S._capi.CacheStats()
+        rows = []
+        for f in range(8):
+            p = S.pt_params(1, MAX_DEPTH, RR_DEPTH, 1, 1, 9000 + f)
+            S.check(S.lib().srt_pt_render_cached(pt.handle, C.c_void_p(film.data_ptr()), C.byref(p), mlp,
+                                                 C.byref(cp), C.byref(st), None))
+            rows.append({"queries": st.queries, "fallback": st.fallback_queries, "train_vertices": st.train_vertices})
+        torch.cuda.synchronize()
+        S.lib().srt_mlp_destroy(mlp)
+        print(json.dumps({"profile_case": "cache 1280x720 8 frames", "frames": rows}))
+        return
     if which == "cornell":
         arrays = S.procedural("cornell")
         arrays.set_aspect(1.0)
@@ -609,7 +711,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     ap.add_argument("--serving-rates", default="5,20,50", help="Poisson arrival rates (jobs/s) of the sweep")
     ap.add_argument("--serving-duration", type=float, default=30.0, help="seconds of arrivals per rate")
-    ap.add_argument("--profile-case", nargs="?", const="spheres", default=None, choices=["spheres", "cornell"],
+    ap.add_argument("--profile-case", nargs="?", const="spheres", default=None, choices=["spheres", "cornell", "cache"],
                     help="short run for ncu captures (direct launches)")
     args = ap.parse_args()
     if args.profile_case:
@@ -749,6 +851,7 @@ def main():
         }
         line["bxdf"] = bxdf_eval_bench(S, cpu=not args.no_cpu_baseline)
         line["cornell"] = cornell_eval(S, cpu=not args.no_cpu_baseline)
+        line["mlp"] = mlp_eval(S)
         if not args.no_cache:
             line["cache"] = cache_eval(S, arrays, scene)
         if not args.no_serving:

@@ -300,8 +300,21 @@ srt_status srt_nr_set_params(srt_nr* nr, const float* host_params);
  * serialisation is not read). */
 srt_status srt_nr_save(const srt_nr* nr, const char* path);
 srt_status srt_nr_load(srt_nr* nr, const char* path);
-/* inputs: n x 12 floats (device), out: n x 16 floats (device; 3 used). */
+/* inputs: n x 12 floats (device), out: n x 16 floats (device, 16-byte
+ * aligned; 3 used).  The encoding kernel writes 128-row tiles; the five
+ * layers run in one fused tensor-core kernel. */
 srt_status srt_nr_infer(srt_nr* nr, const float* inputs, int64_t n, float* out, void* stream);
+/* Profiling of srt_nr_infer (PROFILE() scopes of src/utils/profiler.h:219
+ * applied to its two kernels): enable = 1 records CUDA events around the
+ * encoding and the fused network kernel of every call and waits for them;
+ * the last call's durations are read with srt_nr_get_stats. */
+typedef struct srt_nr_stats {
+    int64_t rows;            /* rows of the last profiled call            */
+    float encode_ms;         /* hash-grid + SH encoding kernel            */
+    float network_ms;        /* fused five-layer tensor-core kernel       */
+} srt_nr_stats;
+srt_status srt_nr_set_profiling(srt_nr* nr, int32_t enable);
+srt_status srt_nr_get_stats(const srt_nr* nr, srt_nr_stats* stats);
 void srt_nr_destroy(srt_nr* nr);
 /* The LHS / RHS raygen of one sample with frame seed `seed` (curand stream
  * seed + pixel): mask (w*h bytes: 1 = the pixel needs no network), base

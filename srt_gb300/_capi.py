@@ -120,6 +120,10 @@ class CacheParams(C.Structure):
                 ("region_threshold", C.c_float), ("region_res", C.c_int32), ("train", C.c_int32)]
 
 
+class NrStats(C.Structure):
+    _fields_ = [("rows", C.c_int64), ("encode_ms", C.c_float), ("network_ms", C.c_float)]
+
+
 class CacheStats(C.Structure):
     _fields_ = [("queries", C.c_int64), ("fallback_queries", C.c_int64), ("train_vertices", C.c_int64),
                 ("loss", C.c_float), ("disabled_cells", C.c_int32), ("trace_ms", C.c_float),
@@ -154,6 +158,8 @@ _PROTOS = [
     ("srt_nr_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("srt_nr_load", C.c_int, [C.c_void_p, C.c_char_p]),
     ("srt_nr_infer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("srt_nr_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
+    ("srt_nr_get_stats", C.c_int, [C.c_void_p, C.c_void_p]),
     ("srt_nr_destroy", None, [C.c_void_p]),
     ("srt_nr_trace", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p]),

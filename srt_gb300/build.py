@@ -25,6 +25,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # the reference formulas with the same roundings as the FP32 oracle (explicit
 # fmaf calls in the BVH slab tests stay fused)
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
+# build-time switches of the kernels (e.g. "-DSRT_NODE_EVICT_LAST=1"); a change
+# needs a clean rebuild (clean())
+NVCC_FLAGS += os.environ.get("SRT_NVCC_DEFINES", "").split()
 # host translation units: -ffp-contract=off keeps host float math identical
 # on x86-64 and aarch64 (scene flattening, CDFs, camera set-up)
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", os.path.join(CUDA, "include")]

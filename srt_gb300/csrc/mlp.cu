@@ -403,11 +403,21 @@ __global__ void k_dw_reduce(const float* __restrict__ partial, int chunks, float
     }
 }
 
+// Element i of the parameter vector (W_l[out][in], layer after layer) in the
+// packed canonical layout of the tensor-core kernels.
+__device__ __forceinline__ int packed_index(int i)
+{
+    int l = 0;
+    while (l + 1 < kMlpLayers && i >= mlp_offset(l + 1)) ++l;
+    const int j = i - mlp_offset(l), in = mlp_in(l);
+    return mlp_offset(l) + (int)(canon_off(j / in, j % in, in) / 2);
+}
+
 // Adam (Kingma & Ba 2015) on the FP32 master weights; refreshes the bf16
-// copy and clears the gradient.
-__global__ void k_adam(float* __restrict__ wf, __nv_bfloat16* __restrict__ wb, float* __restrict__ m,
-                       float* __restrict__ v, float* __restrict__ grad, int n, float lr, float b1, float b2,
-                       float eps, float c1, float c2)
+// copy and its packed canonical copy, and clears the gradient.
+__global__ void k_adam(float* __restrict__ wf, __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wpack,
+                       float* __restrict__ m, float* __restrict__ v, float* __restrict__ grad, int n, float lr,
+                       float b1, float b2, float eps, float c1, float c2)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -419,6 +429,7 @@ __global__ void k_adam(float* __restrict__ wf, __nv_bfloat16* __restrict__ wb, f
     float wi = wf[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
     wf[i] = wi;
     wb[i] = __float2bfloat16(wi);
+    wpack[packed_index(i)] = __float2bfloat16_rn(wi);
     grad[i] = 0.0f;
 }
 
@@ -589,10 +600,8 @@ srt_status mlp_train_launch(srt_mlp* p, const float4* rec, const float4* target,
     if (update) {
         p->step += 1;
         float c1 = 1.0f - std::pow(p->b1, (float)p->step), c2 = 1.0f - std::pow(p->b2, (float)p->step);
-        k_adam<<<(kMlpParams + 255) / 256, 256, 0, st>>>(p->wf, p->wb, p->m, p->v, p->grad, kMlpParams, lr, p->b1,
-                                                         p->b2, p->eps, c1, c2);
-        SRT_CUDA_TRY(cudaGetLastError());
-        SRT_TRY(mlp_pack(p, st));
+        k_adam<<<(kMlpParams + 255) / 256, 256, 0, st>>>(p->wf, p->wb, p->wpack, p->m, p->v, p->grad, kMlpParams, lr,
+                                                         p->b1, p->b2, p->eps, c1, c2);
     }
     SRT_CUDA_TRY(cudaGetLastError());
     return SRT_OK;

@@ -369,9 +369,10 @@ struct Pcg {
 
 }  // namespace
 
-// The network as a fused tensor-core task (umma_mlp.cuh): the encoded input
-// tiles are bulk-copied, the layers' packed weights streamed layer by layer
-// (256 x 256 BF16 = 128 KB each), ReLU after every hidden layer, the 16
+// The network as a fused tensor-core task (umma_mlp.cuh, streaming kernel):
+// the encoded input tiles are bulk-copied two at a time, the layers' packed
+// weights streamed in 32-column K-chunks (16 KB for a 256-wide layer)
+// through the shared-memory ring, ReLU after every hidden layer, the 16
 // outputs of each row stored as FP32.
 struct NrNetTask {
     const uint8_t* x;   // encoded inputs, 128-row canonical tiles (k_nr_encode)
@@ -406,6 +407,14 @@ struct srt_nr {
     DeviceBuffer wpack;    // bf16 weights in the canonical layout, layer after layer
     DeviceBuffer enc, out; // encoded inputs (128-row tiles), network outputs
     int64_t cap = 0;       // rows the buffers hold (a multiple of 128)
+    bool profile = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    srt_nr_stats stats{};
+    ~srt_nr()
+    {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
 };
 
 namespace {
@@ -425,8 +434,8 @@ srt_status nr_reserve(srt_nr* nr, int64_t n)
 srt_status nr_sync_weights(srt_nr* nr)
 {
     for (int l = 0; l < kNrLayers; ++l)
-        SRT_TRY(umma_pack_layer(nr->params.as<float>() + kNrGridParams + nr_w_offset(l), nr_in(l), nr_out(l),
-                                nr->wpack.as<__nv_bfloat16>() + nr_w_offset(l), 0));
+        SRT_TRY(umma_pack_layer_chunked(nr->params.as<float>() + kNrGridParams + nr_w_offset(l), nr_in(l), nr_out(l),
+                                        nr->wpack.as<__nv_bfloat16>() + nr_w_offset(l), 0));
     return SRT_OK;
 }
 
@@ -528,10 +537,39 @@ extern "C" srt_status srt_nr_infer(srt_nr* nr, const float* inputs, int64_t n, f
     cudaStream_t st = as_stream(stream);
     SRT_TRY(nr_reserve(nr, n));
     uint8_t* enc = nr->enc.as<uint8_t>();
+    if (nr->profile) SRT_CUDA_TRY(cudaEventRecord(nr->ev[0], st));
     k_nr_encode<<<grid_for(n * kNrLevels, 256), 256, 0, st>>>(inputs, n, nr->params.as<float>(), enc);
     SRT_CUDA_TRY(cudaGetLastError());
+    if (nr->profile) SRT_CUDA_TRY(cudaEventRecord(nr->ev[1], st));
     NrNetTask task{enc, nr->wpack.as<uint8_t>(), out, n};
-    return umma_mlp_launch(task, n, 1, st);
+    SRT_TRY(umma_mlp_stream_launch(task, n, st));
+    if (nr->profile) {
+        SRT_CUDA_TRY(cudaEventRecord(nr->ev[2], st));
+        SRT_CUDA_TRY(cudaEventSynchronize(nr->ev[2]));
+        nr->stats.rows = n;
+        SRT_CUDA_TRY(cudaEventElapsedTime(&nr->stats.encode_ms, nr->ev[0], nr->ev[1]));
+        SRT_CUDA_TRY(cudaEventElapsedTime(&nr->stats.network_ms, nr->ev[1], nr->ev[2]));
+        SRT_TRY(umma_take_error());
+    }
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_nr_set_profiling(srt_nr* nr, int32_t enable)
+{
+    clear_error();
+    if (!nr || enable < 0 || enable > 1) return set_error(SRT_ERR_ARG, "bad arguments");
+    if (enable && !nr->ev[0])
+        for (cudaEvent_t& e : nr->ev) SRT_CUDA_TRY(cudaEventCreate(&e));
+    nr->profile = enable != 0;
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_nr_get_stats(const srt_nr* nr, srt_nr_stats* stats)
+{
+    clear_error();
+    if (!nr || !stats) return set_error(SRT_ERR_ARG, "NULL argument");
+    *stats = nr->stats;
+    return SRT_OK;
 }
 
 extern "C" srt_status srt_nr_trace(const srt_scene* s, int32_t width, int32_t height, int32_t type, int32_t seed,

@@ -189,6 +189,24 @@ __device__ __forceinline__ void tmem_ld_wait()
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Named barrier `id` over `count` threads (a multiple of 32) whose result is
+// the AND of every participant's `v` (bar.red.and.pred).
+__device__ __forceinline__ bool named_bar_and(uint32_t id, uint32_t count, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n"
+        " .reg .pred p, q;\n"
+        " setp.ne.u32 p, %1, 0;\n"
+        " bar.red.and.pred q, %2, %3, p;\n"
+        " selp.u32 %0, 1, 0, q;\n"
+        "}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+}
+
 __device__ __forceinline__ uint32_t pack2_bf16(float lo, float hi)
 {
     uint32_t r;

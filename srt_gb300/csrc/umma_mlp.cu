@@ -22,6 +22,17 @@ __global__ void k_pack_canonical(const float* __restrict__ src, int in, int out,
     }
 }
 
+__global__ void k_pack_chunked(const float* __restrict__ src, int in, int out, __nv_bfloat16* __restrict__ dst)
+{
+    const int64_t n = (int64_t)in * out;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int r = (int)(i / in), k = (int)(i % in);
+        const size_t chunk = (size_t)(k / kChunkK) * out * kChunkK;  // elements before the chunk
+        dst[chunk + canon_off(r, k % kChunkK, kChunkK) / 2] = __float2bfloat16_rn(src[i]);
+    }
+}
+
 std::mutex g_mu;
 int* g_err[128] = {};
 
@@ -32,6 +43,16 @@ srt_status umma_pack_layer(const float* src, int in, int out, __nv_bfloat16* dst
     if (in % 16 || out % 16 || in <= 0 || out <= 0) return set_error(SRT_ERR_ARG, "layer shape not a multiple of 16");
     const int64_t n = (int64_t)in * out;
     k_pack_canonical<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(src, in, out, dst);
+    SRT_CUDA_TRY(cudaGetLastError());
+    return SRT_OK;
+}
+
+srt_status umma_pack_layer_chunked(const float* src, int in, int out, __nv_bfloat16* dst, cudaStream_t st)
+{
+    if (in % kChunkK || out % 16 || in <= 0 || out <= 0)
+        return set_error(SRT_ERR_ARG, "layer shape not a multiple of the chunk");
+    const int64_t n = (int64_t)in * out;
+    k_pack_chunked<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(src, in, out, dst);
     SRT_CUDA_TRY(cudaGetLastError());
     return SRT_OK;
 }

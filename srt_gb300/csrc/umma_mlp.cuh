@@ -246,9 +246,204 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) k_umma_mlp(Task task, int* er
     if (!ok && tid == 0) atomicExch(err, 1);
 }
 
+// ---------------------------------------------------------------------------
+// Streaming variant for wide networks whose weights do not fit in shared
+// memory (k_umma_mlp_stream): two 128-row tiles per CTA share every weight
+// chunk (both accumulators in TMEM: 2 x 256 columns), and the weights arrive
+// as K-chunks of kChunkK columns (N x 32 BF16, 16 KB for N = 256) through a
+// ring of kStreamStages slots that a producer warp keeps filled: chunk
+// copies overlap the MMAs of earlier chunks and the epilogues, and each
+// chunk is read from L2 once per 256 rows.  Warps 0-3 own tile 0's rows,
+// warps 4-7 tile 1's; warp 8 is the producer; thread 0 issues the MMAs.
+// Barriers: full[s] (chunk landed), empty[s] (its MMAs done), x_full (the two
+// input tiles landed), a_free (the last layer's MMAs done: the A tiles may
+// be overwritten), mma (a layer's MMAs done: epilogue).
+constexpr int kChunkK = 32;
+constexpr int kStreamStages = 6;
+constexpr int kStreamConsumers = 2 * kUmmaRows;
+constexpr int kStreamThreads = kStreamConsumers + 32;
+
+template <class Task>
+struct UmmaStreamLayout {
+    using L = UmmaMlpLayout<Task>;
+    __host__ __device__ static constexpr uint32_t chunk_bytes(int l) { return (uint32_t)Task::out(l) * kChunkK * 2u; }
+    static constexpr uint32_t kChunkMax = (uint32_t)L::max_out() * kChunkK * 2u;
+    static constexpr uint32_t kATile = (uint32_t)kUmmaRows * L::imax(L::max_in(), L::max_out()) * 2u;
+    static constexpr uint32_t kRingOff = 2u * kATile;
+    static constexpr uint32_t kBarOff = kRingOff + kStreamStages * kChunkMax;
+    static constexpr uint32_t kSmem = kBarOff + (2 * kStreamStages + 3) * 8 + 16;
+    static constexpr uint32_t kTmemCols = 2u * 256u;  // two accumulators of up to 256 columns
+};
+
+template <class Task>
+__global__ void __launch_bounds__(kStreamThreads, 1) k_umma_mlp_stream(Task task, int* err)
+{
+    using L = UmmaMlpLayout<Task>;
+    using SL = UmmaStreamLayout<Task>;
+    static_assert(Task::kInputBulk && !Task::kResident, "the streaming kernel takes bulk input tiles");
+    static_assert(L::max_out() <= 256, "one accumulator per tile holds at most 256 columns");
+    extern __shared__ __align__(1024) uint8_t umma_smem[];
+    uint8_t* ring = umma_smem + SL::kRingOff;
+    uint64_t* full = reinterpret_cast<uint64_t*>(umma_smem + SL::kBarOff);
+    uint64_t* empty = full + kStreamStages;
+    uint64_t* x_full = empty + kStreamStages;
+    uint64_t* a_free = x_full + 1;
+    uint64_t* bar_mma = a_free + 1;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar_mma + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int64_t n = task.rows();
+    const int64_t tiles = (n + kUmmaRows - 1) / kUmmaRows;
+    const int64_t pairs = (tiles + 1) / 2;
+    if ((int64_t)blockIdx.x >= pairs) return;  // uniform over the CTA, before any TMEM or barrier use
+
+    if (warp == 0) tmem_alloc(tslot, SL::kTmemCols);
+    if (tid == 0) {
+        for (int s = 0; s < kStreamStages; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(x_full, 1);
+        mbar_init(a_free, 1);
+        mbar_init(bar_mma, 1);
+        mbar_fence_init();
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    const uint32_t tmem = *tslot;
+    constexpr uint32_t kInBytes = (uint32_t)kUmmaRows * Task::in(0) * 2u;
+    bool ok = true;
+
+    if (warp == kStreamConsumers / 32) {
+        // ---- producer: the input tiles and the weight chunks, in the order
+        // the MMAs consume them -------------------------------------------
+        if ((tid & 31) == 0) {
+            uint32_t it = 0, ph_af = 0;
+            for (int64_t pair = blockIdx.x; pair < pairs && ok; pair += gridDim.x) {
+                if (pair != (int64_t)blockIdx.x) {  // the A tiles are free once the last layer's MMAs are done
+                    ok = mbar_wait(a_free, ph_af);
+                    ph_af ^= 1u;
+                    if (!ok) break;
+                }
+                const int64_t t0 = 2 * pair, t1 = t0 + 1;
+                mbar_arrive_expect_tx(x_full, kInBytes * (t1 < tiles ? 2u : 1u));
+                bulk_g2s(umma_smem, task.input_tile(t0), kInBytes, x_full);
+                if (t1 < tiles) bulk_g2s(umma_smem + SL::kATile, task.input_tile(t1), kInBytes, x_full);
+                for (int l = 0; l < Task::kLayers && ok; ++l) {
+                    const uint32_t cb = SL::chunk_bytes(l);
+                    for (int c = 0; c < Task::in(l) / kChunkK; ++c, ++it) {
+                        const uint32_t s = it % kStreamStages, k = it / kStreamStages;
+                        if (k > 0 && !(ok = mbar_wait(empty + s, (k - 1u) & 1u))) break;
+                        mbar_arrive_expect_tx(full + s, cb);
+                        bulk_g2s(ring + s * SL::kChunkMax, task.weights() + Task::w_off(l) + (size_t)c * cb, cb,
+                                 full + s);
+                    }
+                }
+            }
+        }
+    } else {
+        // ---- consumers: thread = row of tile (warp / 4); thread 0 issues ----
+        const int t = warp >> 2, r = tid & (kUmmaRows - 1);
+        uint8_t* a_tile = umma_smem + t * SL::kATile;
+        const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)t * 256u;
+        uint32_t it = 0, ph_x = 0, ph_m = 0;
+        for (int64_t pair = blockIdx.x; pair < pairs && ok; pair += gridDim.x) {
+            const int64_t row = (2 * pair + t) * kUmmaRows + r;
+            const bool valid = row < n;
+            for (int l = 0; l < Task::kLayers; ++l) {
+                const int K = Task::in(l), N = Task::out(l);
+                bool w_ok = true;
+                if (l == 0) {
+                    w_ok = mbar_wait(x_full, ph_x);
+                    if (w_ok) ph_x ^= 1u;
+                }
+                fence_async_smem();  // this thread's epilogue writes to its A tile -> async proxy
+                ok = named_bar_and(1, kStreamConsumers, w_ok);
+                if (!ok) break;
+                bool issue_ok = true;
+                if (tid == 0) {
+                    tc_fence_after_sync();
+                    const uint32_t a0 = smem_u32(umma_smem), a1 = smem_u32(umma_smem + SL::kATile);
+                    const uint32_t sbo = (uint32_t)K * 16u;
+                    const uint32_t idesc = umma_idesc_bf16(kUmmaRows, N);
+                    for (int c = 0; c < K / kChunkK; ++c, ++it) {
+                        const uint32_t s = it % kStreamStages, k = it / kStreamStages;
+                        if (!mbar_wait(full + s, k & 1u)) {
+                            issue_ok = false;
+                            break;
+                        }
+                        tc_fence_after_sync();
+                        const uint32_t b0 = smem_u32(ring + s * SL::kChunkMax);
+#pragma unroll
+                        for (int j = 0; j < kChunkK / 16; ++j) {
+                            const uint32_t kk = (uint32_t)(c * (kChunkK / 16) + j);
+                            const uint64_t bd = umma_desc(b0 + 256u * j, 128u, kChunkK * 16u);
+                            umma_bf16(tmem, umma_desc(a0 + 256u * kk, 128u, sbo), bd, idesc, kk > 0 ? 1u : 0u);
+                            umma_bf16(tmem + 256u, umma_desc(a1 + 256u * kk, 128u, sbo), bd, idesc, kk > 0 ? 1u : 0u);
+                        }
+                        umma_commit(empty + s);  // the slot is free once these MMAs are done
+                    }
+                    umma_commit(bar_mma);
+                    if (l + 1 == Task::kLayers) umma_commit(a_free);
+                }
+                bool m_ok = mbar_wait(bar_mma, ph_m);
+                if (m_ok) ph_m ^= 1u;
+                ok = named_bar_and(1, kStreamConsumers, m_ok && issue_ok);
+                if (!ok) break;
+                tc_fence_after_sync();
+                if (l + 1 < Task::kLayers) {
+                    const bool relu = Task::relu(l);
+#pragma unroll 1
+                    for (int c0 = 0; c0 < N; c0 += 32) {
+                        uint32_t v[32];
+                        tmem_ld32(trow + (uint32_t)c0, v);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 32; j += 8) {
+                            float f[8];
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) {
+                                f[e] = __uint_as_float(v[j + e]);
+                                if (relu) f[e] = fmaxf(f[e], 0.0f);
+                            }
+                            uint4 q;
+                            q.x = pack2_bf16(f[0], f[1]);
+                            q.y = pack2_bf16(f[2], f[3]);
+                            q.z = pack2_bf16(f[4], f[5]);
+                            q.w = pack2_bf16(f[6], f[7]);
+                            *reinterpret_cast<uint4*>(a_tile + canon_off(r, c0 + j, N)) = q;
+                        }
+                    }
+                } else {
+                    constexpr int kOut = Task::out(Task::kLayers - 1);
+                    float o[kOut];
+#pragma unroll
+                    for (int c0 = 0; c0 < kOut; c0 += 16) {
+                        uint32_t v[16];
+                        tmem_ld16(trow + (uint32_t)c0, v);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) o[c0 + e] = __uint_as_float(v[e]);
+                    }
+                    if (valid) task.store(row, o);
+                }
+                tc_fence_before_sync();
+            }
+        }
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    if (warp == 0) tmem_dealloc(tmem, SL::kTmemCols);
+    if (!ok) atomicExch(err, 1);
+}
+
 // Packs one layer's FP32 weights W[out][in] (row-major) into the BF16
 // canonical K-major layout at dst (out x in elements).
 srt_status umma_pack_layer(const float* src, int in, int out, __nv_bfloat16* dst, cudaStream_t st);
+// The same, as in / kChunkK consecutive K-chunks (out x kChunkK each, in the
+// canonical layout with K = kChunkK): the streaming kernel's weight order.
+srt_status umma_pack_layer_chunked(const float* src, int in, int out, __nv_bfloat16* dst, cudaStream_t st);
 
 // Sets up the fused-MLP kernels on the current device (shared-memory limits,
 // the device address of the timeout flag); call before any stream capture
@@ -269,6 +464,10 @@ srt_status umma_mlp_launch(const Task& task, int64_t max_rows, unsigned grid_y, 
     using L = UmmaMlpLayout<Task>;
     static const int resident = [] {
         cudaFuncSetAttribute(k_umma_mlp<Task>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kSmem);
+        // the whole unified L1 / shared array as shared memory, so that several
+        // CTAs fit on an SM (the default carveout leaves room for one)
+        cudaFuncSetAttribute(k_umma_mlp<Task>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
         int nb = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_umma_mlp<Task>, kUmmaThreads, L::kSmem) !=
                 cudaSuccess ||
@@ -282,6 +481,25 @@ srt_status umma_mlp_launch(const Task& task, int64_t max_rows, unsigned grid_y, 
     const int64_t tiles = (max_rows + kUmmaRows - 1) / kUmmaRows;
     const int64_t gx = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)device_sm_count() * resident));
     k_umma_mlp<Task><<<dim3((unsigned)gx, grid_y), kUmmaThreads, L::kSmem, st>>>(task, err);
+    SRT_CUDA_TRY(cudaGetLastError());
+    return SRT_OK;
+}
+
+// Launches k_umma_mlp_stream<Task> over n rows: one CTA per SM at most, each
+// taking pairs of 128-row tiles.
+template <class Task>
+srt_status umma_mlp_stream_launch(const Task& task, int64_t n, cudaStream_t st)
+{
+    using SL = UmmaStreamLayout<Task>;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_umma_mlp_stream<Task>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::kSmem);
+    SRT_CUDA_TRY(attr);
+    int* err = umma_error_word();
+    if (!err) return set_error(SRT_ERR_CUDA, "fused MLP kernels not prepared on this device (umma_prepare)");
+    if (n <= 0) return SRT_OK;
+    const int64_t pairs = ((n + kUmmaRows - 1) / kUmmaRows + 1) / 2;
+    const int64_t gx = std::max<int64_t>(1, std::min<int64_t>(pairs, (int64_t)device_sm_count()));
+    k_umma_mlp_stream<Task><<<(unsigned)gx, kStreamThreads, SL::kSmem, st>>>(task, err);
     SRT_CUDA_TRY(cudaGetLastError());
     return SRT_OK;
 }
