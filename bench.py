@@ -502,11 +502,11 @@ def cache_bound(S, scene, ref, w, h, frames=128):
     refd = torch.from_numpy(ref[:, :3]).cuda().double()
     den = (refd + 1e-6) ** 2
 
-    def rel_per_sample(depth):
+    def rel_per_sample(depth, flags=0):
         s1 = torch.zeros((w * h, 3), dtype=torch.float64, device="cuda")
         s2 = torch.zeros_like(s1)
         for f in range(frames):
-            pt.render(film, S.pt_params(1, depth, RR_DEPTH, 1, 1, 30000 + f))
+            pt.render(film, S.pt_params(1, depth, RR_DEPTH, 1, 1, 30000 + f, flags=flags))
             x = film[:, :3].double()
             s1 += x
             s2 += x * x
@@ -515,29 +515,34 @@ def cache_bound(S, scene, ref, w, h, frames=128):
         keep = int(e.numel() * 0.999)
         return float(torch.sort(e).values[:keep].mean())
 
-    def per_sample_ms(depth):
-        pt.render(film, S.pt_params(64, depth, RR_DEPTH, 1, 1, 777))
+    def per_sample_ms(depth, flags=0):
+        pt.render(film, S.pt_params(64, depth, RR_DEPTH, 1, 1, 777, flags=flags))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for i in range(3):
-            pt.render(film, S.pt_params(64, depth, RR_DEPTH, 1, 1, 778 + i))
+            pt.render(film, S.pt_params(64, depth, RR_DEPTH, 1, 1, 778 + i, flags=flags))
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) / 3 / 64 * 1e3
 
-    e_full, e1, e2 = rel_per_sample(MAX_DEPTH), rel_per_sample(1), rel_per_sample(2)
-    t_full, t1, t2 = per_sample_ms(MAX_DEPTH), per_sample_ms(1), per_sample_ms(2)
-    r1, r2 = e1 / e_full, e2 / e_full
+    nee1 = S._capi.PT_NEE_FIRST_VERTEX_ONLY
+    e_full, e1, e2, ep = (rel_per_sample(MAX_DEPTH), rel_per_sample(1), rel_per_sample(2),
+                          rel_per_sample(2, nee1))
+    t_full, t1, t2, tp = per_sample_ms(MAX_DEPTH), per_sample_ms(1), per_sample_ms(2), per_sample_ms(2, nee1)
+    r1, r2, rp = e1 / e_full, e2 / e_full, ep / e_full
     pt.close()
-    # the prefix a second-vertex cache keeps lies between depth 1 (no emission
-    # at the second vertex) and depth 2 (also its next-event estimate, which
-    # the cache replaces); its cost lies between theirs as well
+    # the prefix a second-vertex cache keeps: depth 2 with next-event
+    # estimation at the first vertex only (the cache replaces the second
+    # vertex's light sample and everything after it, but a ray that reaches
+    # a light at the second vertex adds its MIS-weighted emission); depth 1
+    # and depth 2 with both light samples bracket it
     return {"frames_for_variance": frames, "relmse_per_sample_plain": e_full,
-            "relmse_per_sample_depth1": e1, "relmse_per_sample_depth2": e2,
-            "variance_ratio_depth1": round(r1, 4), "variance_ratio_depth2": round(r2, 4),
-            "samples_a_perfect_cache_needs": [round(64 * r1, 1), round(64 * r2, 1)],
-            "ms_per_sample_plain_depth16": round(t_full, 4), "ms_per_sample_depth1": round(t1, 4),
-            "ms_per_sample_depth2": round(t2, 4),
-            "max_speedup_any_second_vertex_cache": [round((t_full / t2) / r2, 3), round((t_full / t1) / r1, 3)]}
+            "relmse_per_sample_prefix": ep, "relmse_per_sample_depth1": e1, "relmse_per_sample_depth2": e2,
+            "variance_ratio_prefix": round(rp, 4), "variance_ratio_depth1": round(r1, 4),
+            "variance_ratio_depth2": round(r2, 4),
+            "samples_a_perfect_cache_needs": round(64 * rp, 1),
+            "ms_per_sample_plain_depth16": round(t_full, 4), "ms_per_sample_prefix": round(tp, 4),
+            "ms_per_sample_depth1": round(t1, 4), "ms_per_sample_depth2": round(t2, 4),
+            "max_speedup_any_second_vertex_cache": round((t_full / tp) / rp, 3)}
 
 
 def cache_eval(S, arrays, scene, frames=256, w=1280, h=720, ref_frames=64, ref_spp=64):
@@ -622,7 +627,7 @@ def serving_eval(S, rates=(5.0, 20.0, 50.0), duration=30.0):
     scenes = SB.build_scenes(S, n_variants=1, cache_frames=30)
     table = [SB.run_rate(S, scenes, r, duration) for r in rates]
     return {"mix": "res {256^2,512^2,1024^2,1920x1080} x spp {1,4,16,64} x {cornell, 5.2M spheres} x "
-                   "{plain, cached (network trained beforehand, frozen)}",
+                   "{plain, cached (network trained beforehand; half of the cached jobs train it online, half frozen)}",
             "budget_gb": 150, "duration_s": duration, "rates": table}
 
 

@@ -222,7 +222,14 @@ enum {
     /* Light / triangle CDF remap done correctly ((u - cdf[i-1]) / pdf_i).
      * Default (0) reproduces the reference's `int lower = cdf[idx-1]`
      * truncation (light.h:65, gmesh.h:49). */
-    SRT_PT_FIXED_CDF_REMAP = 1
+    SRT_PT_FIXED_CDF_REMAP = 1,
+    /* Next-event estimation at the first surface vertex only (no shadow rays
+     * from later vertices; a later vertex's emission keeps the MIS weight of
+     * the previous vertex's light sample).  With max_depth 2 this is the path
+     * prefix that a cache ending paths at the second vertex keeps: the
+     * benchmark measures its variance to bound what such a cache can gain.
+     * No counterpart in the reference. */
+    SRT_PT_NEE_FIRST_VERTEX_ONLY = 2
 };
 
 /* PathTracer JSON params + frame seed (path_tracer.h:15-19, 30-39;
@@ -510,7 +517,12 @@ typedef struct srt_job_desc {
     int32_t width, height;
     srt_pt_params params;         /* same meaning as for srt_pt_render                      */
     float* film;                  /* caller's device float4[w*h], or NULL: server-owned     */
-    struct srt_mlp* cache;        /* trained radiance cache of this scene (frozen), or NULL */
+    struct srt_mlp* cache;        /* radiance cache of this scene, or NULL                  */
+    int32_t cache_train;          /* 1: train `cache` online on this job's own paths (one
+                                     pixel in 1 + npix / 16384 traces full paths for its
+                                     first sample; the network takes Adam steps when the
+                                     job's first progressive frame completes); 0: frozen */
+    int32_t pad;
 } srt_job_desc;
 
 enum { SRT_JOB_QUEUED = 0, SRT_JOB_RUNNING = 1, SRT_JOB_DONE = 2, SRT_JOB_FAILED = 3 };

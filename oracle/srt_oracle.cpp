@@ -1099,7 +1099,7 @@ void render_pixel(const oracle_scene& s, int w, int h, int ix, int iy, const srt
             }
             float cos_i = dot(hi.normal, -rd);
             if (cos_i < 0.0f) hi.normal = -hi.normal;
-            if (p.use_nee && !is_specular(mat.bxdf)) {
+            if (p.use_nee && !is_specular(mat.bxdf) && !(depth > 0 && (p.flags & SRT_PT_NEE_FIRST_VERTEX_ONLY))) {
                 float lu = rng.next();
                 float lv = rng.next();
                 LSample ls = light_sample(s, lu, lv, fixed);

@@ -415,9 +415,11 @@ class Server:
         self.handle = C.c_void_p()
         check(lib().srt_server_create(C.byref(cfg), C.byref(self.handle)))
 
-    def submit(self, scene: Scene, width, height, params, film=None, cache=None):
+    def submit(self, scene: Scene, width, height, params, film=None, cache=None, cache_train=False):
+        """cache: an srt_mlp handle (radiance cache of the scene) or None;
+        cache_train: the network trains online on this job's own paths."""
         d = _capi.JobDesc(scene.handle, width, height, params, None if film is None else film.data_ptr(),
-                          cache)
+                          cache, int(bool(cache_train)), 0)
         jid = C.c_int64()
         check(lib().srt_server_submit(self.handle, C.byref(d), C.byref(jid)))
         return jid.value

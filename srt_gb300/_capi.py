@@ -23,6 +23,7 @@ CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC = 0, 1
 CAMERA_MIRROR_X = 0x100  # flag OR'd into CameraDesc.type (left-handed pbrt camera frame)
 RNG_CURAND, RNG_HASH = 0, 1
 PT_FIXED_CDF_REMAP = 1
+PT_NEE_FIRST_VERTEX_ONLY = 2
 LAUNCH_GRAPH, LAUNCH_DIRECT = 0, 1
 TONE_NONE, TONE_CLAMP, TONE_REINHARD, TONE_UNCHARTED2, TONE_ACES = 0, 1, 2, 3, 4
 METRIC_MSE, METRIC_MAPE, METRIC_SMAPE, METRIC_RELMSE = 0, 1, 2, 3
@@ -102,7 +103,7 @@ class ServerConfig(C.Structure):
 
 class JobDesc(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("params", PtParams),
-                ("film", C.c_void_p), ("cache", C.c_void_p)]
+                ("film", C.c_void_p), ("cache", C.c_void_p), ("cache_train", C.c_int32), ("pad", C.c_int32)]
 
 
 class JobInfo(C.Structure):

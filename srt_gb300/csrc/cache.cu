@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "cache.cuh"
 #include "common.h"
 #include "mlp.cuh"
 #include "scene.h"
@@ -189,6 +190,48 @@ __global__ void k_region_update(CacheBuffers b, int cells, float threshold, floa
 }
 
 }  // namespace
+
+namespace srt {
+
+size_t cache_job_bytes(int64_t npix, int64_t n_train) { return carve_bytes(npix, n_train, 1); }
+
+void cache_job_carve(char* base, int64_t npix, int64_t n_train, CacheRec& C)
+{
+    CacheBuffers b = carve(base, npix, n_train, 1);
+    C.q_rec = b.q_rec;
+    C.q_beta = b.q_beta;
+    C.q_count = b.q_count;
+    C.t_rec = b.t_rec;
+    C.t_aux = b.t_aux;
+    C.t_len = b.t_len;
+    C.n_train = (int32_t)n_train;
+}
+
+srt_status cache_job_train(char* base, int64_t npix, int64_t n_train, srt_mlp* mlp, int steps, float lr,
+                           cudaStream_t st, int64_t* vertices)
+{
+    CacheBuffers b = carve(base, npix, n_train, 1);
+    const int gblocks = (int)((n_train * kTrainVertices + kGatherThreads - 1) / kGatherThreads);
+    k_gather_count<<<gblocks, kGatherThreads, 0, st>>>(b, (int)n_train);
+    k_gather_scatter<<<gblocks, kGatherThreads, 0, st>>>(b, (int)n_train, b.q_count + 2);
+    SRT_CUDA_TRY(cudaGetLastError());
+    int32_t nb32 = 0;
+    SRT_CUDA_TRY(cudaMemcpyAsync(&nb32, b.q_count + 2, 4, cudaMemcpyDeviceToHost, st));
+    SRT_CUDA_TRY(cudaStreamSynchronize(st));
+    const int64_t nb = nb32;
+    steps = std::max(1, std::min(steps, kMaxTrainSteps));
+    const int64_t slice = (nb + steps - 1) / steps;
+    for (int s = 0; s < steps && nb > 0; ++s) {
+        const int64_t b0 = s * slice, n = std::min(slice, nb - b0);
+        if (n <= 0) break;
+        SRT_TRY(mlp_train_launch(mlp, b.b_rec + 4 * b0, b.b_tgt + b0, n, lr, true, st));
+    }
+    SRT_CUDA_TRY(cudaMemsetAsync(b.q_count + 2, 0, 4, st));
+    if (vertices) *vertices = nb;
+    return SRT_OK;
+}
+
+}  // namespace srt
 
 extern "C" srt_status srt_pt_render_cached(srt_pt* p, float* film, const srt_pt_params* prm, srt_mlp* mlp,
                                            const srt_cache_params* cp, srt_cache_stats* stats, void* stream)

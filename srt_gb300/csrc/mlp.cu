@@ -1,9 +1,10 @@
 // mlp.cu — fused BF16 tensor-core kernels of the radiance-cache network
 // (see mlp.cuh): inference (tcgen05.mma with TMEM accumulators, the fused
 // kernel of umma_mlp.cuh: standalone and the tracer's cache queries),
-// forward+backward-data for training, weight gradients (mma.sync), Adam.  The reference's learned part (tiny-cuda-nn HashGrid +
-// CutlassMLP, src/passes/npr/neural_radiosity.cu:6-52) is an un-vendored
-// library; the network here is a plain fully fused MLP.
+// forward+backward-data for training, weight gradients (mma.sync), Adam.
+// The reference's learned part (tiny-cuda-nn HashGrid + CutlassMLP,
+// src/passes/npr/neural_radiosity.cu:6-52) is an un-vendored library; the
+// network here is a plain fully fused MLP.
 //
 // Fragment layout (mma.sync m16n8k16, bf16 inputs, f32 accumulators), lane
 // = 4*g + t: A regs {0,1,2,3} hold (row g, cols 2t..2t+1), (row g+8, same),

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "cache.cuh"
 #include "common.h"
 #include "mlp.cuh"
 #include "scene.h"
@@ -36,18 +37,30 @@ struct Job {
     double submit_s = 0, admit_s = -1, first_frame_s = -1, done_s = -1;
     std::vector<double> frame_times;
     size_t frames_off = 0;  // byte offset of the frame counters in state_buf
+    bool trained = false;   // online training done (cache_train jobs)
 };
+
+// online training: training pixels per job (one pixel in `stride`)
+constexpr int64_t kServeTrainPaths = 16384;
+constexpr int kServeTrainSteps = 4;
+constexpr float kServeTrainLr = 1e-2f;
+int64_t train_stride(int64_t npix) { return 1 + npix / kServeTrainPaths; }
+int64_t train_pixels(int64_t npix) { return (npix + train_stride(npix) - 1) / train_stride(npix); }
 
 size_t frames_bytes(int spp) { return ((size_t)std::max(spp, 1) * 4 + 255) & ~(size_t)255; }
 
-size_t state_bytes(int64_t npix, int spp, bool cache)
+size_t state_bytes(int64_t npix, int spp, bool cache, bool train)
 {
     // lpath 16 per pixel (rounded), frame counters, and for a cached job its
-    // query records (64 B), throughputs (16 B) and counters
+    // query records (64 B), throughputs (16 B) and counters, or, when it
+    // trains online, the cache module's query and training buffers
     size_t b = (((size_t)npix * 16 + 255) & ~(size_t)255) + frames_bytes(spp);
-    if (cache) b += (size_t)npix * 80 + 256;
+    if (cache && train) b += cache_job_bytes(npix, train_pixels(npix));
+    else if (cache) b += (size_t)npix * 80 + 256;
     return b;
 }
+
+bool trains(const srt_job_desc& d) { return d.cache != nullptr && d.cache_train != 0; }
 
 }  // namespace
 
@@ -83,7 +96,7 @@ struct srt_server {
     {
         const int spp = j.desc.params.samples_per_pixel;
         const bool cached = j.desc.cache != nullptr;
-        size_t sb = state_bytes(j.npix, spp, cached);
+        size_t sb = state_bytes(j.npix, spp, cached, trains(j.desc));
         cudaError_t e = cudaMallocAsync(&j.state_buf, sb, stream);
         if (e != cudaSuccess) return cuda_error(e, "job state allocation");
         if (!j.desc.film) {
@@ -124,20 +137,29 @@ struct srt_server {
         J.flags = j.desc.params.flags;
         J.rng_mode = j.desc.params.rng_mode;
         if (cached) {
-            // frozen network: every pixel ends at its second vertex with a query
+            // every pixel that is not a training pixel ends at its second
+            // vertex with a query (no per-cell fallback while serving)
             char* cb = b + px_bytes + frames_bytes(spp);
             CacheRec& C = J.cache;
             C.w = j.desc.cache->wb;
             C.wpack = j.desc.cache->wpack;
             C.box = j.desc.cache->box;
-            C.q_rec = reinterpret_cast<float4*>(cb);
-            C.q_beta = reinterpret_cast<float4*>(cb + n * 64);
-            C.q_count = reinterpret_cast<int32_t*>(cb + n * 80);
-            SRT_CUDA_TRY(cudaMemsetAsync(C.q_count, 0, 64, stream));
             C.region_off = nullptr;
             C.region_res = 1;
-            C.train_stride = j.npix + 1;  // no training pixels
-            C.train_phase = -1;
+            if (trains(j.desc)) {
+                // online: one pixel in `stride` traces full paths and records
+                // its first sample's vertices for the network's next steps
+                cache_job_carve(cb, j.npix, train_pixels(j.npix), C);
+                C.train_stride = (int32_t)train_stride(j.npix);
+                C.train_phase = 0;
+            } else {
+                C.q_rec = reinterpret_cast<float4*>(cb);
+                C.q_beta = reinterpret_cast<float4*>(cb + n * 64);
+                C.q_count = reinterpret_cast<int32_t*>(cb + n * 80);
+                C.train_stride = j.npix + 1;  // no training pixels
+                C.train_phase = -1;
+            }
+            SRT_CUDA_TRY(cudaMemsetAsync(C.q_count, 0, 64, stream));
             engine.enable_cache();
         }
         SRT_TRY(engine.set_job(slot, J, stream));
@@ -164,7 +186,8 @@ struct srt_server {
         j.state_buf = nullptr;
         slots[j.slot] = 0;
         paths_used -= j.npix;
-        bytes_used -= (int64_t)state_bytes(j.npix, j.desc.params.samples_per_pixel, j.desc.cache != nullptr);
+        bytes_used -= (int64_t)state_bytes(j.npix, j.desc.params.samples_per_pixel, j.desc.cache != nullptr,
+                                           trains(j.desc));
         if (--scene_refs[j.desc.scene] == 0) {
             scene_refs.erase(j.desc.scene);
             bytes_used -= scene_bytes(j.desc.scene);
@@ -209,7 +232,7 @@ extern "C" srt_status srt_server_submit(srt_server* s, const srt_job_desc* d, in
     j->id = s->next_id++;
     j->desc = *d;
     j->npix = d->width * d->height;
-    j->bytes = (int64_t)state_bytes(j->npix, p.samples_per_pixel, d->cache != nullptr) +
+    j->bytes = (int64_t)state_bytes(j->npix, p.samples_per_pixel, d->cache != nullptr, trains(*d)) +
                (d->film ? 0 : (int64_t)j->npix * 16);
     if (d->cache && p.max_depth < 2) return set_error(SRT_ERR_ARG, "cached jobs need max_depth >= 2");
     j->submit_s = s->now();
@@ -289,6 +312,14 @@ extern "C" srt_status srt_server_step(srt_server* s, int32_t* running, int32_t* 
                 j.frame_times.push_back(t);
             }
             off += (size_t)spp;
+            if (trains(j.desc) && !j.trained && !j.frame_times.empty()) {
+                // every training pixel has finished the sample that recorded its vertices
+                char* cb = reinterpret_cast<char*>(j.state_buf) + j.frames_off + frames_bytes(spp);
+                int64_t nv = 0;
+                SRT_TRY(cache_job_train(cb, j.npix, train_pixels(j.npix), j.desc.cache, kServeTrainSteps,
+                                        kServeTrainLr, s->stream, &nv));
+                j.trained = true;
+            }
             if (s->h_pixels_done[k] >= j.npix) SRT_TRY(s->retire(j, t));
         }
     }

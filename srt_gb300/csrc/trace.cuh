@@ -130,59 +130,6 @@ __device__ __forceinline__ uint32_t word4(uint4 v, int j)
     return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
 }
 
-// L2 eviction priority of the traversal's loads (per instruction, through a
-// cache policy: no setting of the device changes).  Nodes (128 B, about a
-// quarter of the scene's bytes) are loaded evict-last so that they stay in
-// L2, triangles evict-first so that they do not push the nodes out.
-#ifndef SRT_NODE_EVICT_LAST
-#define SRT_NODE_EVICT_LAST 0
-#endif
-__device__ __forceinline__ uint64_t l2_policy_evict_last()
-{
-    uint64_t p;
-    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_evict_first()
-{
-    uint64_t p;
-    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
-__device__ __forceinline__ uint4 ldg_hint(const uint4* p, uint64_t pol)
-{
-    uint4 v;
-    asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
-        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-        : "l"(p), "l"(pol));
-    return v;
-}
-__device__ __forceinline__ float4 ldg_hint(const float4* p, uint64_t pol)
-{
-    float4 v;
-    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-        : "l"(p), "l"(pol));
-    return v;
-}
-// node and triangle loads of the traversal
-__device__ __forceinline__ uint4 ld_node(const uint4* p)
-{
-#if SRT_NODE_EVICT_LAST
-    return ldg_hint(p, l2_policy_evict_last());
-#else
-    return __ldg(p);
-#endif
-}
-__device__ __forceinline__ float4 ld_tri(const float4* p)
-{
-#if SRT_NODE_EVICT_LAST
-    return ldg_hint(p, l2_policy_evict_first());
-#else
-    return __ldg(p);
-#endif
-}
-
 // three-input minimum / maximum (one instruction on sm_100 and later; NaN
 // inputs are ignored as by fminf / fmaxf)
 __device__ __forceinline__ float fmax3(float a, float b, float c)
@@ -227,8 +174,8 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
                                            uint32_t& tri_base)
 {
     const uint4* np = reinterpret_cast<const uint4*>(nodes + ni);
-    uint4 w0 = ld_node(np + 0);
-    uint4 w1 = ld_node(np + 1);
+    uint4 w0 = __ldg(np + 0);
+    uint4 w1 = __ldg(np + 1);
     // low planes at lines 2..4, high planes at 5..7.  Along an axis where the
     // ray's idir is negative the high plane is the near one: loading the
     // planes in near/far order replaces the per-child min/max of the two slab
@@ -276,9 +223,9 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
         // (meta >> 5) << (meta & 31); an empty slot's byte is 0
         if (tn <= tf * 1.00000024f) hitmask |= __funnelshift_l(0u, meta >> 5, meta);
     };
-    const uint4 nqx = ld_node(np + 2 + 3 * ox), fqx = ld_node(np + 5 - 3 * ox);
-    const uint4 nqy = ld_node(np + 3 + 3 * oy), fqy = ld_node(np + 6 - 3 * oy);
-    const uint4 nqz = ld_node(np + 4 + 3 * oz), fqz = ld_node(np + 7 - 3 * oz);
+    const uint4 nqx = __ldg(np + 2 + 3 * ox), fqx = __ldg(np + 5 - 3 * ox);
+    const uint4 nqy = __ldg(np + 3 + 3 * oy), fqy = __ldg(np + 6 - 3 * oy);
+    const uint4 nqz = __ldg(np + 4 + 3 * oz), fqz = __ldg(np + 7 - 3 * oz);
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int j = s >> 1;
@@ -337,7 +284,7 @@ __device__ __forceinline__ Hit trace_closest(const SceneView& S, float3 o, float
             tmask &= tmask - 1;
             uint32_t ti = tri_base + b;
             const float4* tp = S.tris + 3 * (size_t)ti;
-            float4 a = ld_tri(tp), bb = ld_tri(tp + 1), c = ld_tri(tp + 2);
+            float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
             float t, u, v;
             if (hit_triangle(r, f3(a), f3(bb), f3(c), tmin, h.t, t, u, v)) {
                 h.t = t;
@@ -408,7 +355,7 @@ __device__ __forceinline__ float2 tri_barycentrics(const RayPre& r, const float4
     float u = 0.0f, v = 0.0f;
     if (tri >= 0) {
         const float4* tp = tris + 3 * (size_t)tri;
-        float4 a = ld_tri(tp), bb = ld_tri(tp + 1), c = ld_tri(tp + 2);
+        float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
         float t;
         if (!hit_triangle(r, f3(a), f3(bb), f3(c), tmin, __int_as_float(0x7f800000), t, u, v)) u = v = 0.0f;
     }
@@ -430,7 +377,7 @@ __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overf
             s.tmask &= s.tmask - 1;
             uint32_t ti = s.tri_base + b;
             const float4* tp = s.tris + 3 * (size_t)ti;
-            float4 a = ld_tri(tp), bb = ld_tri(tp + 1), c = ld_tri(tp + 2);
+            float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
             float t, u, v;
             if (hit_triangle(s.r, f3(a), f3(bb), f3(c), s.tmin, s.tmax, t, u, v)) {
                 s.tri = (int32_t)ti;
@@ -515,7 +462,7 @@ __device__ __forceinline__ bool trace_any(const SceneView& S, float3 o, float3 d
             uint32_t b = __ffs(tmask) - 1;
             tmask &= tmask - 1;
             const float4* tp = S.tris + 3 * (size_t)(tri_base + b);
-            float4 a = ld_tri(tp), bb = ld_tri(tp + 1), c = ld_tri(tp + 2);
+            float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
             float t, u, v;
             if (hit_triangle(r, f3(a), f3(bb), f3(c), tmin, tmax, t, u, v)) return true;
         }

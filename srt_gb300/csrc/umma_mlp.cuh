@@ -468,12 +468,16 @@ srt_status umma_mlp_launch(const Task& task, int64_t max_rows, unsigned grid_y, 
         // CTAs fit on an SM (the default carveout leaves room for one)
         cudaFuncSetAttribute(k_umma_mlp<Task>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
-        int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_umma_mlp<Task>, kUmmaThreads, L::kSmem) !=
-                cudaSuccess ||
-            nb < 1)
-            nb = 1;
-        return nb;
+        // resident CTAs per SM from the limits that bind here: shared memory
+        // (with the 1 KB the driver reserves per CTA), the 512 TMEM columns,
+        // threads
+        int dev = 0, smem_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        int nb = smem_sm / (int)(L::kSmem + 1024u);
+        nb = std::min(nb, (int)(512u / L::tmem_cols()));
+        nb = std::min(nb, 2048 / kUmmaThreads);
+        return std::max(nb, 1);
     }();
     int* err = umma_error_word();
     if (!err) return set_error(SRT_ERR_CUDA, "fused MLP kernels not prepared on this device (umma_prepare)");

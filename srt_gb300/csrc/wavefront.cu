@@ -341,7 +341,8 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                     Frame fr = Frame::from_normal_tangent(sn, tan);
                     const bool transmissive = (mflags & kMatTransmissive) != 0;
                     // NEE with MIS (path_tracer.cu:113-142)
-                    if (J.use_nee && !(mflags & kMatSpecular)) {
+                    if (J.use_nee && !(mflags & kMatSpecular) &&
+                        !(depth > 0 && (J.flags & SRT_PT_NEE_FIRST_VERTEX_ONLY))) {
                         float lu = rng.next();
                         float lv = rng.next();
                         LightSample ls = sample_light(S, lu, lv, (J.flags & SRT_PT_FIXED_CDF_REMAP) != 0);

@@ -4,7 +4,8 @@ Each job draws its resolution from {256^2, 512^2, 1024^2, 1920x1080}, its
 spp from {1, 4, 16, 64}, its scene from {Cornell box, 5.2M-triangle spheres
 scene} (several seeds of each, built once and kept resident) and plain or
 radiance-cache rendering 50/50 (the cache network of each scene is trained
-beforehand with srt_pt_render_cached and frozen while serving).  Jobs are
+beforehand with srt_pt_render_cached; half of the cached jobs keep training
+it online on their own paths, the other half use it frozen).  Jobs are
 admitted under the HBM budget as slots and queue capacity free up, and
 their rays share the wavefront queues.
 
@@ -69,17 +70,18 @@ def run_rate(S, scenes, rate, duration, seed=0, budget_gb=150, max_paths=1 << 24
         spp = SPPS[rng.integers(len(SPPS))]
         sc = scenes[rng.integers(len(scenes))]
         cached = bool(rng.integers(2))
-        arrivals.append((t, w, h, spp, sc, cached))
+        online = cached and bool(rng.integers(2))
+        arrivals.append((t, w, h, spp, sc, cached, online))
     jobs = []
     t0 = srv.now()
     i = 0
     while True:
         now = srv.now() - t0
         while i < len(arrivals) and arrivals[i][0] <= now:
-            _, w, h, spp, sc, cached = arrivals[i]
+            _, w, h, spp, sc, cached, online = arrivals[i]
             p = S.pt_params(spp, sc["depth"], sc["rr"], 1, 1, 1000 + i)
-            jid = srv.submit(sc["scene"], w, h, p, cache=sc["mlp"] if cached else None)
-            jobs.append((jid, w * h * spp, cached))
+            jid = srv.submit(sc["scene"], w, h, p, cache=sc["mlp"] if cached else None, cache_train=online)
+            jobs.append((jid, w * h * spp, cached, online))
             i += 1
         running, queued = srv.step()
         if i >= len(arrivals) and running == 0 and queued == 0:
@@ -89,12 +91,13 @@ def run_rate(S, scenes, rate, duration, seed=0, budget_gb=150, max_paths=1 << 24
         if running == 0 and queued == 0 and i < len(arrivals):
             time.sleep(max(0.0, min(0.002, arrivals[i][0] - now)))
     wall = srv.now() - t0
-    lat, first, interval, samples, done, cached_done = [], [], [], 0, 0, 0
-    for jid, ns, cached in jobs:
+    lat, first, interval, samples, done, cached_done, online_done = [], [], [], 0, 0, 0, 0
+    for jid, ns, cached, online in jobs:
         info = srv.info(jid)
         if info["state"] == 2:
             done += 1
             cached_done += int(cached)
+            online_done += int(online)
             samples += ns
             lat.append(info["done_s"] - info["submit_s"])
             # progressive frames: latency of the first one, and the job's mean
@@ -107,7 +110,8 @@ def run_rate(S, scenes, rate, duration, seed=0, budget_gb=150, max_paths=1 << 24
     srv.close()
     pct = lambda a, q: float(np.quantile(a, q)) if len(a) else None
     return {"rate_jobs_per_s": rate, "duration_s": duration, "submitted": len(jobs), "completed": done,
-            "cached_completed": cached_done, "wall_s": round(wall, 3),
+            "cached_completed": cached_done, "cached_online_training_completed": online_done,
+            "wall_s": round(wall, 3),
             "p50_job_s": pct(lat, 0.5), "p99_job_s": pct(lat, 0.99),
             "p50_first_frame_s": pct(first, 0.5), "p99_first_frame_s": pct(first, 0.99),
             "p50_frame_interval_s": pct(interval, 0.5), "p99_frame_interval_s": pct(interval, 0.99),

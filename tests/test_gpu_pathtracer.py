@@ -41,11 +41,14 @@ def _cornell():
     dict(spp=8, max_depth=16, rr_depth=4, use_nee=1, use_mis=0, seed=7),
     dict(spp=8, max_depth=5, rr_depth=0, use_nee=0, use_mis=0, seed=2147483000),
     dict(spp=4, max_depth=1, rr_depth=4, use_nee=1, use_mis=1, seed=3),
+    # next-event estimation at the first vertex only (the prefix a second-vertex cache keeps)
+    dict(spp=8, max_depth=2, rr_depth=4, use_nee=1, use_mis=1, seed=11, flags=2),
 ])
 def test_cornell_matches_oracle_streams(cuda, cfg):
     w, h = 24, 20
     sa = _cornell()
-    p = pt_params(cfg["spp"], cfg["max_depth"], cfg["rr_depth"], cfg["use_nee"], cfg["use_mis"], cfg["seed"])
+    p = pt_params(cfg["spp"], cfg["max_depth"], cfg["rr_depth"], cfg["use_nee"], cfg["use_mis"], cfg["seed"],
+                  flags=cfg.get("flags", 0))
     film, st = _render(cuda, sa, w, h, p)
     sa.camera.aspect = w / h
     of, s1, s2, cnt = O.OracleScene(sa.desc()).render(w, h, p)

@@ -204,3 +204,45 @@ def test_cached_jobs_equal_alone_and_in_the_mix(cuda):
         assert np.all(np.isfinite(alone)) and np.all(alone[:, 3] == 1.0)
     for h in nets:
         S.lib().srt_mlp_destroy(h)
+
+
+def test_online_training_jobs_train_the_network(cuda):
+    """A cached job that trains online: one pixel in 1 + npix / 16384 traces
+    full paths for its first sample and, when the job's first progressive
+    frame completes, the network takes Adam steps on the recorded vertices.
+    The job completes with finite pixels, the network's parameters change,
+    and a frozen cached job served after it leaves them as they are; a plain
+    job in the same mix stays bit-identical to a lone render."""
+    import srt_gb300 as S
+    cornell, _ = _scenes(S)
+    cornell.set_aspect(1.0)
+    scene = S.Scene(cornell)
+    mlp = C.c_void_p()
+    S.check(S.lib().srt_mlp_create(9, C.byref(mlp)))
+    S.check(S.lib().srt_mlp_set_box(mlp, (C.c_float * 3)(-1.05, -1.05, -1.05), (C.c_float * 3)(1.05, 1.05, 1.05)))
+    n = S._capi.SRT_MLP_PARAMS if hasattr(S._capi, "SRT_MLP_PARAMS") else 23552
+    before = np.zeros(n, np.float32)
+    S.check(S.lib().srt_mlp_get_params(mlp, before.ctypes.data_as(S._capi.f32p)))
+    srv = S.Server(hbm_budget_bytes=4 << 30, max_paths=1 << 16, max_jobs=4, iterations_per_step=4)
+    F = Films(cuda)
+    ft, fp = F.new(128 * 128), F.new(64 * 64)
+    t = srv.submit(scene, 128, 128, pt_params(4, 8, 3, 1, 1, 41), film=ft, cache=mlp, cache_train=True)
+    p = srv.submit(scene, 64, 64, pt_params(4, 8, 3, 1, 1, 42), film=fp)
+    srv.drain(300)
+    assert srv.info(t)["state"] == 2 and srv.info(p)["state"] == 2
+    img = F.host(ft)
+    assert np.all(np.isfinite(img)) and np.all(img[:, 3] == 1.0) and img[:, :3].mean() > 0.0
+    np.testing.assert_array_equal(F.host(fp), _alone(S, scene, 64, 64, pt_params(4, 8, 3, 1, 1, 42), cuda))
+    after = np.zeros(n, np.float32)
+    S.check(S.lib().srt_mlp_get_params(mlp, after.ctypes.data_as(S._capi.f32p)))
+    assert np.all(np.isfinite(after)) and not np.array_equal(before, after)
+    # a frozen job does not change the network
+    ff = F.new(64 * 64)
+    f = srv.submit(scene, 64, 64, pt_params(2, 8, 3, 1, 1, 43), film=ff, cache=mlp)
+    srv.drain(300)
+    assert srv.info(f)["state"] == 2
+    again = np.zeros(n, np.float32)
+    S.check(S.lib().srt_mlp_get_params(mlp, again.ctypes.data_as(S._capi.f32p)))
+    np.testing.assert_array_equal(after, again)
+    srv.close()
+    S.lib().srt_mlp_destroy(mlp)
