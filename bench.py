@@ -642,6 +642,30 @@ def profile_case(which="spheres"):
     launch; a few hundred launches in all."""
     import torch
     import srt_gb300 as S
+    if which == "mlp":
+        # the two networks' tensor-core kernels on 262,144 random rows: three
+        # NeuralRadiosity inferences (encoding + fused network), then three
+        # radiance-cache inferences
+        import ctypes as C
+        L = S.lib()
+        n = 262144
+        nr, mlp = C.c_void_p(), C.c_void_p()
+        S.check(L.srt_nr_create(7, C.byref(nr)))
+        S.check(L.srt_mlp_create(3, C.byref(mlp)))
+        x = torch.rand((n, 12), device="cuda")
+        y = torch.empty((n, 16), device="cuda")
+        rec = torch.rand((n, 16), device="cuda")
+        o4 = torch.empty((n, 4), device="cuda")
+        for _ in range(3):
+            S.check(L.srt_nr_infer(nr, C.c_void_p(x.data_ptr()), n, C.c_void_p(y.data_ptr()), None))
+        for _ in range(3):
+            S.check(L.srt_mlp_infer(mlp, C.c_void_p(rec.data_ptr()), n, C.c_void_p(o4.data_ptr()), None))
+        torch.cuda.synchronize()
+        ok = bool(torch.isfinite(y).all()) and bool(torch.isfinite(o4).all())
+        L.srt_nr_destroy(nr)
+        L.srt_mlp_destroy(mlp)
+        print(json.dumps({"profile_case": "mlp 262144 rows", "finite": ok}))
+        return
     if which == "cache":
         # radiance-cache frames of the learned-cache workload (1280x720, 1 spp,
         # online training on 2^16 paths per frame), every kernel launched directly
@@ -716,7 +740,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     ap.add_argument("--serving-rates", default="5,20,50", help="Poisson arrival rates (jobs/s) of the sweep")
     ap.add_argument("--serving-duration", type=float, default=30.0, help="seconds of arrivals per rate")
-    ap.add_argument("--profile-case", nargs="?", const="spheres", default=None, choices=["spheres", "cornell", "cache"],
+    ap.add_argument("--profile-case", nargs="?", const="spheres", default=None, choices=["spheres", "cornell", "cache", "mlp"],
                     help="short run for ncu captures (direct launches)")
     args = ap.parse_args()
     if args.profile_case:
