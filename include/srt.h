@@ -321,6 +321,12 @@ typedef struct srt_nr_stats {
     float network_ms;        /* fused five-layer tensor-core kernel       */
 } srt_nr_stats;
 srt_status srt_nr_set_profiling(srt_nr* nr, int32_t enable);
+/* Self-test of the bounded waits the tensor-core kernels use (no counterpart
+ * in the reference, which has no such kernels): one CTA waits on an mbarrier
+ * that nothing completes, gives up after limit_ns nanoseconds (1e3 .. 1e9)
+ * and reports it through the flag those kernels set.  Returns
+ * SRT_ERR_TIMEOUT, the expected outcome, with the device still usable. */
+srt_status srt_selftest_wait_timeout(int64_t limit_ns);
 srt_status srt_nr_get_stats(const srt_nr* nr, srt_nr_stats* stats);
 void srt_nr_destroy(srt_nr* nr);
 /* The LHS / RHS raygen of one sample with frame seed `seed` (curand stream

@@ -161,6 +161,7 @@ _PROTOS = [
     ("srt_nr_infer", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("srt_nr_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
     ("srt_nr_get_stats", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("srt_selftest_wait_timeout", C.c_int, [C.c_int64]),
     ("srt_nr_destroy", None, [C.c_void_p]),
     ("srt_nr_trace", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p]),

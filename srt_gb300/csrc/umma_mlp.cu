@@ -33,6 +33,18 @@ __global__ void k_pack_chunked(const float* __restrict__ src, int in, int out, _
     }
 }
 
+// One thread initialises an mbarrier that expects one arrival and waits for
+// a phase that nothing completes: the bounded wait of the fused kernels
+// runs out after limit_ns and the CTA reports it as they do.
+__global__ void k_wait_timeout_selftest(uint64_t limit_ns, int* err)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+    if (!mbar_wait(&bar, 0u, limit_ns)) atomicExch(err, 1);
+}
+
 std::mutex g_mu;
 int* g_err[128] = {};
 
@@ -92,3 +104,17 @@ srt_status umma_take_error()
 }
 
 }  // namespace srt
+
+using namespace srt;
+
+extern "C" srt_status srt_selftest_wait_timeout(int64_t limit_ns)
+{
+    clear_error();
+    if (limit_ns < 1000 || limit_ns > 1000000000) return set_error(SRT_ERR_ARG, "limit_ns out of [1e3, 1e9]");
+    SRT_TRY(umma_prepare());
+    SRT_TRY(umma_take_error());  // a timeout of an earlier kernel is not this call's
+    k_wait_timeout_selftest<<<1, 32>>>((uint64_t)limit_ns, umma_error_word());
+    SRT_CUDA_TRY(cudaGetLastError());
+    SRT_CUDA_TRY(cudaDeviceSynchronize());
+    return umma_take_error();
+}

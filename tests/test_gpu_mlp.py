@@ -129,3 +129,28 @@ def test_training_reduces_loss(cuda):
     rel = np.abs(out.cpu().numpy()[:, :3] - _target(rec)[:, :3]) / _target(rec)[:, :3]
     assert np.median(rel) < 0.1
     S.lib().srt_mlp_destroy(h)
+
+
+def test_bounded_wait_reports_a_timeout_and_the_device_stays_usable(cuda):
+    """The tensor-core kernels' waits on their mbarriers are bounded: a wait
+    on a phase that nothing completes (a self-test kernel) gives up after its
+    limit and comes back as SRT_ERR_TIMEOUT; the next calls work normally."""
+    import ctypes as C
+    import time
+    import torch
+    import srt_gb300 as S
+    L = S.lib()
+    t0 = time.perf_counter()
+    assert L.srt_selftest_wait_timeout(2_000_000) == 4  # SRT_ERR_TIMEOUT after 2 ms
+    assert time.perf_counter() - t0 >= 0.002
+    assert "gave up" in L.srt_last_error().decode()
+    assert L.srt_selftest_wait_timeout(10) == 1  # out of range
+    # the context is intact: a network inference and a render still run
+    mlp = C.c_void_p()
+    S.check(L.srt_mlp_create(1, C.byref(mlp)))
+    rec = torch.rand((1000, 16), device=cuda)
+    out = torch.zeros((1000, 4), device=cuda)
+    S.check(L.srt_mlp_infer(mlp, C.c_void_p(rec.data_ptr()), 1000, C.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    assert torch.isfinite(out).all()
+    L.srt_mlp_destroy(mlp)

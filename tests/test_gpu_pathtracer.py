@@ -162,6 +162,35 @@ def test_cornell_512_queue_counts_exact(cuda):
     assert rel <= 1e-3
 
 
+def test_8k_frame_queue_counts_and_samples(cuda):
+    """The largest film class the benchmark's engine is sized for: a
+    7680x4320 frame (33,177,600 paths in flight) of the Cornell box at 1 spp,
+    depth 8: every pixel finishes exactly one sample, no queue or stack
+    overflows, and the first iteration's queue counts equal the oracle's
+    exactly (33,177,600 camera rays, hits, misses, shadow rays)."""
+    import torch
+    import srt_gb300 as S
+    w, h = 7680, 4320
+    sa = S.procedural("cornell")
+    sa.set_aspect(w / h)
+    sc = S.Scene(sa)
+    pt = S.PathTracer(sc, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device=cuda)
+    p = pt_params(1, 8, 3, 1, 1, 5)
+    pt.render(film, p)
+    torch.cuda.synchronize()
+    st = pt.stats()
+    assert st["samples"] == w * h and st["stack_overflows"] == 0
+    assert np.all(pt.pixel_samples() == 1)
+    gpu = pt.iteration_counts()
+    assert np.all(np.isfinite(film[:, :3].cpu().numpy())) and float(film[:, 3].min()) == 1.0
+    osc = O.OracleScene(sa.desc(), bvh=True)
+    _, _, _, cnt, ora = osc.render_timeline(w, h, p, threads=os.cpu_count() or 1)
+    assert cnt[0] == w * h
+    np.testing.assert_array_equal(gpu[0].astype(np.int64), ora[0])
+    assert gpu[0, 0] == w * h
+
+
 def test_zero_spp_and_zero_depth(cuda):
     sa = _cornell()
     for spp, md in ((0, 8), (4, 0)):
