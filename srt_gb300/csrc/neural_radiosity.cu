@@ -282,8 +282,9 @@ __global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inp
             } else {
                 e = (int64_t)((x * 1u ^ y * 2654435761u ^ z * 805459861u) & ((1u << kNrLog2T) - 1u));
             }
-            const float4* p = reinterpret_cast<const float4*>(g + e * kNrFeat);
-            const float4 f0 = __ldg(p), f1 = __ldg(p + 1);
+            // one 32-byte entry, 32-byte aligned: one 256-bit load
+            float4 f0, f1;
+            ld_nc_v8f(reinterpret_cast<const float4*>(g + e * kNrFeat), f0, f1);
             acc[0] += wc * f0.x;
             acc[1] += wc * f0.y;
             acc[2] += wc * f0.z;

@@ -264,8 +264,8 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                 // miss: environment light (path_tracer.cu:81-85)
                 L_add = beta * env_radiance(S, rd);
             } else {
-                const float4* tp = S.tris + 3 * (size_t)tri;
-                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float4 a, b, c;
+                load_tri(S.tris, (uint32_t)tri, a, b, c);
                 float3 v0 = f3(a), v1 = f3(b), v2 = f3(c);
                 InstanceRec ir = S.insts[__float_as_int(a.w)];
                 float3 base_color;
