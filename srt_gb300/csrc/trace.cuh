@@ -465,6 +465,10 @@ __device__ __forceinline__ void trace_persistent(int64_t n, unsigned long long* 
 {
     const uint32_t full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    // Warps past the first n / 32 leave before touching the fetch counter:
+    // the ones below take every ray, and a short queue (the end of a frame)
+    // does not cost one contended atomic per resident warp of the grid.
+    if ((int64_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 >= n) return;
     int64_t ray = -1;
     TravState s;
     bool drained = false;
