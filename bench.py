@@ -376,9 +376,10 @@ CLOSEST_QUEUE_BYTES = 52
 
 
 def kernel_bytes(st, hist, npix):
-    """Algorithmic bytes of one frame per kernel, from the frame's exact
-    counts and the queue layout (wavefront.cuh): R closest rays (H of them
-    hits), Sh shadow rays, N samples over npix pixels.
+    """Algorithmic bytes of one frame's wavefront iterations per kernel, from
+    their exact counts (the iteration history: the finishing kernel's rays
+    are not in it) and the queue layout (wavefront.cuh): R closest rays (H of
+    them hits), Sh shadow rays, N samples ended over npix pixels.
       k_closest (+ k_order): ray 32 B + job word 4 B in, hit 16 B out; order
         pass 4 B in, 4 B out (BVH nodes and triangles are not included: they
         come from ncu's DRAM bytes where the scene exceeds L2)
@@ -390,12 +391,11 @@ def kernel_bytes(st, hist, npix):
       k_shadow: 48 B in + 32 B radiance update per ray
       k_regen: done record 32 B + radiance 32 B + film 32 B per sample, 72 B
         per next-sample camera ray"""
-    R, Sh, N = st["closest_rays"], st["shadow_rays"], st["samples"]
-    Hh = int(hist[:, 1].sum())
+    R, Hh, Sh, N = (int(hist[:, k].sum()) for k in (0, 1, 3, 4))
     return {"k_closest": R * (CLOSEST_QUEUE_BYTES + 8),
             "k_shade": R * 92 + Hh * 144 + Sh * 96 + (R - N) * 72 + N * 32 + (R - Hh) * 32,
             "k_shadow": Sh * 80,
-            "k_regen": N * 96 + (N - npix) * 72,
+            "k_regen": N * 96 + max(0, N - npix) * 72,
             "k_advance": 0}
 
 
@@ -437,7 +437,8 @@ def cornell_eval(S, steps=10, warmup=3, cpu=True):
     p.seed = SEED
     pt.set_profiling(2)
     pt.render(film, p, stream)
-    kms = dict(zip(KERNELS, pt.stats()["kernel_ms"]))
+    st_p = pt.stats()
+    kms = dict(zip(KERNELS, st_p["kernel_ms"]))
     pt.set_profiling(0)
     top = max(kms, key=kms.get)
     alg = kernel_bytes(st, hist, w * h)
@@ -452,8 +453,9 @@ def cornell_eval(S, steps=10, warmup=3, cpu=True):
     out = {"workload": "Cornell box, 36 triangles, 512x512, 16 spp, depth 8, rr 3, NEE + MIS",
            "msamples_per_s": round(w * h * spp / (ms / 1e3) / 1e6, 1), "ms_per_frame": round(ms, 3),
            "closest_rays_per_frame": st["closest_rays"], "shadow_rays_per_frame": st["shadow_rays"],
-           "iterations": st["iterations"],
-           "profile_frame_kernel_ms": {k: round(v, 3) for k, v in kms.items()},
+           "iterations": st["iterations"], "tail_paths": st["tail_paths"],
+           "profile_frame_kernel_ms": dict({k: round(v, 3) for k, v in kms.items()},
+                                           k_finish=round(st_p["tail_ms"], 3)),
            "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak,
                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                         "traffic": traffic, "traffic_source": rec["capture"] if rec else None,
@@ -822,6 +824,7 @@ def main():
     pt.set_profiling(1)
     pt.render(film, params, stream)
     st = pt.stats()
+    hist = pt.iteration_counts()
     pt.set_profiling(2)
     pt.render(film, params, stream)
     st_t = pt.stats()
@@ -829,12 +832,18 @@ def main():
     kms = dict(zip(KERNELS, st_t["kernel_ms"]))
     top = max(kms, key=kms.get)
     iters = max(1, st["iterations"])
+    # the traversal counters include the finishing kernel's rays: scale them
+    # to the rays of the wavefront iterations (whose launches are timed here)
     if top == "k_shadow":
-        rays, nodes, tris, per_ray = st["shadow_rays"], st["shadow_nodes"], st["shadow_tris"], 44
+        all_rays, nodes, tris, per_ray = st["shadow_rays"], st["shadow_nodes"], st["shadow_tris"], 44
+        rays = int(hist[:, 3].sum())
         queue = 48
     else:
-        rays, nodes, tris, per_ray = st["closest_rays"], st["closest_nodes"], st["closest_tris"], 40
+        all_rays, nodes, tris, per_ray = st["closest_rays"], st["closest_nodes"], st["closest_tris"], 40
+        rays = int(hist[:, 0].sum())
         queue = CLOSEST_QUEUE_BYTES
+    wave = rays / max(all_rays, 1)
+    nodes, tris = nodes * wave, tris * wave
     peak, peak_kind = peaks()
     # algorithmic bytes per ray (the scope table): the ray and its hit
     # (per_ray) plus the BVH traffic ncu measured in DRAM per ray (its DRAM
@@ -874,9 +883,12 @@ def main():
             "gpu_launches": int(launches),
             "mrays_per_s": round((st["closest_rays"] + st["shadow_rays"]) / (ms / args.steps / 1e3) / 1e6, 1),
             "roofline": roof,
-            "profile_frame": {"kernel_ms": {k: round(v, 2) for k, v in kms.items()},
+            "profile_frame": {"kernel_ms": dict({k: round(v, 2) for k, v in kms.items()},
+                                                k_finish=round(st_t["tail_ms"], 2)),
                               "closest_rays": st["closest_rays"], "shadow_rays": st["shadow_rays"],
-                              "iterations": st["iterations"]},
+                              "iterations": st["iterations"], "tail_paths": st["tail_paths"],
+                              "wavefront_closest_rays": int(hist[:, 0].sum()),
+                              "wavefront_shadow_rays": int(hist[:, 3].sum())},
         }
         line["bxdf"] = bxdf_eval_bench(S, cpu=not args.no_cpu_baseline)
         line["cornell"] = cornell_eval(S, cpu=not args.no_cpu_baseline)

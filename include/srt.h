@@ -260,6 +260,13 @@ typedef struct srt_pt_stats {
      * work: 128-byte nodes visited and triangles tested. */
     float kernel_ms[5];
     int64_t closest_nodes, closest_tris, shadow_nodes, shadow_tris;
+    /* End of the frame (srt_pt_set_tail): paths the finishing kernel took
+     * from the queue, each carried to its pixel's last sample, and that
+     * kernel's device time (profiling only).  Rays it traced are in
+     * closest_rays / shadow_rays; `iterations` counts the wavefront
+     * iterations before it. */
+    int64_t tail_paths;
+    float tail_ms;
 } srt_pt_stats;
 
 typedef struct srt_pt srt_pt;
@@ -359,6 +366,18 @@ srt_status srt_pt_set_profiling(srt_pt* pt, int32_t enable);
  * kernel-level tools that do not look inside graphs see every kernel). */
 enum { SRT_LAUNCH_GRAPH = 0, SRT_LAUNCH_DIRECT = 1 };
 srt_status srt_pt_set_launch_mode(srt_pt* pt, int32_t mode);
+
+/* End of a frame.  Each pixel's samples run one after another on its own
+ * curand stream (path_tracer.cu:56-68), so near the end of a frame few
+ * paths are left while a wavefront iteration still lasts as long as its
+ * slowest ray.  Once at most `max_paths` paths are in flight, one kernel
+ * takes them over and carries each, with its pixel's remaining samples, to
+ * the end, through the same device code (the image is the same bit for
+ * bit; iteration counts past that point are not recorded).  0 disables it;
+ * the default is SRT_PT_TAIL_DEFAULT paths.  Renders with a radiance cache
+ * always run their iterations to the end. */
+enum { SRT_PT_TAIL_DEFAULT = 32768 };
+srt_status srt_pt_set_tail(srt_pt* pt, int64_t max_paths);
 
 /* Queue counts of the last render's wavefront iterations (no counterpart in
  * the reference's megakernel; these are the integer counts its per-pixel

@@ -15,8 +15,8 @@ import numpy as np
 from . import _capi
 from ._capi import (BXDF_DIELECTRIC, BXDF_DIFFUSE, BXDF_DIFFUSE_TRANSMISSION, BXDF_DISNEY, CAMERA_ORTHOGRAPHIC,
                     CAMERA_PERSPECTIVE, LAUNCH_DIRECT, LAUNCH_GRAPH, METRIC_MAPE, METRIC_MSE, METRIC_RELMSE,
-                    METRIC_SMAPE, PT_FIXED_CDF_REMAP, RNG_CURAND, RNG_HASH, TONE_ACES, TONE_CLAMP, TONE_NONE,
-                    TONE_REINHARD, TONE_UNCHARTED2, SrtError, check, lib)
+                    METRIC_SMAPE, PT_FIXED_CDF_REMAP, PT_TAIL_DEFAULT, RNG_CURAND, RNG_HASH, TONE_ACES, TONE_CLAMP,
+                    TONE_NONE, TONE_REINHARD, TONE_UNCHARTED2, SrtError, check, lib)
 
 __all__ = [
     "SceneArrays", "Scene", "PathTracer", "procedural", "import_scene", "lib", "check", "SrtError", "bxdf_sample", "bxdf_eval",
@@ -279,6 +279,11 @@ class PathTracer:
         """LAUNCH_GRAPH (one graph launch per frame) or LAUNCH_DIRECT (the
         same kernels launched one by one)."""
         check(lib().srt_pt_set_launch_mode(self.handle, int(mode)))
+
+    def set_tail(self, max_paths):
+        """Paths in flight at or below which one kernel finishes the frame's
+        remaining samples (0: the wavefront iterations run to the end)."""
+        check(lib().srt_pt_set_tail(self.handle, int(max_paths)))
 
     def iteration_counts(self, max_iterations=4096):
         """int32 [iterations, 5]: closest rays, hits, misses, shadow rays,

@@ -25,6 +25,7 @@ RNG_CURAND, RNG_HASH = 0, 1
 PT_FIXED_CDF_REMAP = 1
 PT_NEE_FIRST_VERTEX_ONLY = 2
 LAUNCH_GRAPH, LAUNCH_DIRECT = 0, 1
+PT_TAIL_DEFAULT = 32768
 TONE_NONE, TONE_CLAMP, TONE_REINHARD, TONE_UNCHARTED2, TONE_ACES = 0, 1, 2, 3, 4
 METRIC_MSE, METRIC_MAPE, METRIC_SMAPE, METRIC_RELMSE = 0, 1, 2, 3
 MEASURE_NONE, MEASURE_REFERENCE, MEASURE_ERROR = 0, 1, 2
@@ -93,7 +94,8 @@ class PtStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("closest_rays", C.c_int64), ("shadow_rays", C.c_int64),
                 ("iterations", C.c_int64), ("stack_overflows", C.c_int64), ("render_ms", C.c_float),
                 ("kernel_launches", C.c_int64), ("kernel_ms", C.c_float * 5), ("closest_nodes", C.c_int64),
-                ("closest_tris", C.c_int64), ("shadow_nodes", C.c_int64), ("shadow_tris", C.c_int64)]
+                ("closest_tris", C.c_int64), ("shadow_nodes", C.c_int64), ("shadow_tris", C.c_int64),
+                ("tail_paths", C.c_int64), ("tail_ms", C.c_float)]
 
 
 class ServerConfig(C.Structure):
@@ -170,6 +172,7 @@ _PROTOS = [
     ("srt_pt_get_stats", C.c_int, [C.c_void_p, C.POINTER(PtStats)]),
     ("srt_pt_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
     ("srt_pt_set_launch_mode", C.c_int, [C.c_void_p, C.c_int32]),
+    ("srt_pt_set_tail", C.c_int, [C.c_void_p, C.c_int64]),
     ("srt_pt_get_iteration_counts", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     ("srt_pt_get_pixel_samples", C.c_int, [C.c_void_p, C.c_void_p]),
     ("srt_pt_destroy", None, [C.c_void_p]),

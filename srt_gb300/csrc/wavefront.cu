@@ -218,6 +218,168 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(const float4* __restric
 #endif
 constexpr int kShadeThreads = SRT_SHADE_THREADS;
 
+// Shades one path vertex (path_tracer.cu:79-166 for one segment): the
+// path's state (origin and pixel, direction and scatter pdf, throughput and
+// flags, rng words ra / rb) and its closest hit h (t, u, v, triangle bits)
+// in; the vertex's emitted or environment radiance, the next segment, the
+// shadow ray and whether the path ended out.  k_shade runs it for every
+// queue entry; k_finish for the paths it carries to their last sample.
+template <bool kCache>
+__device__ __forceinline__ void shade_vertex(const JobRec* __restrict__ jobs, float4 o4, float4 d4, float4 b4, float4 h,
+                                             bool& push_next, bool& push_shadow, bool& terminate, bool& push_query,
+                                             float4 (&qrec)[4], float3& ro, float3& rd, float3& beta, float3& L_add,
+                                             float3& sh_o, float3& sh_d, float3& sh_c, float& sh_t, float& pdf_next,
+                                             uint32_t& flags, int& pix, int& job, uint4& ra, uint2& rb)
+{
+    flags = __float_as_uint(b4.w);
+    job = (int)(flags >> 16);
+    int depth = (int)(flags & 0xffu);
+    bool specular = (flags & 0x100u) != 0u;
+    pix = __float_as_int(o4.w);
+    ro = f3(o4);
+    rd = f3(d4);
+    beta = f3(b4);
+    const float scatter_pdf = d4.w;
+    const JobRec& J = jobs[job];
+    const SceneView& S = J.scene;
+    const int tri = __float_as_int(h.w);
+    terminate = true;
+    if (tri < 0) {
+        // miss: environment light (path_tracer.cu:81-85)
+        L_add = beta * env_radiance(S, rd);
+    } else {
+        float4 a, b, c;
+        load_tri(S.tris, (uint32_t)tri, a, b, c);
+        float3 v0 = f3(a), v1 = f3(b), v2 = f3(c);
+        InstanceRec ir = S.insts[__float_as_int(a.w)];
+        float3 base_color;
+        float4 em;
+        int mflags;
+        Bxdf bx = unpack_bxdf(S.mats, ir.material, base_color, em, mflags);
+        // get_hitinfo (hit_info.h:27-64)
+        float u = h.y, v = h.z;
+        float3 pos = v0 * (1.0f - u - v) + v1 * u + v2 * v;
+        float3 ng = normalize(cross(v1 - v0, v2 - v0));
+        float3 sn = ng;
+        if (ir.attr & kAttrNormals) {
+            const float4* np = S.normals + 3 * (size_t)tri;
+            sn = normalize(f3(__ldg(np)) * (1.0f - u - v) + f3(__ldg(np + 1)) * u + f3(__ldg(np + 2)) * v);
+        }
+        if (mflags & kMatTextured)
+            apply_material_textures(S, ir.attr, ir.material, __float_as_int(a.w), tri, u, v, base_color, em, sn);
+        if (dot(ng, sn) < 0.0f) ng = -ng;
+        if (mflags & kMatEmissive) {
+            // emitter hit with MIS (path_tracer.cu:88-106)
+            float cos_i = dot(ng, -rd);
+            if (cos_i > 1e-4f) {
+                float mis = 1.0f;
+                if (J.use_nee && !specular) {
+                    mis = 0.0f;
+                    if (J.use_mis) {
+                        float t2 = dot(pos - ro, pos - ro);
+                        float lpdf = S.lights[ir.light_id].pdf * t2 / cos_i;
+                        mis = scatter_pdf / (lpdf + scatter_pdf);
+                    }
+                }
+                L_add = beta * f3(em) * mis;
+            }
+        } else {
+            if (dot(ng, -rd) < 0.0f) ng = -ng;
+            const float3 wo = -rd;
+            // radiance cache: non-training pixels end at the second vertex
+            const CacheRec& Cc = J.cache;
+            const bool cache_job = kCache && Cc.w != nullptr;
+            const bool train_pix = cache_job && (pix % Cc.train_stride) == Cc.train_phase;
+            if (cache_job && !train_pix && depth == 1) {
+                push_query = !Cc.region_off || !Cc.region_off[region_cell(Cc, pos)];
+                if (!push_query) atomicAdd(Cc.q_count + 1, 1);
+            }
+            if (push_query) {
+                qrec[0] = make_float4(pos.x, pos.y, pos.z, bx.type == BXDF_DISNEY ? bx.roughness : 1.0f);
+                qrec[1] = make_float4(ng.x, ng.y, ng.z, 0.0f);
+                qrec[2] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+                qrec[3] = make_float4(base_color.x, base_color.y, base_color.z, 0.0f);
+            } else {
+            if (train_pix && depth >= 1 && depth <= kTrainVertices &&
+                __float_as_int(J.lpath[pix].w) == 0) {
+                // training vertex: features, arriving throughput, radiance gathered so far
+                int slot = (pix / Cc.train_stride) * kTrainVertices + depth - 1;
+                float4* tr = Cc.t_rec + 4 * (size_t)slot;
+                tr[0] = make_float4(pos.x, pos.y, pos.z, bx.type == BXDF_DISNEY ? bx.roughness : 1.0f);
+                tr[1] = make_float4(ng.x, ng.y, ng.z, 0.0f);
+                tr[2] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+                tr[3] = make_float4(base_color.x, base_color.y, base_color.z, 0.0f);
+                float4 lnow = J.lpath[pix];
+                Cc.t_aux[2 * (size_t)slot] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+                Cc.t_aux[2 * (size_t)slot + 1] = make_float4(lnow.x, lnow.y, lnow.z, 0.0f);
+                Cc.t_len[pix / Cc.train_stride] = depth;
+            }
+            Rng rng;
+            rng.load(ra, rb);
+            float3 tan = (fabsf(sn.x) > fabsf(sn.y)) ? make_float3(0.f, 1.f, 0.f) : make_float3(1.f, 0.f, 0.f);
+            if (ir.attr & kAttrTangents) {
+                // the mesh's interpolated tangent (hit_info.h:48-50)
+                const float4* gp = S.tangents + 3 * (size_t)tri;
+                tan = f3(__ldg(gp)) * (1.0f - u - v) + f3(__ldg(gp + 1)) * u + f3(__ldg(gp + 2)) * v;
+            }
+            Frame fr = Frame::from_normal_tangent(sn, tan);
+            const bool transmissive = (mflags & kMatTransmissive) != 0;
+            // NEE with MIS (path_tracer.cu:113-142)
+            if (J.use_nee && !(mflags & kMatSpecular) &&
+                !(depth > 0 && (J.flags & SRT_PT_NEE_FIRST_VERTEX_ONLY))) {
+                float lu = rng.next();
+                float lv = rng.next();
+                LightSample ls = sample_light(S, lu, lv, (J.flags & SRT_PT_FIXED_CDF_REMAP) != 0);
+                float3 sd = normalize(ls.pos - pos);
+                float cos_o = dot(ng, sd);
+                float cos_l = dot(ls.normal, -sd);
+                float t = length(ls.pos - pos);
+                if (cos_l > 1e-4f && ls.pdf > 1e-4f && t > 1e-3f && (cos_o > 0.0f || transmissive)) {
+                    float lpdf = ls.pdf * t * t / cos_l;
+                    float mis = 1.0f;
+                    if (J.use_mis) {
+                        float mpdf = material_pdf(bx, fr, sd, wo, base_color);
+                        mis = lpdf / (lpdf + mpdf);
+                    }
+                    float3 fv = material_eval(bx, fr, sd, wo, base_color);
+                    sh_c = beta * fv * fabsf(cos_o) * ls.emission * mis / lpdf;
+                    sh_o = pos;
+                    sh_d = sd;
+                    sh_t = t - 1e-3f;
+                    push_shadow = true;
+                }
+            }
+            // BSDF sample (path_tracer.cu:145-153)
+            float bu = rng.next();
+            float bv = rng.next();
+            BxdfSample ms = material_sample(bx, fr, wo, make_float2(bu, bv), base_color);
+            if (ms.pdf > 1e-4f && !(dot(ms.wi, ng) < 0.0f && !transmissive)) {
+                beta *= ms.f / ms.pdf;
+                if (!ms.delta) beta *= fabsf(dot(ms.wi, ng));
+                bool alive = true;
+                // Russian roulette (path_tracer.cu:156-161)
+                if (depth >= J.rr_depth) {
+                    float p = fmaxf(fmaxf(beta.x, fmaxf(beta.y, beta.z)), 0.05f);
+                    if (rng.next() > p)
+                        alive = false;
+                    else
+                        beta /= p;
+                }
+                if (alive && depth + 1 < J.max_depth) {
+                    terminate = false;
+                    push_next = true;
+                    ro = pos;
+                    rd = ms.wi;
+                    pdf_next = ms.pdf;
+                    flags = pack_flags(depth + 1, (mflags & kMatSpecular) != 0, job);
+                }
+            }
+            rng.store(ra, rb);
+            }
+        }
+    }
+}
+
 // kCache: the iteration carries radiance-cache jobs (queries and training
 // records); the plain variant leaves that code out
 template <bool kCache>
@@ -247,153 +409,8 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
             float4 h = hits[i];
             ra = q.ra[i];
             rb = q.rb[i];
-            flags = __float_as_uint(b4.w);
-            job = (int)(flags >> 16);
-            int depth = (int)(flags & 0xffu);
-            bool specular = (flags & 0x100u) != 0u;
-            pix = __float_as_int(o4.w);
-            ro = f3(o4);
-            rd = f3(d4);
-            beta = f3(b4);
-            const float scatter_pdf = d4.w;
-            const JobRec& J = jobs[job];
-            const SceneView& S = J.scene;
-            const int tri = __float_as_int(h.w);
-            terminate = true;
-            if (tri < 0) {
-                // miss: environment light (path_tracer.cu:81-85)
-                L_add = beta * env_radiance(S, rd);
-            } else {
-                float4 a, b, c;
-                load_tri(S.tris, (uint32_t)tri, a, b, c);
-                float3 v0 = f3(a), v1 = f3(b), v2 = f3(c);
-                InstanceRec ir = S.insts[__float_as_int(a.w)];
-                float3 base_color;
-                float4 em;
-                int mflags;
-                Bxdf bx = unpack_bxdf(S.mats, ir.material, base_color, em, mflags);
-                // get_hitinfo (hit_info.h:27-64)
-                float u = h.y, v = h.z;
-                float3 pos = v0 * (1.0f - u - v) + v1 * u + v2 * v;
-                float3 ng = normalize(cross(v1 - v0, v2 - v0));
-                float3 sn = ng;
-                if (ir.attr & kAttrNormals) {
-                    const float4* np = S.normals + 3 * (size_t)tri;
-                    sn = normalize(f3(__ldg(np)) * (1.0f - u - v) + f3(__ldg(np + 1)) * u + f3(__ldg(np + 2)) * v);
-                }
-                if (mflags & kMatTextured)
-                    apply_material_textures(S, ir.attr, ir.material, __float_as_int(a.w), tri, u, v, base_color, em, sn);
-                if (dot(ng, sn) < 0.0f) ng = -ng;
-                if (mflags & kMatEmissive) {
-                    // emitter hit with MIS (path_tracer.cu:88-106)
-                    float cos_i = dot(ng, -rd);
-                    if (cos_i > 1e-4f) {
-                        float mis = 1.0f;
-                        if (J.use_nee && !specular) {
-                            mis = 0.0f;
-                            if (J.use_mis) {
-                                float t2 = dot(pos - ro, pos - ro);
-                                float lpdf = S.lights[ir.light_id].pdf * t2 / cos_i;
-                                mis = scatter_pdf / (lpdf + scatter_pdf);
-                            }
-                        }
-                        L_add = beta * f3(em) * mis;
-                    }
-                } else {
-                    if (dot(ng, -rd) < 0.0f) ng = -ng;
-                    const float3 wo = -rd;
-                    // radiance cache: non-training pixels end at the second vertex
-                    const CacheRec& Cc = J.cache;
-                    const bool cache_job = kCache && Cc.w != nullptr;
-                    const bool train_pix = cache_job && (pix % Cc.train_stride) == Cc.train_phase;
-                    if (cache_job && !train_pix && depth == 1) {
-                        push_query = !Cc.region_off || !Cc.region_off[region_cell(Cc, pos)];
-                        if (!push_query) atomicAdd(Cc.q_count + 1, 1);
-                    }
-                    if (push_query) {
-                        qrec[0] = make_float4(pos.x, pos.y, pos.z, bx.type == BXDF_DISNEY ? bx.roughness : 1.0f);
-                        qrec[1] = make_float4(ng.x, ng.y, ng.z, 0.0f);
-                        qrec[2] = make_float4(wo.x, wo.y, wo.z, 0.0f);
-                        qrec[3] = make_float4(base_color.x, base_color.y, base_color.z, 0.0f);
-                    } else {
-                    if (train_pix && depth >= 1 && depth <= kTrainVertices &&
-                        __float_as_int(J.lpath[pix].w) == 0) {
-                        // training vertex: features, arriving throughput, radiance gathered so far
-                        int slot = (pix / Cc.train_stride) * kTrainVertices + depth - 1;
-                        float4* tr = Cc.t_rec + 4 * (size_t)slot;
-                        tr[0] = make_float4(pos.x, pos.y, pos.z, bx.type == BXDF_DISNEY ? bx.roughness : 1.0f);
-                        tr[1] = make_float4(ng.x, ng.y, ng.z, 0.0f);
-                        tr[2] = make_float4(wo.x, wo.y, wo.z, 0.0f);
-                        tr[3] = make_float4(base_color.x, base_color.y, base_color.z, 0.0f);
-                        float4 lnow = J.lpath[pix];
-                        Cc.t_aux[2 * (size_t)slot] = make_float4(beta.x, beta.y, beta.z, 0.0f);
-                        Cc.t_aux[2 * (size_t)slot + 1] = make_float4(lnow.x, lnow.y, lnow.z, 0.0f);
-                        Cc.t_len[pix / Cc.train_stride] = depth;
-                    }
-                    Rng rng;
-                    rng.load(ra, rb);
-                    float3 tan = (fabsf(sn.x) > fabsf(sn.y)) ? make_float3(0.f, 1.f, 0.f) : make_float3(1.f, 0.f, 0.f);
-                    if (ir.attr & kAttrTangents) {
-                        // the mesh's interpolated tangent (hit_info.h:48-50)
-                        const float4* gp = S.tangents + 3 * (size_t)tri;
-                        tan = f3(__ldg(gp)) * (1.0f - u - v) + f3(__ldg(gp + 1)) * u + f3(__ldg(gp + 2)) * v;
-                    }
-                    Frame fr = Frame::from_normal_tangent(sn, tan);
-                    const bool transmissive = (mflags & kMatTransmissive) != 0;
-                    // NEE with MIS (path_tracer.cu:113-142)
-                    if (J.use_nee && !(mflags & kMatSpecular) &&
-                        !(depth > 0 && (J.flags & SRT_PT_NEE_FIRST_VERTEX_ONLY))) {
-                        float lu = rng.next();
-                        float lv = rng.next();
-                        LightSample ls = sample_light(S, lu, lv, (J.flags & SRT_PT_FIXED_CDF_REMAP) != 0);
-                        float3 sd = normalize(ls.pos - pos);
-                        float cos_o = dot(ng, sd);
-                        float cos_l = dot(ls.normal, -sd);
-                        float t = length(ls.pos - pos);
-                        if (cos_l > 1e-4f && ls.pdf > 1e-4f && t > 1e-3f && (cos_o > 0.0f || transmissive)) {
-                            float lpdf = ls.pdf * t * t / cos_l;
-                            float mis = 1.0f;
-                            if (J.use_mis) {
-                                float mpdf = material_pdf(bx, fr, sd, wo, base_color);
-                                mis = lpdf / (lpdf + mpdf);
-                            }
-                            float3 fv = material_eval(bx, fr, sd, wo, base_color);
-                            sh_c = beta * fv * fabsf(cos_o) * ls.emission * mis / lpdf;
-                            sh_o = pos;
-                            sh_d = sd;
-                            sh_t = t - 1e-3f;
-                            push_shadow = true;
-                        }
-                    }
-                    // BSDF sample (path_tracer.cu:145-153)
-                    float bu = rng.next();
-                    float bv = rng.next();
-                    BxdfSample ms = material_sample(bx, fr, wo, make_float2(bu, bv), base_color);
-                    if (ms.pdf > 1e-4f && !(dot(ms.wi, ng) < 0.0f && !transmissive)) {
-                        beta *= ms.f / ms.pdf;
-                        if (!ms.delta) beta *= fabsf(dot(ms.wi, ng));
-                        bool alive = true;
-                        // Russian roulette (path_tracer.cu:156-161)
-                        if (depth >= J.rr_depth) {
-                            float p = fmaxf(fmaxf(beta.x, fmaxf(beta.y, beta.z)), 0.05f);
-                            if (rng.next() > p)
-                                alive = false;
-                            else
-                                beta /= p;
-                        }
-                        if (alive && depth + 1 < J.max_depth) {
-                            terminate = false;
-                            push_next = true;
-                            ro = pos;
-                            rd = ms.wi;
-                            pdf_next = ms.pdf;
-                            flags = pack_flags(depth + 1, (mflags & kMatSpecular) != 0, job);
-                        }
-                    }
-                    rng.store(ra, rb);
-                    }
-                }
-            }
+            shade_vertex<kCache>(jobs, o4, d4, b4, h, push_next, push_shadow, terminate, push_query, qrec, ro, rd,
+                                 beta, L_add, sh_o, sh_d, sh_c, sh_t, pdf_next, flags, pix, job, ra, rb);
         }
         // network query of a cached path (its radiance is added by k_cache)
         int32_t qslot = kCache ? warp_append_multi(jobs[job].cache.q_count, valid && push_query) : -1;
@@ -559,6 +576,138 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
     }
 }
 
+// The end of a frame.  A wavefront iteration lasts as long as its slowest
+// ray, however few paths are left, and each pixel's samples follow one
+// another (one curand stream per pixel), so the last fifth of a frame's
+// iterations carries about 2 % of its rays.  Once k_advance finds at most
+// tail_below paths in flight, each thread here takes one queue entry and
+// carries that path, and its pixel's later samples, to the pixel's last
+// sample: closest hit as k_closest, shade_vertex as k_shade, the shadow ray
+// as k_shadow, the next sample as k_regen, in the same order on the same
+// values, so every pixel ends with the value the iterations would give.
+// Plain jobs only (no radiance-cache work).
+constexpr int kFinishThreads = kTraceThreads;
+
+template <bool kCount>
+__global__ void __launch_bounds__(kFinishThreads) k_finish(const JobRec* __restrict__ jobs, PathQueue q, Counters* ctr,
+                                                           int64_t capacity)
+{
+    if (!ctr->tail_go) return;
+    const int64_t n = min((int64_t)ctr->n_cur, capacity);
+    __shared__ uint2 stack_mem[kStackEntries * kFinishThreads];
+    Stack st{stack_mem + threadIdx.x, kFinishThreads, 0};
+    int overflow = 0;
+    TraceCount cnt, scnt;  // closest-hit and shadow traversal work (profiling variant)
+    int closest = 0, shadow = 0, ended = 0, taken = 0;
+    for (;;) {
+        const unsigned long long i = atomicAdd(&ctr->fetch_tail, 1ull);
+        if (i >= (unsigned long long)n) break;
+        ++taken;
+        float4 o4 = q.o[i], d4 = q.d[i], b4 = q.beta[i];
+        uint4 ra = q.ra[i];
+        uint2 rb = q.rb[i];
+        for (;;) {
+            // closest hit (k_closest)
+            TravState s;
+            {
+                const SceneView& S = jobs[__float_as_uint(b4.w) >> 16].scene;
+                trav_init(s, S.nodes, S.tris, f3(o4), f3(d4), 1e-3f, 1e16f, st);
+            }
+            while (!trav_advance<false, kCount>(s, st, overflow, cnt)) {
+            }
+            const float2 uv = hit_barycentrics(s);
+            const float4 h = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
+            ++closest;
+            // shading (k_shade)
+            bool push_next = false, push_shadow = false, terminate = false, push_query = false;
+            float4 qrec[4];
+            float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
+            float3 sh_o = f3(0.0f), sh_d = f3(0.0f), sh_c = f3(0.0f);
+            float sh_t = 0.0f, pdf_next = 0.0f;
+            uint32_t flags = 0;
+            int pix = 0, job = 0;
+            shade_vertex<false>(jobs, o4, d4, b4, h, push_next, push_shadow, terminate, push_query, qrec, ro, rd, beta,
+                                L_add, sh_o, sh_d, sh_c, sh_t, pdf_next, flags, pix, job, ra, rb);
+            const JobRec& J = jobs[job];
+            float4* lp = J.lpath + pix;
+            if (L_add.x != 0.0f || L_add.y != 0.0f || L_add.z != 0.0f || !finite3(L_add)) {
+                const float4 l = *lp;
+                *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, l.w);
+            }
+            // shadow ray (k_shadow)
+            if (push_shadow) {
+                ++shadow;
+                trav_init(s, J.scene.nodes, J.scene.tris, sh_o, sh_d, 1e-3f, sh_t, st, SRT_SHADOW_FAR_FIRST != 0);
+                while (!trav_advance<true, kCount>(s, st, overflow, scnt)) {
+                }
+                if (s.tri < 0) {
+                    const float4 l = *lp;
+                    *lp = make_float4(l.x + sh_c.x, l.y + sh_c.y, l.z + sh_c.z, l.w);
+                }
+            }
+            if (push_next) {
+                o4 = make_float4(ro.x, ro.y, ro.z, __int_as_float(pix));
+                d4 = make_float4(rd.x, rd.y, rd.z, pdf_next);
+                b4 = make_float4(beta.x, beta.y, beta.z, __uint_as_float(flags));
+                continue;
+            }
+            // the sample ends and the pixel's next one starts (k_regen)
+            ++ended;
+            const float4 l = *lp;
+            if (isfinite(l.x) && isfinite(l.y) && isfinite(l.z)) {
+                const float4 f = J.film[pix];
+                const float sp = (float)J.spp;
+                J.film[pix] = make_float4(f.x + l.x / sp, f.y + l.y / sp, f.z + l.z / sp, 1.0f);
+            }
+            const int k = __float_as_int(l.w) + 1;
+            *lp = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(k));
+            if (J.frame_done) atomicAdd(J.frame_done + (k - 1), 1);
+            if (k >= J.spp) {
+                if (J.pixels_done) atomicAdd(J.pixels_done, 1);
+                break;
+            }
+            Rng rng;
+            rng.load(ra, rb);
+            const int ix = pix % J.width, iy = pix / J.width;
+            const float xx = ((float)ix + rng.next()) / (float)J.width;
+            const float yy = ((float)iy + rng.next()) / (float)J.height;
+            float3 o, d;
+            camera_ray(J.cam, xx, yy, o, d);
+            rng.store(ra, rb);
+            o4 = make_float4(o.x, o.y, o.z, __int_as_float(pix));
+            d4 = make_float4(d.x, d.y, d.z, 1.0f);
+            b4 = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pack_flags(0, true, job)));
+        }
+    }
+    // one atomic per warp and counter
+    closest = __reduce_add_sync(kFull, closest);
+    shadow = __reduce_add_sync(kFull, shadow);
+    ended = __reduce_add_sync(kFull, ended);
+    taken = __reduce_add_sync(kFull, taken);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->closest_total), (unsigned long long)closest);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->shadow_total), (unsigned long long)shadow);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->started), (unsigned long long)ended);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->tail_paths), (unsigned long long)taken);
+    }
+    if (overflow) atomicAdd(&ctr->overflow_stack, 1);
+    if (kCount && (cnt.nodes | cnt.tris | scnt.nodes | scnt.tris)) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_nodes), (unsigned long long)cnt.nodes);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_tris), (unsigned long long)cnt.tris);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_nodes), (unsigned long long)scnt.nodes);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_tris), (unsigned long long)scnt.tris);
+    }
+}
+
+// After k_finish: nothing is left in flight.
+__global__ void k_end_tail(Counters* c)
+{
+    if (!c->tail_go) return;
+    c->n_cur = 0;
+    c->fetch_tail = 0;
+    c->tail_go = 0;
+}
+
 // Ends an iteration: swaps the queues' counts and, in the device-side loop,
 // decides whether the loop runs again (paths in flight, no overflow, and the
 // launch's iteration bound not reached: the loop always terminates).
@@ -594,18 +743,23 @@ __global__ void k_advance(Counters* c, IterCount* history, const JobRec* __restr
     c->n_hit = 0;
     c->n_miss = 0;
     c->run_iters += 1;
+    const bool clean = c->overflow_queue == 0 && c->overflow_stack == 0;
+    const bool tail = c->tail_below > 0 && c->n_cur > 0 && c->n_cur <= c->tail_below && clean;
+    c->tail_go = tail ? 1 : 0;
     if (kCond) {
-        const bool again = c->n_cur > 0 && c->run_iters < c->run_limit && c->overflow_queue == 0 &&
-                           c->overflow_stack == 0;
+        const bool again = c->n_cur > 0 && c->run_iters < c->run_limit && clean && !tail;
         cudaGraphSetConditional(cond, again ? 1u : 0u);
     }
 }
 
-// Starts a launch of the device-side loop: at most `limit` iterations.
-__global__ void k_begin_run(Counters* c, long long limit)
+// Starts a launch of the device-side loop: at most `limit` iterations,
+// handing the frame to k_finish at `tail_below` paths in flight (0: never).
+__global__ void k_begin_run(Counters* c, long long limit, int32_t tail_below)
 {
     c->run_iters = 0;
     c->run_limit = limit;
+    c->tail_below = tail_below;
+    c->tail_go = 0;
 }
 
 __global__ void k_rng_tape(int32_t seed, int64_t npix, int32_t ndraws, float* out)
@@ -633,6 +787,8 @@ Engine::~Engine()
         for (auto& b : a)
             for (auto& e : b)
                 if (e) cudaEventDestroy(e);
+    for (auto& e : ev_tail_)
+        if (e) cudaEventDestroy(e);
     if (graph_stream_) cudaStreamDestroy(graph_stream_);
     if (host_counters_) cudaFreeHost(host_counters_);
 }
@@ -690,6 +846,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     };
     grid_closest_ = resident(reinterpret_cast<const void*>(k_closest<false>));
     grid_shadow_ = resident(reinterpret_cast<const void*>(k_shadow<false>));
+    grid_finish_ = resident(reinterpret_cast<const void*>(k_finish<false>));
     grid_stride_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kThreads - 1) / kThreads, sms * 8));
     grid_order_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kOrderThreads - 1) / kOrderThreads, sms * 8));
     grid_shade_ = (int)std::max<int64_t>(
@@ -764,6 +921,26 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     mark(4, 1);
 }
 
+void Engine::launch_tail(cudaStream_t st, bool prof)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (prof) cudaStreamIsCapturing(st, &cs);
+    auto mark = [&](int e) {
+        if (!prof) return;
+        if (cs == cudaStreamCaptureStatusActive)
+            cudaEventRecordWithFlags(ev_tail_[e], st, cudaEventRecordExternal);
+        else
+            cudaEventRecord(ev_tail_[e], st);
+    };
+    mark(0);
+    if (prof && count_)
+        k_finish<true><<<grid_finish_, kFinishThreads, 0, st>>>(jobs_, q_[0], counters_, capacity_);
+    else
+        k_finish<false><<<grid_finish_, kFinishThreads, 0, st>>>(jobs_, q_[0], counters_, capacity_);
+    k_end_tail<<<1, 1, 0, st>>>(counters_);
+    mark(1);
+}
+
 void Engine::drop_graphs()
 {
     if (graph_) cudaGraphExecDestroy(graph_);
@@ -780,6 +957,7 @@ srt_status Engine::capture(bool prof)
         SRT_CUDA_TRY(cudaStreamBeginCapture(graph_stream_, cudaStreamCaptureModeThreadLocal));
         launch_iteration(0, graph_stream_, true, nullptr);
         launch_iteration(1, graph_stream_, true, nullptr);
+        if (tail_on()) launch_tail(graph_stream_, true);
         e = cudaStreamEndCapture(graph_stream_, &g);
         if (e != cudaSuccess) return cuda_error(e, "capture wavefront iteration");
     } else {
@@ -803,6 +981,15 @@ srt_status Engine::capture(bool prof)
             launch_iteration(0, graph_stream_, false, &cond);
             launch_iteration(1, graph_stream_, false, &cond);
             e = cudaStreamEndCapture(graph_stream_, &body);
+        }
+        // after the loop: the end of the frame, when the loop stopped for it
+        if (e == cudaSuccess && tail_on()) {
+            e = cudaStreamBeginCaptureToGraph(graph_stream_, g, &node, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                launch_tail(graph_stream_, false);
+                cudaGraph_t same = g;
+                e = cudaStreamEndCapture(graph_stream_, &same);
+            }
         }
         if (e != cudaSuccess) {
             cudaGraphDestroy(g);
@@ -855,6 +1042,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         for (auto& a : ev_)
             for (auto& b : a)
                 for (auto& e : b) SRT_CUDA_TRY(cudaEventCreate(&e));
+        for (auto& e : ev_tail_) SRT_CUDA_TRY(cudaEventCreate(&e));
     }
     if (!no_graph && prof && !graph_prof_) SRT_TRY(capture(true));
     if (!no_graph && !prof && !graph_) SRT_TRY(capture(false));
@@ -875,7 +1063,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         // queue or stack overflows, or the launch's iteration bound is reached
         const long long limit = budget_iters > 0 ? budget_iters : (max_iters > 0 ? max_iters + 1 : (1LL << 20));
         what = "start device loop";
-        k_begin_run<<<1, 1, 0, graph_stream_>>>(counters_, limit);
+        k_begin_run<<<1, 1, 0, graph_stream_>>>(counters_, limit, tail_on() ? tail_below_ : 0);
         e = cudaGetLastError();
         if (e == cudaSuccess) {
             what = "cudaGraphLaunch";
@@ -892,7 +1080,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         if (e == cudaSuccess) {
             const Counters& c = *host_counters_;
             iters = c.run_iters;
-            times_.launches += 1 + iters * (cache_ ? 7 : 6);
+            times_.launches += 1 + iters * (cache_ ? 7 : 6) + (tail_on() ? 2 : 0);
             if (c.overflow_queue)
                 status = set_error(SRT_ERR_ARG, "wavefront queue capacity exceeded");
             else if (c.overflow_stack)
@@ -902,6 +1090,13 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         }
     }
     int per_check = 2;
+    long long tail_seen = 0;
+    if ((prof || no_graph) && e == cudaSuccess) {
+        what = "start host loop";
+        k_begin_run<<<1, 1, 0, graph_stream_>>>(counters_, 1LL << 40, tail_on() ? tail_below_ : 0);
+        e = cudaGetLastError();
+        times_.launches += 1;
+    }
     while ((prof || no_graph) && e == cudaSuccess) {
         if (prof) per_check = 1;  // events are re-recorded by every launch: read them each time
         what = "cudaGraphLaunch";
@@ -910,12 +1105,13 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
                 what = "direct iteration launch";
                 launch_iteration(0, graph_stream_, prof, nullptr);
                 launch_iteration(1, graph_stream_, prof, nullptr);
+                if (tail_on()) launch_tail(graph_stream_, prof);
                 e = cudaGetLastError();
             } else {
                 e = cudaGraphLaunch(graph, graph_stream_);
             }
             iters += 2;
-            times_.launches += 2 * (cache_ ? 7 : 6);
+            times_.launches += 2 * (cache_ ? 7 : 6) + (tail_on() ? 2 : 0);
         }
         if (e != cudaSuccess) break;
         what = "copy counters";
@@ -933,6 +1129,13 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
                     e = cudaEventElapsedTime(&ms, ev_[par][k][0], ev_[par][k][1]);
                     times_.ms[k] += ms;
                 }
+            if (e == cudaSuccess && tail_on() && host_counters_->tail_paths != tail_seen) {
+                // only the check whose pair ended in k_finish: elsewhere it returned at once
+                float ms = 0.0f;
+                e = cudaEventElapsedTime(&ms, ev_tail_[0], ev_tail_[1]);
+                times_.tail_ms += ms;
+                tail_seen = host_counters_->tail_paths;
+            }
             if (e != cudaSuccess) break;
         }
         const Counters& c = *host_counters_;
@@ -990,6 +1193,7 @@ extern "C" srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t hei
     p->height = height;
     const size_t npix = (size_t)width * height;
     srt_status st = p->engine.init((int64_t)npix, 1);
+    p->engine.set_tail(SRT_PT_TAIL_DEFAULT);
     if (st == SRT_OK) st = p->job_buf.alloc(npix * 16 + 1024, "per-pixel path state");
     if (st != SRT_OK) {
         delete p;
@@ -1065,6 +1269,8 @@ extern "C" srt_status srt_pt_render(srt_pt* p, float* film, const srt_pt_params*
     p->stats.closest_tris = c.c_tris;
     p->stats.shadow_nodes = c.s_nodes;
     p->stats.shadow_tris = c.s_tris;
+    p->stats.tail_paths = c.tail_paths;
+    p->stats.tail_ms = (float)kt.tail_ms;
     return SRT_OK;
 }
 
@@ -1092,6 +1298,15 @@ extern "C" srt_status srt_pt_set_launch_mode(srt_pt* p, int32_t mode)
     if (mode != SRT_LAUNCH_GRAPH && mode != SRT_LAUNCH_DIRECT)
         return set_error(SRT_ERR_ARG, "launch mode must be SRT_LAUNCH_GRAPH or SRT_LAUNCH_DIRECT");
     p->engine.set_direct(mode == SRT_LAUNCH_DIRECT);
+    return SRT_OK;
+}
+
+extern "C" srt_status srt_pt_set_tail(srt_pt* p, int64_t max_paths)
+{
+    clear_error();
+    if (!p) return set_error(SRT_ERR_ARG, "NULL argument");
+    if (max_paths < 0 || max_paths > (int64_t)0x7fffffff) return set_error(SRT_ERR_ARG, "max_paths out of range");
+    p->engine.set_tail((int32_t)max_paths);
     return SRT_OK;
 }
 

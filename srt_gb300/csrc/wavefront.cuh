@@ -81,6 +81,11 @@ struct Counters {
     long long c_nodes, c_tris, s_nodes, s_tris;  // traversal work (profiling kernels)
     int32_t overflow_stack, overflow_queue;
     long long run_iters, run_limit;  // iterations of the current graph launch and its bound
+    // end of a frame: at or below tail_below paths in flight (0: never) the
+    // iterations stop (tail_go) and k_finish carries the rest to the end
+    int32_t tail_below, tail_go;
+    unsigned long long fetch_tail;  // k_finish's next queue entry
+    long long tail_paths;           // queue entries k_finish took
 };
 
 // Queue counts of one wavefront iteration (written by k_advance for the
@@ -98,6 +103,7 @@ constexpr int kIterHistory = 4096;
 // Per-kernel device time gathered in profiling mode.
 struct KernelTimes {
     double ms[5] = {0, 0, 0, 0, 0};  // closest, shade, shadow, regen, advance
+    double tail_ms = 0;              // k_finish
     long long launches = 0;          // every kernel the engine launched
 };
 
@@ -150,6 +156,15 @@ public:
     // results)
     void set_direct(bool direct) { direct_ = direct; }
     bool direct() const { return direct_; }
+    // paths in flight at or below which a run's remaining samples are
+    // finished by k_finish (plain jobs only; 0: the iterations run to the end)
+    void set_tail(int32_t below)
+    {
+        if ((below > 0) != (tail_below_ > 0)) drop_graphs();  // k_finish joins or leaves the graphs
+        tail_below_ = below;
+    }
+    int32_t tail() const { return tail_below_; }
+    bool tail_on() const { return tail_below_ > 0 && !cache_; }
     KernelTimes& times() { return times_; }
 
 private:
@@ -158,6 +173,8 @@ private:
     // cond: the while-loop handle whose value k_advance sets, or null when
     // the host relaunches the iteration (profiling graph, direct launches)
     void launch_iteration(int parity, cudaStream_t st, bool profile, const cudaGraphConditionalHandle* cond);
+    // k_finish and its counter update (no work unless the loop stopped for them)
+    void launch_tail(cudaStream_t st, bool profile);
 
     int64_t capacity_ = 0;
     int max_jobs_ = 0;
@@ -176,12 +193,14 @@ private:
     cudaGraphExec_t graph_ = nullptr, graph_prof_ = nullptr;
     cudaStream_t graph_stream_ = nullptr;
     cudaEvent_t ev_[2][5][2] = {};
+    cudaEvent_t ev_tail_[2] = {};
     bool profile_ = false;
     bool count_ = true;
     bool cache_ = false;
     bool direct_ = false;
     KernelTimes times_;
-    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0, grid_shade_ = 0, grid_order_ = 0;
+    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0, grid_shade_ = 0, grid_order_ = 0, grid_finish_ = 0;
+    int32_t tail_below_ = 0;
 };
 
 }  // namespace srt

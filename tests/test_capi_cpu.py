@@ -109,6 +109,7 @@ def test_batch_argument_checks_without_gpu():
     assert L.srt_film_metric_scratch_bytes(1000) >= 4000
     # path-tracer handle calls validate their arguments before any CUDA call
     assert L.srt_pt_set_launch_mode(None, S.LAUNCH_DIRECT) == 1
+    assert L.srt_pt_set_tail(None, 0) == 1
     n = C.c_int32()
     assert L.srt_pt_get_iteration_counts(None, None, 0, C.byref(n)) == 1
     assert L.srt_pt_get_pixel_samples(None, None) == 1

@@ -110,6 +110,7 @@ def test_full_frame_queue_counts_exact(cuda, frame_scene):
     sa, sc, osc = frame_scene
     p = pt_params(1, 16, 4, 1, 1, 1)
     pt = S.PathTracer(sc, W, H)
+    pt.set_tail(0)  # every iteration recorded
     film = torch.zeros((W * H, 4), dtype=torch.float32, device=cuda)
     pt.render(film, p)
     torch.cuda.synchronize()
@@ -153,3 +154,35 @@ def test_full_scene_traversal_vs_oracle_bvh(cuda, frame_scene):
     v = vis.cpu().numpy()
     assert 0.05 < np.mean(ov) < 0.95  # both outcomes occur
     assert np.all(v[safe] == ov[safe])
+
+
+def test_finishing_kernel_gives_the_same_frame(cuda, frame_scene):
+    """The end of a frame run by the finishing kernel (each remaining path
+    carried to its pixel's last sample) gives the image the wavefront
+    iterations give, bit for bit, with the same sample and ray counts; so
+    does handing it the frame after the first iteration."""
+    import torch
+    import srt_gb300 as S
+    sa, sc, osc = frame_scene
+    p = pt_params(8, 16, 4, 1, 1, 5)
+    out = {}
+    for tail in (0, S.PT_TAIL_DEFAULT, W * H):
+        pt = S.PathTracer(sc, W, H)
+        pt.set_tail(tail)
+        film = torch.zeros((W * H, 4), dtype=torch.float32, device=cuda)
+        pt.render(film, p)
+        torch.cuda.synchronize()
+        st = pt.stats()
+        out[tail] = (film.cpu().numpy(), st)
+        assert st["samples"] == W * H * 8 and st["stack_overflows"] == 0
+        assert np.all(pt.pixel_samples() == 8)
+        assert (st["tail_paths"] > 0) == (tail > 0)
+        print(f"tail {tail}: {st['iterations']} iterations, {st['tail_paths']} paths finished by one kernel")
+        pt.close()
+    f0, s0 = out[0]
+    for tail in (S.PT_TAIL_DEFAULT, W * H):
+        f, st = out[tail]
+        assert np.array_equal(f, f0), tail
+        for k in ("samples", "closest_rays", "shadow_rays"):
+            assert st[k] == s0[k], (tail, k, st[k], s0[k])
+    assert out[W * H][1]["iterations"] <= 2 < out[S.PT_TAIL_DEFAULT][1]["iterations"] < s0["iterations"]

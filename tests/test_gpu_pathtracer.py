@@ -138,6 +138,7 @@ def test_cornell_512_queue_counts_exact(cuda):
     p = pt_params(16, 8, 3, 1, 1, 1)
     sc = S.Scene(sa)
     pt = S.PathTracer(sc, w, h)
+    pt.set_tail(0)  # every iteration recorded
     film = torch.zeros((w * h, 4), dtype=torch.float32, device=cuda)
     pt.render(film, p)
     torch.cuda.synchronize()
