@@ -369,7 +369,8 @@ def mlp_eval(S, n=1920 * 1080, reps=10):
     return out
 
 
-KERNELS = ["k_closest", "k_shade", "k_shadow", "k_regen", "k_advance"]
+# the profiling slots of srt_pt_stats.kernel_ms
+KERNELS = ["k_trace", "k_shade", "k_order", "k_regen", "k_advance"]
 # queue bytes a closest-hit ray moves in k_closest (origin 16 B, direction 16 B,
 # job word 4 B in; hit record 16 B out)
 CLOSEST_QUEUE_BYTES = 52
@@ -380,22 +381,24 @@ def kernel_bytes(st, hist, npix):
     their exact counts (the iteration history: the finishing kernel's rays
     are not in it) and the queue layout (wavefront.cuh): R closest rays (H of
     them hits), Sh shadow rays, N samples ended over npix pixels.
-      k_closest (+ k_order): ray 32 B + job word 4 B in, hit 16 B out; order
-        pass 4 B in, 4 B out (BVH nodes and triangles are not included: they
-        come from ncu's DRAM bytes where the scene exceeds L2)
+      k_trace: per closest ray 32 B of ray + 4 B job word in, 16 B hit out;
+        per shadow ray 48 B in + 32 B radiance update (BVH nodes and
+        triangles are not included: they come from ncu's DRAM bytes where the
+        scene exceeds L2)
+      k_order: 4 B in, 4 B out per ray
       k_shade: order index 4 B + hit 16 B + path state 72 B in per ray; per
         hit the triangle 48 B, instance 16 B, material 80 B; per shadow ray
         the light triangle 48 B in and the shadow record 48 B out; 72 B out
-        per continuing path, 32 B per ended sample, 32 B radiance update per
-        miss
-      k_shadow: 48 B in + 32 B radiance update per ray
-      k_regen: done record 32 B + radiance 32 B + film 32 B per sample, 72 B
-        per next-sample camera ray"""
+        per continuing path and per next-sample camera ray, 8 B done record
+        and 16 B radiance record read per ended sample, 32 B radiance update
+        per miss
+      k_regen: done record 8 B + radiance 32 B + film 32 B per sample"""
     R, Hh, Sh, N = (int(hist[:, k].sum()) for k in (0, 1, 3, 4))
-    return {"k_closest": R * (CLOSEST_QUEUE_BYTES + 8),
-            "k_shade": R * 92 + Hh * 144 + Sh * 96 + (R - N) * 72 + N * 32 + (R - Hh) * 32,
-            "k_shadow": Sh * 80,
-            "k_regen": N * 96 + max(0, N - npix) * 72,
+    return {"k_trace": R * CLOSEST_QUEUE_BYTES + Sh * 80,
+            "k_shade": (R * 92 + Hh * 144 + Sh * 96 + (R - N) * 72 + N * 24 + max(0, N - npix) * 72
+                        + (R - Hh) * 32),
+            "k_order": R * 8,
+            "k_regen": N * 72,
             "k_advance": 0}
 
 
@@ -721,12 +724,15 @@ def profile_case(which="spheres"):
     pt.render(film, S.pt_params(1, 2, RR_DEPTH, 1, 1, 0))
     torch.cuda.synchronize()
     a = pt.stats()
+    ha = pt.iteration_counts()
     pt.render(film, S.pt_params(1, MAX_DEPTH, RR_DEPTH, 1, 1, 1))
     torch.cuda.synchronize()
     b = pt.stats()
     print(json.dumps({"profile_case": "1920x1080x1spp",
                       "frame_a": {"max_depth": 2, "camera_rays": W * H,
-                                  "bounce_rays": a["closest_rays"] - W * H, "shadow_rays": a["shadow_rays"]},
+                                  "bounce_rays": a["closest_rays"] - W * H, "shadow_rays": a["shadow_rays"],
+                                  # the second k_trace launch: iteration 0's shadow rays and iteration 1's rays
+                                  "k_trace_launch_2": {"shadow_rays": int(ha[0, 3]), "closest_rays": int(ha[1, 0])}},
                       "frame_b": {"max_depth": MAX_DEPTH, "closest_rays": b["closest_rays"],
                                   "shadow_rays": b["shadow_rays"], "iterations": b["iterations"]}}))
 
@@ -832,18 +838,17 @@ def main():
     kms = dict(zip(KERNELS, st_t["kernel_ms"]))
     top = max(kms, key=kms.get)
     iters = max(1, st["iterations"])
-    # the traversal counters include the finishing kernel's rays: scale them
-    # to the rays of the wavefront iterations (whose launches are timed here)
-    if top == "k_shadow":
-        all_rays, nodes, tris, per_ray = st["shadow_rays"], st["shadow_nodes"], st["shadow_tris"], 44
-        rays = int(hist[:, 3].sum())
-        queue = 48
-    else:
-        all_rays, nodes, tris, per_ray = st["closest_rays"], st["closest_nodes"], st["closest_tris"], 40
-        rays = int(hist[:, 0].sum())
-        queue = CLOSEST_QUEUE_BYTES
-    wave = rays / max(all_rays, 1)
-    nodes, tris = nodes * wave, tris * wave
+    # k_trace traces both kinds of ray; the traversal counters include the
+    # finishing kernel's rays: scale them to the rays of the wavefront
+    # iterations (whose launches are timed here)
+    rc, rs = int(hist[:, 0].sum()), int(hist[:, 3].sum())
+    wc = rc / max(st["closest_rays"], 1)
+    ws = rs / max(st["shadow_rays"], 1)
+    rays = rc + rs
+    nodes = st["closest_nodes"] * wc + st["shadow_nodes"] * ws
+    tris = st["closest_tris"] * wc + st["shadow_tris"] * ws
+    per_ray = (rc * 40 + rs * 44) / max(rays, 1)  # ray and hit (closest), ray and tmax (shadow)
+    queue = (rc * CLOSEST_QUEUE_BYTES + rs * 80) / max(rays, 1)
     peak, peak_kind = peaks()
     # algorithmic bytes per ray (the scope table): the ray and its hit
     # (per_ray) plus the BVH traffic ncu measured in DRAM per ray (its DRAM
@@ -867,7 +872,8 @@ def main():
     l2_gbs = logical / iters / (launch_ms / 1e3) / 1e9
     roof["l2_level"] = {"alg_bytes_per_launch": int(logical / iters), "achieved": round(l2_gbs, 1),
                         "frac_of_hbm_peak": round(l2_gbs / peak, 4),
-                        "nodes_per_ray": round(nodes / max(rays, 1), 2), "tris_per_ray": round(tris / max(rays, 1), 2),
+                        "nodes_per_ray": round(st["closest_nodes"] / max(st["closest_rays"], 1), 2),
+                        "tris_per_ray": round(st["closest_tris"] / max(st["closest_rays"], 1), 2),
                         "shadow_nodes_per_ray": round(st["shadow_nodes"] / max(st["shadow_rays"], 1), 2),
                         "shadow_tris_per_ray": round(st["shadow_tris"] / max(st["shadow_rays"], 1), 2)}
 

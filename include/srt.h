@@ -255,15 +255,19 @@ typedef struct srt_pt_stats {
     float render_ms;             /* wall time of srt_pt_render (host clock)      */
     int64_t kernel_launches;     /* kernels this library launched for the frame  */
     /* Filled only while profiling is on (srt_pt_set_profiling): summed device
-     * time of each kernel of the iteration (closest, shade, shadow, regen,
-     * advance) from CUDA events recorded between them, and the traversal
-     * work: 128-byte nodes visited and triangles tested. */
+     * time of each kernel of the iteration from CUDA events recorded between
+     * them -- [0] the traversal (the previous iteration's shadow rays and this
+     * iteration's closest-hit rays), [1] shading, [2] the shading order,
+     * [3] film accumulation, [4] the iteration's end -- and the traversal
+     * work: 128-byte nodes visited and triangles tested, for closest-hit and
+     * for shadow rays. */
     float kernel_ms[5];
     int64_t closest_nodes, closest_tris, shadow_nodes, shadow_tris;
     /* End of the frame (srt_pt_set_tail): paths the finishing kernel took
-     * from the queue, each carried to its pixel's last sample, and that
-     * kernel's device time (profiling only).  Rays it traced are in
-     * closest_rays / shadow_rays; `iterations` counts the wavefront
+     * from the queue, each carried to its pixel's last sample, and the device
+     * time after the iterations (profiling only: the last iteration's shadow
+     * rays and ended samples, then the finishing kernel).  Rays it traced are
+     * in closest_rays / shadow_rays; `iterations` counts the wavefront
      * iterations before it. */
     int64_t tail_paths;
     float tail_ms;

@@ -49,8 +49,9 @@ struct RayPre {
     float3 idir;
     float sx, sy, sz;
     // packed: kx (bits 0-1), ky (2-3), kz (4-5) of the watertight test's axis
-    // permutation, octant (8-10), child visiting order (11-13: the octant for
-    // near-to-far, its complement for far-to-near); one register instead of five
+    // permutation, any-hit ray (7: see trav_advance_impl), octant (8-10), child
+    // visiting order (11-13: the octant for near-to-far, its complement for
+    // far-to-near); one register instead of six
     uint32_t axes;
     __device__ __forceinline__ int kx() const { return (int)(axes & 3u); }
     __device__ __forceinline__ int ky() const { return (int)((axes >> 2) & 3u); }
@@ -422,11 +423,13 @@ __device__ __forceinline__ float2 hit_barycentrics(const TravState& s)
 }
 
 // Advances one ray; returns true when its traversal is complete (for any-hit
-// rays: on the first hit, with s.tri set).
-template <bool kAny, bool kCount>
-__device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overflow, TraceCount& cnt)
+// rays: on the first hit, with s.tri set).  `any` is a constant where the
+// kind of ray is fixed (trav_advance) and read from the ray where a kernel
+// traces both kinds (bit 7 of its axes word, set by mark_any_hit).
+template <bool kCount>
+__device__ __forceinline__ bool trav_advance_impl(TravState& s, Stack& st, int& overflow, TraceCount& cnt, bool any)
 {
-    for (int it = 0; it < (kAny ? kShadowStepBudget : kStepBudget); ++it) {
+    for (int it = 0; it < (any ? kShadowStepBudget : kStepBudget); ++it) {
         while (s.tmask) {
             uint32_t b = __ffs(s.tmask) - 1;
             s.tmask &= s.tmask - 1;
@@ -436,7 +439,7 @@ __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overf
             float t, u, v;
             if (hit_triangle(s.r, f3(a), f3(bb), f3(c), s.tmin, s.tmax, t, u, v)) {
                 s.tri = (int32_t)ti;
-                if (kAny) return true;
+                if (any) return true;
                 s.tmax = t;
             }
         }
@@ -454,14 +457,29 @@ __device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overf
     }
     return false;
 }
+template <bool kAny, bool kCount>
+__device__ __forceinline__ bool trav_advance(TravState& s, Stack& st, int& overflow, TraceCount& cnt)
+{
+    return trav_advance_impl<kCount>(s, st, overflow, cnt, kAny);
+}
+// a ray of a mixed kernel: any-hit (shadow) or closest-hit, by bit 7 of its axes
+__device__ __forceinline__ void mark_any_hit(TravState& s) { s.r.axes |= 1u << 7; }
+__device__ __forceinline__ bool is_any_hit(const TravState& s) { return (s.r.axes >> 7) & 1u; }
+template <bool kCount>
+__device__ __forceinline__ bool trav_advance_mixed(TravState& s, Stack& st, int& overflow, TraceCount& cnt,
+                                                   TraceCount& scnt)
+{
+    const bool any = is_any_hit(s);
+    return trav_advance_impl<kCount>(s, st, overflow, any ? scnt : cnt, any);
+}
 
 // Drives a warp over rays [0, n) taken from *fetch.  load(i, state, stack)
 // starts ray i (calls trav_init); store(i, state, fin) is called by all 32
 // lanes after every round (so it may use warp-wide votes and appends), with
 // fin set in the lanes whose ray i just finished.
-template <bool kAny, bool kCount, class Load, class Store>
-__device__ __forceinline__ void trace_persistent(int64_t n, unsigned long long* fetch, Stack& st, int& overflow,
-                                                 TraceCount& cnt, Load load, Store store)
+template <class Advance, class Load, class Store>
+__device__ __forceinline__ void trace_persistent_with(int64_t n, unsigned long long* fetch, Stack& st, Advance advance,
+                                                      Load load, Store store)
 {
     const uint32_t full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -489,10 +507,18 @@ __device__ __forceinline__ void trace_persistent(int64_t n, unsigned long long* 
             idle = __ballot_sync(full, ray < 0);
         }
         if (idle == full && drained) break;
-        const bool fin = ray >= 0 && trav_advance<kAny, kCount>(s, st, overflow, cnt);
+        const bool fin = ray >= 0 && advance(s, st);
         store(ray, s, fin);
         if (fin) ray = -1;
     }
+}
+template <bool kAny, bool kCount, class Load, class Store>
+__device__ __forceinline__ void trace_persistent(int64_t n, unsigned long long* fetch, Stack& st, int& overflow,
+                                                 TraceCount& cnt, Load load, Store store)
+{
+    trace_persistent_with(
+        n, fetch, st, [&](TravState& s, Stack& stk) { return trav_advance<kAny, kCount>(s, stk, overflow, cnt); },
+        load, store);
 }
 
 // Any hit in (tmin, tmax): true when occluded.

@@ -1,14 +1,19 @@
 // wavefront.cu — kernels and host driver of the streaming wavefront tracer.
 //
 //   k_start    raygen for every pixel of a newly admitted job (SoA queue)
-//   k_closest  closest-hit traversal of the current queue -> hit records
+//   k_trace    one persistent traversal over the previous iteration's shadow
+//              rays (any hit; unoccluded contributions added to the pixel)
+//              and the current queue's closest-hit rays (-> hit records)
+//   k_regen    the previous iteration's ended samples: NaN/Inf filter, film
+//              accumulation
 //   k_order    shading order: the queue's hits first, then its misses
 //   k_shade    miss / emitter-hit MIS / NEE + MIS / BSDF sample / Russian
-//              roulette; survivors compacted into the next queue with one
+//              roulette; survivors, and the next sample's camera ray of a
+//              path that ended, compacted into the next queue with one
 //              atomic per warp; NEE rays into the shadow queue
-//   k_shadow   any-hit traversal; unoccluded contributions added to the pixel
-//   k_regen    NaN/Inf sample filter, film accumulation, next-sample raygen
 //   k_advance  one thread: swaps the queue counters, keeps statistics
+//   k_finish   the end of a frame (few paths left): each thread carries a
+//              path and its pixel's later samples to the end
 //
 // The per-path arithmetic follows the megakernel raygen program
 // src/shader/integrator/path_tracer.cu:50-169 statement by statement.
@@ -135,33 +140,66 @@ __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ j
     }
 }
 
+// The iteration's traversal: the shadow rays the previous iteration's
+// k_shade cast (any hit, far-to-near) and this iteration's closest-hit rays,
+// one persistent launch over both (entries [0, n_sp) of the shadow queue,
+// then [0, n_cur) of the path queue).  Between the two kinds a frame pays
+// one kernel drain per iteration instead of two.  An unoccluded shadow ray
+// adds its contribution to its pixel's radiance, before k_regen adds an
+// ended sample to the film and before k_shade adds the pixel's next emitted
+// radiance, the order of the reference's per-pixel loop (path_tracer.cu:
+// 113-142 then 88-106 of the next segment).  shadows_only: the flush after
+// the last iteration.
 template <bool kCount>
-__global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_closest(const JobRec* __restrict__ jobs, PathQueue q,
-                                                              float4* __restrict__ hits, Counters* ctr,
-                                                              int64_t capacity)
+__global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace(const JobRec* __restrict__ jobs, PathQueue q,
+                                                                              ShadowQueue sq, float4* __restrict__ hits,
+                                                                              Counters* ctr, int64_t capacity,
+                                                                              int shadows_only)
 {
-    // a counter past the capacity (overflow, reported by the host) never indexes past the queue
-    const int64_t n = min((int64_t)ctr->n_cur, capacity);
+    // a counter past the capacity (overflow, reported by the host) never indexes past a queue
+    const int64_t ns = min((int64_t)ctr->n_sp, capacity);
+    const int64_t nc = shadows_only ? 0 : min((int64_t)ctr->n_cur, capacity);
     int overflow = 0;
-    TraceCount cnt;
+    TraceCount cnt, scnt;
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
     Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
-    trace_persistent<false, kCount>(
-        n, &ctr->fetch_closest, st, overflow, cnt,
+    trace_persistent_with(
+        ns + nc, &ctr->fetch_closest, st,
+        [&](TravState& s, Stack& stk) { return trav_advance_mixed<kCount>(s, stk, overflow, cnt, scnt); },
         [&](int64_t i, TravState& s, Stack& stk) {
-            float4 o = q.o[i], d = q.d[i];
-            const SceneView& S = jobs[__float_as_uint(q.beta[i].w) >> 16].scene;
-            trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, 1e16f, stk);
+            if (i < ns) {
+                const float4 o = sq.o[i], d = sq.d[i];
+                const SceneView& S = jobs[__float_as_int(sq.c[i].w)].scene;
+                trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, d.w, stk, SRT_SHADOW_FAR_FIRST != 0);
+                mark_any_hit(s);
+            } else {
+                const int64_t j = i - ns;
+                const float4 o = q.o[j], d = q.d[j];
+                const SceneView& S = jobs[__float_as_uint(q.beta[j].w) >> 16].scene;
+                trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, 1e16f, stk);
+            }
         },
         [&](int64_t i, const TravState& s, bool fin) {
             if (!fin) return;
-            const float2 uv = hit_barycentrics(s);
-            hits[i] = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
+            if (i < ns) {
+                if (s.tri < 0) {
+                    // unoccluded; one path per pixel in flight: plain read-modify-write
+                    const float4 o = sq.o[i], c = sq.c[i];
+                    float4* lp = jobs[__float_as_int(c.w)].lpath + __float_as_int(o.w);
+                    const float4 l = *lp;
+                    *lp = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+                }
+            } else {
+                const float2 uv = hit_barycentrics(s);
+                hits[i - ns] = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
+            }
         });
     if (overflow) atomicAdd(&ctr->overflow_stack, 1);
-    if (kCount && (cnt.nodes | cnt.tris)) {
+    if (kCount && (cnt.nodes | cnt.tris | scnt.nodes | scnt.tris)) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_nodes), (unsigned long long)cnt.nodes);
         atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->c_tris), (unsigned long long)cnt.tris);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_nodes), (unsigned long long)scnt.nodes);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_tris), (unsigned long long)scnt.tris);
     }
 }
 
@@ -429,6 +467,25 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
             float4 l = *lp;
             *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, l.w);
         }
+        // a path that ended starts its pixel's next sample (path_tracer.cu:64-68):
+        // the camera ray continues the pixel's curand stream where shading left it
+        const bool fin = valid && terminate;
+        if (fin) {
+            const JobRec& J = jobs[job];
+            if (__float_as_int(J.lpath[pix].w) + 1 < J.spp) {
+                Rng rng;
+                rng.load(ra, rb);
+                const int ix = pix % J.width, iy = pix / J.width;
+                const float xx = ((float)ix + rng.next()) / (float)J.width;
+                const float yy = ((float)iy + rng.next()) / (float)J.height;
+                camera_ray(J.cam, xx, yy, ro, rd);
+                rng.store(ra, rb);
+                beta = f3(1.0f);
+                pdf_next = 1.0f;
+                flags = pack_flags(0, true, job);
+                push_next = true;
+            }
+        }
         int32_t slot = warp_append(&ctr->n_next, push_next);
         if (push_next) {
             if (slot < capacity) {
@@ -451,12 +508,10 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                 atomicAdd(&ctr->overflow_queue, 1);
             }
         }
-        bool fin = valid && terminate;
         slot = warp_append(&ctr->n_done, fin);
         if (fin) {
             if (slot < capacity) {
-                done.rec[2 * (size_t)slot] = ra;
-                done.rec[2 * (size_t)slot + 1] = make_uint4((uint32_t)job, (uint32_t)pix, rb.x, rb.y);
+                done.rec[slot] = make_uint2((uint32_t)job, (uint32_t)pix);
             } else {
                 atomicAdd(&ctr->overflow_queue, 1);
             }
@@ -464,58 +519,23 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
     }
 }
 
-template <bool kCount>
-__global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_shadow(const JobRec* __restrict__ jobs, ShadowQueue sq,
-                                                             Counters* ctr, int64_t capacity)
+// Ends the samples that ended in the previous iteration (path_tracer.cu:
+// 164-165), after k_trace has traced their last shadow rays: the film takes
+// each sample's radiance once every contribution to it is in (its last
+// shadow ray, a radiance-cache query); the pixel's next sample was started
+// by k_shade.
+__global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ jobs, DoneQueue done, Counters* ctr,
+                                                    int64_t capacity)
 {
-    const int64_t n = min((int64_t)ctr->n_shadow, capacity);
-    int overflow = 0;
-    TraceCount cnt;
-    __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
-    Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
-    trace_persistent<true, kCount>(
-        n, &ctr->fetch_shadow, st, overflow, cnt,
-        [&](int64_t i, TravState& s, Stack& stk) {
-            float4 o = sq.o[i], d = sq.d[i];
-            const SceneView& S = jobs[__float_as_int(sq.c[i].w)].scene;
-            trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, d.w, stk, SRT_SHADOW_FAR_FIRST != 0);
-        },
-        [&](int64_t i, const TravState& s, bool fin) {
-            if (fin && s.tri < 0) {
-                // unoccluded; one path per pixel in flight: plain read-modify-write
-                float4 o = sq.o[i], c = sq.c[i];
-                float4* lp = jobs[__float_as_int(c.w)].lpath + __float_as_int(o.w);
-                float4 l = *lp;
-                *lp = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
-            }
-        });
-    if (overflow) atomicAdd(&ctr->overflow_stack, 1);
-    if (kCount && (cnt.nodes | cnt.tris)) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_nodes), (unsigned long long)cnt.nodes);
-        atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->s_tris), (unsigned long long)cnt.tris);
-    }
-}
-
-// Ends the samples of the done pixels (path_tracer.cu:164-165) and starts
-// their next sample (path_tracer.cu:64-68).
-__global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ jobs, DoneQueue done,
-                                                    PathQueue qn, Counters* ctr, int64_t capacity)
-{
-    const int n = (int)min((int64_t)ctr->n_done, capacity);
+    const int n = (int)min((int64_t)ctr->n_dp, capacity);
     const int stride = gridDim.x * blockDim.x;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
         const int i = base + (threadIdx.x & 31);
-        bool again = false;
-        int job = 0, pix = 0;
-        float3 o = f3(0.0f), d = f3(0.0f);
-        uint4 ra = make_uint4(0, 0, 0, 0);
-        uint2 rb = make_uint2(0, 0);
         int32_t* frame_ctr = nullptr;  // progressive-frame counter of the finished sample
         int32_t* pixel_ctr = nullptr;  // finished-pixel counter, when the pixel's last sample ended
         if (i < n) {
-            const uint4 e = done.rec[2 * (size_t)i + 1];
-            job = (int)e.x;
-            pix = (int)e.y;
+            const uint2 e = done.rec[i];
+            const int job = (int)e.x, pix = (int)e.y;
             const JobRec& J = jobs[job];
             float4 l = J.lpath[pix];
             const int spp_done = __float_as_int(l.w);
@@ -545,34 +565,11 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
             const int k = spp_done + 1;
             J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(k));
             if (J.frame_done) frame_ctr = J.frame_done + (k - 1);
-            if (k < J.spp) {
-                Rng rng;
-                rng.load(done.rec[2 * (size_t)i], make_uint2(e.z, e.w));
-                int ix = pix % J.width, iy = pix / J.width;
-                float xx = ((float)ix + rng.next()) / (float)J.width;
-                float yy = ((float)iy + rng.next()) / (float)J.height;
-                camera_ray(J.cam, xx, yy, o, d);
-                rng.store(ra, rb);
-                again = true;
-            } else {
-                pixel_ctr = J.pixels_done;
-            }
+            if (k >= J.spp) pixel_ctr = J.pixels_done;
         }
         // progress counters: one atomic per distinct counter in the warp
         warp_count(frame_ctr);
         warp_count(pixel_ctr);
-        int32_t slot = warp_append(&ctr->n_next, again);
-        if (again) {
-            if (slot < capacity) {
-                qn.o[slot] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
-                qn.d[slot] = make_float4(d.x, d.y, d.z, 1.0f);
-                qn.beta[slot] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pack_flags(0, true, job)));
-                qn.ra[slot] = ra;
-                qn.rb[slot] = rb;
-            } else {
-                atomicAdd(&ctr->overflow_queue, 1);
-            }
-        }
     }
 }
 
@@ -582,9 +579,9 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
 // iterations carries about 2 % of its rays.  Once k_advance finds at most
 // tail_below paths in flight, each thread here takes one queue entry and
 // carries that path, and its pixel's later samples, to the pixel's last
-// sample: closest hit as k_closest, shade_vertex as k_shade, the shadow ray
-// as k_shadow, the next sample as k_regen, in the same order on the same
-// values, so every pixel ends with the value the iterations would give.
+// sample: closest hit and shadow ray as k_trace, shade_vertex as k_shade,
+// the film and the next sample as k_regen and k_shade, in the same order on
+// the same values, so every pixel ends with the value the iterations give.
 // Plain jobs only (no radiance-cache work).
 constexpr int kFinishThreads = kTraceThreads;
 
@@ -607,7 +604,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish(const JobRec* __restr
         uint4 ra = q.ra[i];
         uint2 rb = q.rb[i];
         for (;;) {
-            // closest hit (k_closest)
+            // closest hit (k_trace)
             TravState s;
             {
                 const SceneView& S = jobs[__float_as_uint(b4.w) >> 16].scene;
@@ -634,7 +631,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish(const JobRec* __restr
                 const float4 l = *lp;
                 *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, l.w);
             }
-            // shadow ray (k_shadow)
+            // shadow ray (k_trace)
             if (push_shadow) {
                 ++shadow;
                 trav_init(s, J.scene.nodes, J.scene.tris, sh_o, sh_d, 1e-3f, sh_t, st, SRT_SHADOW_FAR_FIRST != 0);
@@ -651,7 +648,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish(const JobRec* __restr
                 b4 = make_float4(beta.x, beta.y, beta.z, __uint_as_float(flags));
                 continue;
             }
-            // the sample ends and the pixel's next one starts (k_regen)
+            // the sample ends (k_regen) and the pixel's next one starts (k_shade)
             ++ended;
             const float4 l = *lp;
             if (isfinite(l.x) && isfinite(l.y) && isfinite(l.z)) {
@@ -699,6 +696,15 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish(const JobRec* __restr
     }
 }
 
+// After the flush (k_trace over the pending shadow rays, k_regen over the
+// pending ended samples): nothing pending.
+__global__ void k_end_flush(Counters* c)
+{
+    c->n_sp = 0;
+    c->n_dp = 0;
+    c->fetch_closest = 0;
+}
+
 // After k_finish: nothing is left in flight.
 __global__ void k_end_tail(Counters* c)
 {
@@ -734,6 +740,8 @@ __global__ void k_advance(Counters* c, IterCount* history, const JobRec* __restr
     c->shadow_total += c->n_shadow;
     c->iterations += 1;
     c->started += c->n_done;
+    c->n_sp = c->n_shadow;  // traced by the next k_trace
+    c->n_dp = c->n_done;    // added to the film by the next k_regen
     c->n_cur = c->n_next;
     c->n_next = 0;
     c->n_shadow = 0;
@@ -820,7 +828,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
         sq_.c = (float4*)take(C * 16);
         hits_ = (float4*)take(C * 16);
         order_ = (int32_t*)take(C * 4);
-        done_.rec = (uint4*)take(C * 32);
+        done_.rec = (uint2*)take(C * 8);
         counters_ = (Counters*)take(sizeof(Counters));
         history_ = (IterCount*)take(sizeof(IterCount) * kIterHistory);
         jobs_ = (JobRec*)take(sizeof(JobRec) * max_jobs);
@@ -844,8 +852,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
             nb = SRT_TRACE_MIN_BLOCKS;
         return sms * nb;
     };
-    grid_closest_ = resident(reinterpret_cast<const void*>(k_closest<false>));
-    grid_shadow_ = resident(reinterpret_cast<const void*>(k_shadow<false>));
+    grid_trace_ = resident(reinterpret_cast<const void*>(k_trace<false>));
     grid_finish_ = resident(reinterpret_cast<const void*>(k_finish<false>));
     grid_stride_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kThreads - 1) / kThreads, sms * 8));
     grid_order_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kOrderThreads - 1) / kOrderThreads, sms * 8));
@@ -890,11 +897,16 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     };
     mark(0, 0);
     if (prof && count_)
-        k_closest<true><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+        k_trace<true><<<grid_trace_, kTraceThreads, 0, st>>>(jobs_, cur, sq_, hits_, counters_, capacity_, 0);
     else
-        k_closest<false><<<grid_closest_, kTraceThreads, 0, st>>>(jobs_, cur, hits_, counters_, capacity_);
+        k_trace<false><<<grid_trace_, kTraceThreads, 0, st>>>(jobs_, cur, sq_, hits_, counters_, capacity_, 0);
+    mark(0, 1);
+    mark(3, 0);
+    k_regen<<<grid_stride_, kThreads, 0, st>>>(jobs_, done_, counters_, capacity_);
+    mark(3, 1);
+    mark(2, 0);
     k_order<<<grid_order_, kOrderThreads, 0, st>>>(hits_, order_, counters_, capacity_);
-    mark(0, 1);  // the closest-hit time includes the shading-order pass
+    mark(2, 1);
     mark(1, 0);
     if (cache_)
         k_shade<true><<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,
@@ -902,17 +914,8 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     else
         k_shade<false><<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,
                                                               capacity_);
-    mark(1, 1);
-    mark(2, 0);
-    if (prof && count_)
-        k_shadow<true><<<grid_shadow_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
-    else
-        k_shadow<false><<<grid_shadow_, kTraceThreads, 0, st>>>(jobs_, sq_, counters_, capacity_);
-    mark(2, 1);
     if (cache_) launch_cache_queries(jobs_, max_jobs_, st);
-    mark(3, 0);
-    k_regen<<<grid_stride_, kThreads, 0, st>>>(jobs_, done_, nxt, counters_, capacity_);
-    mark(3, 1);
+    mark(1, 1);
     mark(4, 0);
     if (cond)
         k_advance<true><<<1, 1, 0, st>>>(counters_, history_, jobs_, max_jobs_, *cond);
@@ -921,7 +924,7 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     mark(4, 1);
 }
 
-void Engine::launch_tail(cudaStream_t st, bool prof)
+void Engine::launch_post(cudaStream_t st, bool prof)
 {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (prof) cudaStreamIsCapturing(st, &cs);
@@ -933,11 +936,20 @@ void Engine::launch_tail(cudaStream_t st, bool prof)
             cudaEventRecord(ev_tail_[e], st);
     };
     mark(0);
+    // the last iteration's shadow rays and ended samples
     if (prof && count_)
-        k_finish<true><<<grid_finish_, kFinishThreads, 0, st>>>(jobs_, q_[0], counters_, capacity_);
+        k_trace<true><<<grid_trace_, kTraceThreads, 0, st>>>(jobs_, q_[0], sq_, hits_, counters_, capacity_, 1);
     else
-        k_finish<false><<<grid_finish_, kFinishThreads, 0, st>>>(jobs_, q_[0], counters_, capacity_);
-    k_end_tail<<<1, 1, 0, st>>>(counters_);
+        k_trace<false><<<grid_trace_, kTraceThreads, 0, st>>>(jobs_, q_[0], sq_, hits_, counters_, capacity_, 1);
+    k_regen<<<grid_stride_, kThreads, 0, st>>>(jobs_, done_, counters_, capacity_);
+    k_end_flush<<<1, 1, 0, st>>>(counters_);
+    if (tail_on()) {
+        if (prof && count_)
+            k_finish<true><<<grid_finish_, kFinishThreads, 0, st>>>(jobs_, q_[0], counters_, capacity_);
+        else
+            k_finish<false><<<grid_finish_, kFinishThreads, 0, st>>>(jobs_, q_[0], counters_, capacity_);
+        k_end_tail<<<1, 1, 0, st>>>(counters_);
+    }
     mark(1);
 }
 
@@ -957,7 +969,6 @@ srt_status Engine::capture(bool prof)
         SRT_CUDA_TRY(cudaStreamBeginCapture(graph_stream_, cudaStreamCaptureModeThreadLocal));
         launch_iteration(0, graph_stream_, true, nullptr);
         launch_iteration(1, graph_stream_, true, nullptr);
-        if (tail_on()) launch_tail(graph_stream_, true);
         e = cudaStreamEndCapture(graph_stream_, &g);
         if (e != cudaSuccess) return cuda_error(e, "capture wavefront iteration");
     } else {
@@ -982,11 +993,12 @@ srt_status Engine::capture(bool prof)
             launch_iteration(1, graph_stream_, false, &cond);
             e = cudaStreamEndCapture(graph_stream_, &body);
         }
-        // after the loop: the end of the frame, when the loop stopped for it
-        if (e == cudaSuccess && tail_on()) {
+        // after the loop: the last iteration's shadow rays and ended samples,
+        // then the end of the frame when the loop stopped for it
+        if (e == cudaSuccess) {
             e = cudaStreamBeginCaptureToGraph(graph_stream_, g, &node, nullptr, 1, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                launch_tail(graph_stream_, false);
+                launch_post(graph_stream_, false);
                 cudaGraph_t same = g;
                 e = cudaStreamEndCapture(graph_stream_, &same);
             }
@@ -1080,7 +1092,7 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         if (e == cudaSuccess) {
             const Counters& c = *host_counters_;
             iters = c.run_iters;
-            times_.launches += 1 + iters * (cache_ ? 7 : 6) + (tail_on() ? 2 : 0);
+            times_.launches += 1 + iters * (cache_ ? 6 : 5) + 3 + (tail_on() ? 2 : 0);
             if (c.overflow_queue)
                 status = set_error(SRT_ERR_ARG, "wavefront queue capacity exceeded");
             else if (c.overflow_stack)
@@ -1090,13 +1102,20 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
         }
     }
     int per_check = 2;
-    long long tail_seen = 0;
     if ((prof || no_graph) && e == cudaSuccess) {
         what = "start host loop";
         k_begin_run<<<1, 1, 0, graph_stream_>>>(counters_, 1LL << 40, tail_on() ? tail_below_ : 0);
         e = cudaGetLastError();
         times_.launches += 1;
     }
+    auto read_counters_now = [&]() {
+        what = "copy counters";
+        e = cudaMemcpyAsync(host_counters_, counters_, sizeof(Counters), cudaMemcpyDeviceToHost, graph_stream_);
+        if (e == cudaSuccess) {
+            what = "synchronize iteration graph";
+            e = cudaStreamSynchronize(graph_stream_);
+        }
+    };
     while ((prof || no_graph) && e == cudaSuccess) {
         if (prof) per_check = 1;  // events are re-recorded by every launch: read them each time
         what = "cudaGraphLaunch";
@@ -1105,21 +1124,15 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
                 what = "direct iteration launch";
                 launch_iteration(0, graph_stream_, prof, nullptr);
                 launch_iteration(1, graph_stream_, prof, nullptr);
-                if (tail_on()) launch_tail(graph_stream_, prof);
                 e = cudaGetLastError();
             } else {
                 e = cudaGraphLaunch(graph, graph_stream_);
             }
             iters += 2;
-            times_.launches += 2 * (cache_ ? 7 : 6) + (tail_on() ? 2 : 0);
+            times_.launches += 2 * (cache_ ? 6 : 5);
         }
         if (e != cudaSuccess) break;
-        what = "copy counters";
-        e = cudaMemcpyAsync(host_counters_, counters_, sizeof(Counters), cudaMemcpyDeviceToHost, graph_stream_);
-        if (e == cudaSuccess) {
-            what = "synchronize iteration graph";
-            e = cudaStreamSynchronize(graph_stream_);
-        }
+        read_counters_now();
         if (e != cudaSuccess) break;
         if (prof) {
             what = "cudaEventElapsedTime";
@@ -1129,13 +1142,6 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
                     e = cudaEventElapsedTime(&ms, ev_[par][k][0], ev_[par][k][1]);
                     times_.ms[k] += ms;
                 }
-            if (e == cudaSuccess && tail_on() && host_counters_->tail_paths != tail_seen) {
-                // only the check whose pair ended in k_finish: elsewhere it returned at once
-                float ms = 0.0f;
-                e = cudaEventElapsedTime(&ms, ev_tail_[0], ev_tail_[1]);
-                times_.tail_ms += ms;
-                tail_seen = host_counters_->tail_paths;
-            }
             if (e != cudaSuccess) break;
         }
         const Counters& c = *host_counters_;
@@ -1147,10 +1153,23 @@ srt_status Engine::run(cudaStream_t st, long long max_iters, bool until_idle, lo
             status = set_error(SRT_ERR_STACK, "traversal stack overflow");
             break;
         }
-        if (c.n_cur == 0) break;  // nothing in flight: only a new job can add work
-        if (budget_iters > 0 && iters >= budget_iters) break;
-        if (max_iters > 0 && iters > max_iters) {
-            status = set_error(SRT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+        // stop: nothing in flight (only a new job can add work), the end of
+        // the frame for k_finish, the step's budget, or the bound
+        const bool over = max_iters > 0 && iters > max_iters;
+        if (c.n_cur == 0 || c.tail_go || (budget_iters > 0 && iters >= budget_iters) || over) {
+            what = "flush and end of frame";
+            launch_post(graph_stream_, prof);
+            e = cudaGetLastError();
+            times_.launches += 3 + (tail_on() ? 2 : 0);
+            if (e == cudaSuccess) read_counters_now();
+            if (e == cudaSuccess && prof) {
+                what = "cudaEventElapsedTime";
+                float ms = 0.0f;
+                e = cudaEventElapsedTime(&ms, ev_tail_[0], ev_tail_[1]);
+                times_.tail_ms += ms;
+            }
+            if (e == cudaSuccess && over && budget_iters <= 0 && host_counters_->n_cur > 0)
+                status = set_error(SRT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
             break;
         }
         per_check = std::min(per_check * 2, 16);

@@ -60,11 +60,10 @@ struct PathQueue {
     uint2* rb;
 };
 
-// A path that ended in this iteration: its pixel's RNG state travels with it
-// from k_shade to k_regen (stored as two 16-byte words: ra, then job, pixel,
-// rb.x, rb.y).
+// A sample that ended in this iteration: its job and pixel, from k_shade to
+// k_regen, which adds it to the film.
 struct DoneQueue {
-    uint4* rec;  // 2 per entry
+    uint2* rec;  // job, pixel
 };
 
 struct ShadowQueue {
@@ -75,6 +74,9 @@ struct ShadowQueue {
 
 struct Counters {
     int32_t n_cur, n_next, n_shadow, n_done;
+    // the previous iteration's shadow rays and ended samples, which this
+    // iteration's k_trace and k_regen take
+    int32_t n_sp, n_dp;
     int32_t n_hit, n_miss;  // closest-hit results of the iteration, by kind
     unsigned long long fetch_closest, fetch_shadow;
     long long closest_total, shadow_total, iterations, started;
@@ -173,8 +175,10 @@ private:
     // cond: the while-loop handle whose value k_advance sets, or null when
     // the host relaunches the iteration (profiling graph, direct launches)
     void launch_iteration(int parity, cudaStream_t st, bool profile, const cudaGraphConditionalHandle* cond);
-    // k_finish and its counter update (no work unless the loop stopped for them)
-    void launch_tail(cudaStream_t st, bool profile);
+    // after the loop: the flush of the last iteration's shadow rays and ended
+    // samples, then k_finish and its counter update (no work unless the loop
+    // stopped for it)
+    void launch_post(cudaStream_t st, bool profile);
 
     int64_t capacity_ = 0;
     int max_jobs_ = 0;
@@ -199,7 +203,7 @@ private:
     bool cache_ = false;
     bool direct_ = false;
     KernelTimes times_;
-    int grid_closest_ = 0, grid_shadow_ = 0, grid_stride_ = 0, grid_shade_ = 0, grid_order_ = 0, grid_finish_ = 0;
+    int grid_trace_ = 0, grid_stride_ = 0, grid_shade_ = 0, grid_order_ = 0, grid_finish_ = 0;
     int32_t tail_below_ = 0;
 };
 
