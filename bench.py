@@ -371,7 +371,7 @@ def mlp_eval(S, n=1920 * 1080, reps=10):
 
 # the profiling slots of srt_pt_stats.kernel_ms
 KERNELS = ["k_trace", "k_shade", "k_order", "k_regen", "k_advance"]
-# queue bytes a closest-hit ray moves in k_closest (origin 16 B, direction 16 B,
+# queue bytes a closest-hit ray moves in k_trace (origin 16 B, direction 16 B,
 # job word 4 B in; hit record 16 B out)
 CLOSEST_QUEUE_BYTES = 52
 
@@ -859,10 +859,12 @@ def main():
     roof = {"bound": "hbm", "kernel": top, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "launches": iters, "per_launch_ms": round(launch_ms, 4)}
     if rec:
-        alg_per_ray = per_ray + max(0.0, rec["dram_bytes_per_ray"] - queue)
+        # BVH bytes per ray measured in DRAM (the capture's DRAM bytes less its queue traffic)
+        bvh = rec.get("bvh_dram_bytes_per_ray", max(0.0, rec["dram_bytes_per_ray"] - queue))
+        alg_per_ray = per_ray + bvh
         achieved = alg_per_ray * rays_per_launch / (launch_ms / 1e3) / 1e9
         roof.update({"achieved": round(achieved, 1), "frac": round(achieved / peak, 4),
-                     "traffic": int(rec["dram_bytes_per_ray"] * rays_per_launch),
+                     "traffic": int((queue + bvh) * rays_per_launch),
                      "traffic_source": rec["capture"], "alg_bytes_per_ray": round(alg_per_ray, 1),
                      "alg_bytes_per_launch": int(alg_per_ray * rays_per_launch),
                      "limiter": rec.get("limiter")})
