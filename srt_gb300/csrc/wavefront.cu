@@ -94,6 +94,24 @@ __device__ __forceinline__ uint32_t pack_flags(int depth, bool specular, int job
     return (uint32_t)depth | (specular ? 0x100u : 0u) | ((uint32_t)job << 16);
 }
 
+// A sample ends (path_tracer.cu:164-165): its radiance l goes to the film
+// unless it is NaN or infinite, and the pixel's finished-sample count (l.w)
+// steps.  Sets the progress counters to bump: the progressive frame's and,
+// at the pixel's last sample, the finished pixels'.
+__device__ __forceinline__ void end_sample(const JobRec& J, int pix, float4 l, int32_t*& frame_ctr,
+                                           int32_t*& pixel_ctr)
+{
+    if (isfinite(l.x) && isfinite(l.y) && isfinite(l.z)) {
+        const float4 f = J.film[pix];
+        const float s = (float)J.spp;
+        J.film[pix] = make_float4(f.x + l.x / s, f.y + l.y / s, f.z + l.z / s, 1.0f);
+    }
+    const int k = __float_as_int(l.w) + 1;
+    J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(k));
+    if (J.frame_done) frame_ctr = J.frame_done + (k - 1);
+    if (k >= J.spp) pixel_ctr = J.pixels_done;
+}
+
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
@@ -557,15 +575,7 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
                     ax[1] = tgt;
                 }
             }
-            if (isfinite(l.x) && isfinite(l.y) && isfinite(l.z)) {
-                float4 f = J.film[pix];
-                float s = (float)J.spp;
-                J.film[pix] = make_float4(f.x + l.x / s, f.y + l.y / s, f.z + l.z / s, 1.0f);
-            }
-            const int k = spp_done + 1;
-            J.lpath[pix] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(k));
-            if (J.frame_done) frame_ctr = J.frame_done + (k - 1);
-            if (k >= J.spp) pixel_ctr = J.pixels_done;
+            end_sample(J, pix, l, frame_ctr, pixel_ctr);
         }
         // progress counters: one atomic per distinct counter in the warp
         warp_count(frame_ctr);
@@ -577,12 +587,18 @@ __global__ void __launch_bounds__(kThreads) k_regen(const JobRec* __restrict__ j
 // ray, however few paths are left, and each pixel's samples follow one
 // another (one curand stream per pixel), so the last fifth of a frame's
 // iterations carries about 2 % of its rays.  Once k_advance finds at most
-// tail_below paths in flight, each thread here takes one queue entry and
-// carries that path, and its pixel's later samples, to the pixel's last
-// sample: closest hit and shadow ray as k_trace, shade_vertex as k_shade,
-// the film and the next sample as k_regen and k_shade, in the same order on
-// the same values, so every pixel ends with the value the iterations give.
-// Plain jobs only (no radiance-cache work).
+// tail_below paths in flight, pairs of lanes here take one queue entry each
+// and carry that path, and its pixel's later samples, to the pixel's last
+// sample.  The even lane owns the path: closest hit (as k_trace),
+// shade_vertex (as k_shade), the film and the next sample (as k_regen and
+// k_shade).  The odd lane traces the shadow ray the owner's last shading
+// cast, in the same traversal phase as the owner's next closest-hit ray, so
+// a segment costs the longer of the two traversals, not their sum.  Per
+// pixel the radiance additions keep the iterations' order -- the previous
+// vertex's NEE contribution, then the film if that vertex ended its sample,
+// then the next vertex's emitted radiance -- on the same values, so every
+// pixel ends with the value the iterations give.  Plain jobs only (no
+// radiance-cache work).
 constexpr int kFinishThreads = kTraceThreads;
 
 template <bool kCount>
@@ -593,87 +609,134 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish(const JobRec* __restr
     const int64_t n = min((int64_t)ctr->n_cur, capacity);
     __shared__ uint2 stack_mem[kStackEntries * kFinishThreads];
     Stack st{stack_mem + threadIdx.x, kFinishThreads, 0};
+    const int lane = threadIdx.x & 31;
+    const bool owner = (lane & 1) == 0;
     int overflow = 0;
     TraceCount cnt, scnt;  // closest-hit and shadow traversal work (profiling variant)
     int closest = 0, shadow = 0, ended = 0, taken = 0;
+    // owner: the path in flight (its next closest-hit ray) and what its last
+    // shading left pending for the next round: a shadow ray's contribution
+    // and the end of its sample, both for the pixel pend_pix of job pend_job
+    bool has_path = false, drained = false;
+    float4 o4 = make_float4(0.f, 0.f, 0.f, 0.f), d4 = o4, b4 = o4;
+    uint4 ra = make_uint4(0, 0, 0, 0);
+    uint2 rb = make_uint2(0, 0);
+    bool pend_shadow = false, pend_end = false;
+    float3 pend_c = f3(0.0f), sh_o = f3(0.0f), sh_d = f3(0.0f);
+    float sh_t = 0.0f;
+    int pend_pix = 0, pend_job = 0;
     for (;;) {
-        const unsigned long long i = atomicAdd(&ctr->fetch_tail, 1ull);
-        if (i >= (unsigned long long)n) break;
-        ++taken;
-        float4 o4 = q.o[i], d4 = q.d[i], b4 = q.beta[i];
-        uint4 ra = q.ra[i];
-        uint2 rb = q.rb[i];
-        for (;;) {
-            // closest hit (k_trace)
-            TravState s;
-            {
-                const SceneView& S = jobs[__float_as_uint(b4.w) >> 16].scene;
-                trav_init(s, S.nodes, S.tris, f3(o4), f3(d4), 1e-3f, 1e16f, st);
+        if (owner && !has_path && !drained) {
+            const unsigned long long i = atomicAdd(&ctr->fetch_tail, 1ull);
+            if (i < (unsigned long long)n) {
+                o4 = q.o[i];
+                d4 = q.d[i];
+                b4 = q.beta[i];
+                ra = q.ra[i];
+                rb = q.rb[i];
+                has_path = true;
+                ++taken;
+            } else {
+                drained = true;
             }
-            while (!trav_advance<false, kCount>(s, st, overflow, cnt)) {
-            }
-            const float2 uv = hit_barycentrics(s);
-            const float4 h = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
+        }
+        if (!__any_sync(kFull, owner && (has_path || pend_shadow || pend_end))) break;
+        // the owner's shadow ray to its partner lane
+        const bool sh_active = __shfl_sync(kFull, pend_shadow, lane & ~1);
+        const float sox = __shfl_sync(kFull, sh_o.x, lane & ~1), soy = __shfl_sync(kFull, sh_o.y, lane & ~1),
+                    soz = __shfl_sync(kFull, sh_o.z, lane & ~1);
+        const float sdx = __shfl_sync(kFull, sh_d.x, lane & ~1), sdy = __shfl_sync(kFull, sh_d.y, lane & ~1),
+                    sdz = __shfl_sync(kFull, sh_d.z, lane & ~1);
+        const float stm = __shfl_sync(kFull, sh_t, lane & ~1);
+        const int sjob = __shfl_sync(kFull, pend_job, lane & ~1);
+        // traversal phase: owner's closest-hit ray, partner's shadow ray
+        TravState s;
+        bool active = false;
+        if (owner && has_path) {
+            const SceneView& S = jobs[__float_as_uint(b4.w) >> 16].scene;
+            trav_init(s, S.nodes, S.tris, f3(o4), f3(d4), 1e-3f, 1e16f, st);
+            active = true;
             ++closest;
-            // shading (k_shade)
-            bool push_next = false, push_shadow = false, terminate = false, push_query = false;
-            float4 qrec[4];
-            float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
-            float3 sh_o = f3(0.0f), sh_d = f3(0.0f), sh_c = f3(0.0f);
-            float sh_t = 0.0f, pdf_next = 0.0f;
-            uint32_t flags = 0;
-            int pix = 0, job = 0;
-            shade_vertex<false>(jobs, o4, d4, b4, h, push_next, push_shadow, terminate, push_query, qrec, ro, rd, beta,
-                                L_add, sh_o, sh_d, sh_c, sh_t, pdf_next, flags, pix, job, ra, rb);
-            const JobRec& J = jobs[job];
-            float4* lp = J.lpath + pix;
-            if (L_add.x != 0.0f || L_add.y != 0.0f || L_add.z != 0.0f || !finite3(L_add)) {
-                const float4 l = *lp;
-                *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, l.w);
-            }
-            // shadow ray (k_trace)
-            if (push_shadow) {
-                ++shadow;
-                trav_init(s, J.scene.nodes, J.scene.tris, sh_o, sh_d, 1e-3f, sh_t, st, SRT_SHADOW_FAR_FIRST != 0);
-                while (!trav_advance<true, kCount>(s, st, overflow, scnt)) {
+        } else if (!owner && sh_active) {
+            const SceneView& S = jobs[sjob].scene;
+            trav_init(s, S.nodes, S.tris, make_float3(sox, soy, soz), make_float3(sdx, sdy, sdz), 1e-3f, stm, st,
+                      SRT_SHADOW_FAR_FIRST != 0);
+            mark_any_hit(s);
+            active = true;
+            ++shadow;
+        }
+        bool done = !active;
+        while (__any_sync(kFull, !done)) {
+            if (!done) done = trav_advance_mixed<kCount>(s, st, overflow, cnt, scnt);
+        }
+        const bool unoccluded = __shfl_sync(kFull, active && s.tri < 0, lane | 1);
+        if (owner) {
+            // the previous vertex's NEE contribution, then the end of its sample (k_trace)
+            if (pend_shadow || pend_end) {
+                const JobRec& P = jobs[pend_job];
+                float4* lp = P.lpath + pend_pix;
+                float4 l = *lp;
+                if (pend_shadow && unoccluded) {
+                    l = make_float4(l.x + pend_c.x, l.y + pend_c.y, l.z + pend_c.z, l.w);
+                    *lp = l;
                 }
-                if (s.tri < 0) {
+                if (pend_end) {
+                    int32_t* frame_ctr = nullptr;
+                    int32_t* pixel_ctr = nullptr;
+                    end_sample(P, pend_pix, l, frame_ctr, pixel_ctr);
+                    if (frame_ctr) atomicAdd(frame_ctr, 1);
+                    if (pixel_ctr) atomicAdd(pixel_ctr, 1);
+                    ++ended;
+                }
+                pend_shadow = pend_end = false;
+            }
+            if (has_path) {
+                const float2 uv = hit_barycentrics(s);
+                const float4 h = make_float4(s.tmax, uv.x, uv.y, __int_as_float(s.tri));
+                // shading (k_shade)
+                bool push_next = false, push_shadow = false, terminate = false, push_query = false;
+                float4 qrec[4];
+                float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f), sh_c = f3(0.0f);
+                float pdf_next = 0.0f;
+                uint32_t flags = 0;
+                int pix = 0, job = 0;
+                shade_vertex<false>(jobs, o4, d4, b4, h, push_next, push_shadow, terminate, push_query, qrec, ro, rd,
+                                    beta, L_add, sh_o, sh_d, sh_c, sh_t, pdf_next, flags, pix, job, ra, rb);
+                const JobRec& J = jobs[job];
+                float4* lp = J.lpath + pix;
+                if (L_add.x != 0.0f || L_add.y != 0.0f || L_add.z != 0.0f || !finite3(L_add)) {
                     const float4 l = *lp;
-                    *lp = make_float4(l.x + sh_c.x, l.y + sh_c.y, l.z + sh_c.z, l.w);
+                    *lp = make_float4(l.x + L_add.x, l.y + L_add.y, l.z + L_add.z, l.w);
+                }
+                pend_pix = pix;
+                pend_job = job;
+                pend_shadow = push_shadow;
+                pend_c = sh_c;
+                if (push_next) {
+                    o4 = make_float4(ro.x, ro.y, ro.z, __int_as_float(pix));
+                    d4 = make_float4(rd.x, rd.y, rd.z, pdf_next);
+                    b4 = make_float4(beta.x, beta.y, beta.z, __uint_as_float(flags));
+                } else {
+                    // the sample ends once its last shadow ray is in; the pixel's
+                    // next sample starts now, from where shading left the stream
+                    pend_end = true;
+                    if (__float_as_int(lp->w) + 1 < J.spp) {
+                        Rng rng;
+                        rng.load(ra, rb);
+                        const int ix = pix % J.width, iy = pix / J.width;
+                        const float xx = ((float)ix + rng.next()) / (float)J.width;
+                        const float yy = ((float)iy + rng.next()) / (float)J.height;
+                        float3 o, d;
+                        camera_ray(J.cam, xx, yy, o, d);
+                        rng.store(ra, rb);
+                        o4 = make_float4(o.x, o.y, o.z, __int_as_float(pix));
+                        d4 = make_float4(d.x, d.y, d.z, 1.0f);
+                        b4 = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pack_flags(0, true, job)));
+                    } else {
+                        has_path = false;
+                    }
                 }
             }
-            if (push_next) {
-                o4 = make_float4(ro.x, ro.y, ro.z, __int_as_float(pix));
-                d4 = make_float4(rd.x, rd.y, rd.z, pdf_next);
-                b4 = make_float4(beta.x, beta.y, beta.z, __uint_as_float(flags));
-                continue;
-            }
-            // the sample ends (k_regen) and the pixel's next one starts (k_shade)
-            ++ended;
-            const float4 l = *lp;
-            if (isfinite(l.x) && isfinite(l.y) && isfinite(l.z)) {
-                const float4 f = J.film[pix];
-                const float sp = (float)J.spp;
-                J.film[pix] = make_float4(f.x + l.x / sp, f.y + l.y / sp, f.z + l.z / sp, 1.0f);
-            }
-            const int k = __float_as_int(l.w) + 1;
-            *lp = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(k));
-            if (J.frame_done) atomicAdd(J.frame_done + (k - 1), 1);
-            if (k >= J.spp) {
-                if (J.pixels_done) atomicAdd(J.pixels_done, 1);
-                break;
-            }
-            Rng rng;
-            rng.load(ra, rb);
-            const int ix = pix % J.width, iy = pix / J.width;
-            const float xx = ((float)ix + rng.next()) / (float)J.width;
-            const float yy = ((float)iy + rng.next()) / (float)J.height;
-            float3 o, d;
-            camera_ray(J.cam, xx, yy, o, d);
-            rng.store(ra, rb);
-            o4 = make_float4(o.x, o.y, o.z, __int_as_float(pix));
-            d4 = make_float4(d.x, d.y, d.z, 1.0f);
-            b4 = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pack_flags(0, true, job)));
         }
     }
     // one atomic per warp and counter
