@@ -861,6 +861,9 @@ Engine::~Engine()
     for (auto& e : ev_tail_)
         if (e) cudaEventDestroy(e);
     if (graph_stream_) cudaStreamDestroy(graph_stream_);
+    if (side_stream_) cudaStreamDestroy(side_stream_);
+    if (fork_ev_) cudaEventDestroy(fork_ev_);
+    if (join_ev_) cudaEventDestroy(join_ev_);
     if (host_counters_) cudaFreeHost(host_counters_);
 }
 
@@ -907,6 +910,9 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     SRT_CUDA_TRY(cudaMemset(pixels_done_, 0, 4 * (size_t)max_jobs));
     SRT_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&host_counters_), sizeof(Counters)));
     SRT_CUDA_TRY(cudaStreamCreateWithFlags(&graph_stream_, cudaStreamNonBlocking));
+    SRT_CUDA_TRY(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking));
+    SRT_CUDA_TRY(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
+    SRT_CUDA_TRY(cudaEventCreateWithFlags(&join_ev_, cudaEventDisableTiming));
     int sms = device_sm_count();
     // persistent traversal (dynamic ray fetch): as many blocks as are resident at once
     auto resident = [&](const void* fn) {
@@ -951,25 +957,34 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     // External flag makes it a real timestamp node of the graph
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (prof) cudaStreamIsCapturing(st, &cs);
-    auto mark = [&](int k, int e) {
+    auto mark_on = [&](cudaStream_t s, int k, int e) {
         if (!prof) return;
         if (cs == cudaStreamCaptureStatusActive)
-            cudaEventRecordWithFlags(ev_[parity][k][e], st, cudaEventRecordExternal);
+            cudaEventRecordWithFlags(ev_[parity][k][e], s, cudaEventRecordExternal);
         else
-            cudaEventRecord(ev_[parity][k][e], st);  // direct launches (SRT_NO_GRAPH=1)
+            cudaEventRecord(ev_[parity][k][e], s);  // direct launches (SRT_NO_GRAPH=1)
     };
+    auto mark = [&](int k, int e) { mark_on(st, k, e); };
     mark(0, 0);
     if (prof && count_)
         k_trace<true><<<grid_trace_, kTraceThreads, 0, st>>>(jobs_, cur, sq_, hits_, counters_, capacity_, 0);
     else
         k_trace<false><<<grid_trace_, kTraceThreads, 0, st>>>(jobs_, cur, sq_, hits_, counters_, capacity_, 0);
     mark(0, 1);
-    mark(3, 0);
-    k_regen<<<grid_stride_, kThreads, 0, st>>>(jobs_, done_, counters_, capacity_);
-    mark(3, 1);
+    // k_regen (the previous iteration's ended samples) and k_order (this
+    // iteration's hits) touch disjoint data: k_regen runs on a forked stream
+    // beside k_order, and k_shade, which reads the sample counts k_regen
+    // writes, waits for both
+    cudaEventRecord(fork_ev_, st);
+    cudaStreamWaitEvent(side_stream_, fork_ev_, 0);
+    mark_on(side_stream_, 3, 0);
+    k_regen<<<grid_stride_, kThreads, 0, side_stream_>>>(jobs_, done_, counters_, capacity_);
+    mark_on(side_stream_, 3, 1);
+    cudaEventRecord(join_ev_, side_stream_);
     mark(2, 0);
     k_order<<<grid_order_, kOrderThreads, 0, st>>>(hits_, order_, counters_, capacity_);
     mark(2, 1);
+    cudaStreamWaitEvent(st, join_ev_, 0);
     mark(1, 0);
     if (cache_)
         k_shade<true><<<grid_shade_, kShadeThreads, 0, st>>>(jobs_, cur, hits_, order_, nxt, sq_, done_, counters_,

@@ -196,6 +196,8 @@ private:
     Counters* host_counters_ = nullptr;
     cudaGraphExec_t graph_ = nullptr, graph_prof_ = nullptr;
     cudaStream_t graph_stream_ = nullptr;
+    cudaStream_t side_stream_ = nullptr;        // k_regen beside k_order
+    cudaEvent_t fork_ev_ = nullptr, join_ev_ = nullptr;
     cudaEvent_t ev_[2][5][2] = {};
     cudaEvent_t ev_tail_[2] = {};
     bool profile_ = false;
