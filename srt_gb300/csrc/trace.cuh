@@ -261,15 +261,16 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     uint32_t hitmask = 0;
     // a child's x and y near planes come from one two-wide FMA, and its x and
     // y far planes from another (the same values as four fmaf: 744.6 -> 748.8
-    // Msamples/s, k_closest 87.7 -> 86.85 ms per benchmark frame; pairing
-    // across two children instead needs the constants twice and spills)
+    // Msamples/s); the z planes of two siblings, which share a plane word,
+    // likewise (880.3 -> 887.1).  Pairing x and y across siblings too needs
+    // every scale and offset twice in registers and spills.
     const float2 axy = make_float2(Ax, Ay), cnxy = make_float2(cnx, cny), cfxy = make_float2(cfx, cfy);
-    auto child = [&](int s, uint32_t wnx, uint32_t wfx, uint32_t wny, uint32_t wfy, uint32_t wnz, uint32_t wfz) {
+    const float2 az2 = make_float2(Az, Az), cnz2 = make_float2(cnz, cnz), cfz2 = make_float2(cfz, cfz);
+    auto child = [&](int s, uint32_t wnx, uint32_t wfx, uint32_t wny, uint32_t wfy, float nz, float fz) {
         const uint32_t meta = ((s < 4 ? mlo : mhi) >> (8 * (s & 3))) & 0xffu;
         int hi = s & 1;
         const float2 n = fma2(make_float2(q23(wnx, hi), q23(wny, hi)), axy, cnxy);
         const float2 f = fma2(make_float2(q23(wfx, hi), q23(wfy, hi)), axy, cfxy);
-        float nz = fmaf(q23(wnz, hi), Az, cnz), fz = fmaf(q23(wfz, hi), Az, cfz);
         float tn = fmax3(n.x, n.y, fmaxf(nz, tmin));
         float tf = fmin3(f.x, f.y, fminf(fz, tmax));
         // (meta >> 5) << (meta & 31); an empty slot's byte is 0
@@ -283,9 +284,12 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     const uint4 nqy = sel4(oy, l6, l3), fqy = sel4(oy, l3, l6);
     const uint4 nqz = sel4(oz, l7, l4), fqz = sel4(oz, l4, l7);
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const int j = s >> 1;
-        child(s, word4(nqx, j), word4(fqx, j), word4(nqy, j), word4(fqy, j), word4(nqz, j), word4(fqz, j));
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t wnz = word4(nqz, j), wfz = word4(fqz, j);
+        const float2 nz = fma2(make_float2(q23(wnz, 0), q23(wnz, 1)), az2, cnz2);
+        const float2 fz = fma2(make_float2(q23(wfz, 0), q23(wfz, 1)), az2, cfz2);
+        child(2 * j, word4(nqx, j), word4(fqx, j), word4(nqy, j), word4(fqy, j), nz.x, fz.x);
+        child(2 * j + 1, word4(nqx, j), word4(fqx, j), word4(nqy, j), word4(fqy, j), nz.y, fz.y);
     }
     group = make_uint2(w1.x, imask | ((hitmask >> 24) << 8));
     tmask = hitmask & 0x00ffffffu;
