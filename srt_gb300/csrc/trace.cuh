@@ -74,6 +74,18 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
         : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
     return d;
 }
+// two-wide round-to-nearest product (mul.rn.f32x2), each lane equal to
+// __fmul_rn; only where the product feeds no add (a product feeding a
+// two-wide subtract came back contracted)
+__device__ __forceinline__ float2 mul2(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n .reg .b64 a, b, d;\n mov.b64 a, {%2, %3};\n mov.b64 b, {%4, %5};\n mul.rn.f32x2 d, a, b;\n"
+        " mov.b64 {%0, %1}, d;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
 __device__ __forceinline__ RayPre make_ray(float3 o, float3 d)
 {
     RayPre r;
@@ -266,16 +278,7 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     // every scale and offset twice in registers and spills.
     const float2 axy = make_float2(Ax, Ay), cnxy = make_float2(cnx, cny), cfxy = make_float2(cfx, cfy);
     const float2 az2 = make_float2(Az, Az), cnz2 = make_float2(cnz, cnz), cfz2 = make_float2(cfz, cfz);
-    auto child = [&](int s, uint32_t wnx, uint32_t wfx, uint32_t wny, uint32_t wfy, float nz, float fz) {
-        const uint32_t meta = ((s < 4 ? mlo : mhi) >> (8 * (s & 3))) & 0xffu;
-        int hi = s & 1;
-        const float2 n = fma2(make_float2(q23(wnx, hi), q23(wny, hi)), axy, cnxy);
-        const float2 f = fma2(make_float2(q23(wfx, hi), q23(wfy, hi)), axy, cfxy);
-        float tn = fmax3(n.x, n.y, fmaxf(nz, tmin));
-        float tf = fmin3(f.x, f.y, fminf(fz, tmax));
-        // (meta >> 5) << (meta & 31); an empty slot's byte is 0
-        if (tn <= tf * 1.00000024f) hitmask |= __funnelshift_l(0u, meta >> 5, meta);
-    };
+    const float2 widen2 = make_float2(1.00000024f, 1.00000024f);
     uint4 l2, l3, l4, l5, l6, l7;  // lo x, y, z then hi x, y, z
     ld_nc_v8(np + 2, l2, l3);
     ld_nc_v8(np + 4, l4, l5);
@@ -285,11 +288,24 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     const uint4 nqz = sel4(oz, l7, l4), fqz = sel4(oz, l4, l7);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
+        // children 2j (low halves of the plane words) and 2j + 1 (high halves)
+        const uint32_t wnx = word4(nqx, j), wfx = word4(fqx, j), wny = word4(nqy, j), wfy = word4(fqy, j);
         const uint32_t wnz = word4(nqz, j), wfz = word4(fqz, j);
         const float2 nz = fma2(make_float2(q23(wnz, 0), q23(wnz, 1)), az2, cnz2);
         const float2 fz = fma2(make_float2(q23(wfz, 0), q23(wfz, 1)), az2, cfz2);
-        child(2 * j, word4(nqx, j), word4(fqx, j), word4(nqy, j), word4(fqy, j), nz.x, fz.x);
-        child(2 * j + 1, word4(nqx, j), word4(fqx, j), word4(nqy, j), word4(fqy, j), nz.y, fz.y);
+        const float2 n0 = fma2(make_float2(q23(wnx, 0), q23(wny, 0)), axy, cnxy);
+        const float2 f0 = fma2(make_float2(q23(wfx, 0), q23(wfy, 0)), axy, cfxy);
+        const float2 n1 = fma2(make_float2(q23(wnx, 1), q23(wny, 1)), axy, cnxy);
+        const float2 f1 = fma2(make_float2(q23(wfx, 1), q23(wfy, 1)), axy, cfxy);
+        const float tn0 = fmax3(n0.x, n0.y, fmaxf(nz.x, tmin)), tn1 = fmax3(n1.x, n1.y, fmaxf(nz.y, tmin));
+        // the far distances widened by one two-wide multiply (a lone product: nothing to contract)
+        const float2 tf = mul2(make_float2(fmin3(f0.x, f0.y, fminf(fz.x, tmax)), fmin3(f1.x, f1.y, fminf(fz.y, tmax))),
+                               widen2);
+        const uint32_t mw = j < 2 ? mlo : mhi;
+        const uint32_t m0 = (mw >> (16 * (j & 1))) & 0xffu, m1 = (mw >> (16 * (j & 1) + 8)) & 0xffu;
+        // (meta >> 5) << (meta & 31); an empty slot's byte is 0
+        if (tn0 <= tf.x) hitmask |= __funnelshift_l(0u, m0 >> 5, m0);
+        if (tn1 <= tf.y) hitmask |= __funnelshift_l(0u, m1 >> 5, m1);
     }
     group = make_uint2(w1.x, imask | ((hitmask >> 24) << 8));
     tmask = hitmask & 0x00ffffffu;
