@@ -86,6 +86,17 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b)
         : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
     return d;
 }
+// two-wide round-to-nearest difference (sub.rn.f32x2); only where no
+// product feeds it
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n .reg .b64 a, b, d;\n mov.b64 a, {%2, %3};\n mov.b64 b, {%4, %5};\n sub.rn.f32x2 d, a, b;\n"
+        " mov.b64 {%0, %1}, d;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
 __device__ __forceinline__ RayPre make_ray(float3 o, float3 d)
 {
     RayPre r;
@@ -247,10 +258,14 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     uint32_t imask = w0.w >> 24;
     float sx = __int_as_float((ex + 127) << 23), sy = __int_as_float((ey + 127) << 23),
           sz = __int_as_float((ez + 127) << 23);
-    float Ax = sx * r.idir.x, Ay = sy * r.idir.y, Az = sz * r.idir.z;
-    float Bx = (__uint_as_float(w0.x) - r.o.x) * r.idir.x;
-    float By = (__uint_as_float(w0.y) - r.o.y) * r.idir.y;
-    float Bz = (__uint_as_float(w0.z) - r.o.z) * r.idir.z;
+    // x and y in two-wide operations (each lane equal to the scalar one; the
+    // difference feeds a product, which cannot contract)
+    const float2 idxy = make_float2(r.idir.x, r.idir.y);
+    const float2 Axy = mul2(make_float2(sx, sy), idxy);
+    const float2 Bxy = mul2(sub2(make_float2(__uint_as_float(w0.x), __uint_as_float(w0.y)), make_float2(r.o.x, r.o.y)),
+                            idxy);
+    const float Ax = Axy.x, Ay = Axy.y, Az = sz * r.idir.z;
+    const float Bz = (__uint_as_float(w0.z) - r.o.z) * r.idir.z;
     // Plane q of an axis is at t = q A + B = (2^23 + q) A + C with C = B - 2^23 A,
     // so each plane costs one permute and one FMA (the fused product is exact).
     // Rounding C costs at most |A| / 2 (one quantisation step is |A| in t), so
@@ -258,7 +273,8 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     // farther: the test stays conservative (no exactly-hit slab missed on 4M
     // random borderline cases from a margin of 0.625 up).
     const float K = 8388608.0f;
-    const float Cx = fmaf(-K, Ax, Bx), Cy = fmaf(-K, Ay, By), Cz = fmaf(-K, Az, Bz);
+    const float2 Cxy = fma2(make_float2(-K, -K), Axy, Bxy);
+    const float Cx = Cxy.x, Cy = Cxy.y, Cz = fmaf(-K, Az, Bz);
     const float mx = SRT_SLAB_MARGIN * fabsf(Ax), my = SRT_SLAB_MARGIN * fabsf(Ay), mz = SRT_SLAB_MARGIN * fabsf(Az);
     const float cnx = Cx - mx, cfx = Cx + mx;
     const float cny = Cy - my, cfy = Cy + my;
@@ -276,7 +292,7 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
     // Msamples/s); the z planes of two siblings, which share a plane word,
     // likewise (880.3 -> 887.1).  Pairing x and y across siblings too needs
     // every scale and offset twice in registers and spills.
-    const float2 axy = make_float2(Ax, Ay), cnxy = make_float2(cnx, cny), cfxy = make_float2(cfx, cfy);
+    const float2 axy = Axy, cnxy = make_float2(cnx, cny), cfxy = make_float2(cfx, cfy);
     const float2 az2 = make_float2(Az, Az), cnz2 = make_float2(cnz, cnz), cfz2 = make_float2(cfz, cfz);
     const float2 widen2 = make_float2(1.00000024f, 1.00000024f);
     uint4 l2, l3, l4, l5, l6, l7;  // lo x, y, z then hi x, y, z
