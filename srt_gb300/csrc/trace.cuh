@@ -317,8 +317,9 @@ __device__ __forceinline__ void visit_node(const WideNode* __restrict__ nodes, u
         // the far distances widened by one two-wide multiply (a lone product: nothing to contract)
         const float2 tf = mul2(make_float2(fmin3(f0.x, f0.y, fminf(fz.x, tmax)), fmin3(f1.x, f1.y, fminf(fz.y, tmax))),
                                widen2);
+        // meta bytes 2j and 2j + 1 (one byte permute each, zeros above)
         const uint32_t mw = j < 2 ? mlo : mhi;
-        const uint32_t m0 = (mw >> (16 * (j & 1))) & 0xffu, m1 = (mw >> (16 * (j & 1) + 8)) & 0xffu;
+        const uint32_t m0 = __byte_perm(mw, 0u, 0x4440u | (2u * (j & 1))), m1 = __byte_perm(mw, 0u, 0x4441u | (2u * (j & 1)));
         // (meta >> 5) << (meta & 31); an empty slot's byte is 0
         if (tn0 <= tf.x) hitmask |= __funnelshift_l(0u, m0 >> 5, m0);
         if (tn1 <= tf.y) hitmask |= __funnelshift_l(0u, m1 >> 5, m1);
