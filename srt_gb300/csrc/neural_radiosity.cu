@@ -51,6 +51,7 @@ constexpr int kNrEnc = 96, kNrWidth = 256, kNrOut = 16;
 constexpr int kNrLayers = 5;
 
 __host__ __device__ constexpr int64_t nr_level_res(int l) { return (int64_t)kNrBaseRes << l; }
+static_assert((kNrBaseRes & (kNrBaseRes - 1)) == 0, "level resolutions are powers of two (dense grid index)");
 __host__ __device__ constexpr int64_t nr_level_size(int l)
 {
     return nr_level_res(l) * nr_level_res(l) * nr_level_res(l) <= (1ll << kNrLog2T)
@@ -253,9 +254,6 @@ __global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inp
         const int64_t q = t / kNrLevels;
         const int l = (int)(t % kNrLevels);
         const float* in = inputs + 12 * q;
-        auto put = [&](int col, float v) {
-            *reinterpret_cast<__nv_bfloat16*>(out + nr_enc_off(q, col)) = __float2bfloat16_rn(v);
-        };
         const float scale = (float)nr_level_res(l) - 1.0f;
         const int64_t res = nr_level_res(l);
         const bool dense = nr_level_size(l) == res * res * res;
@@ -276,9 +274,10 @@ __global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inp
             const uint32_t x = (uint32_t)(pi[0] + dx), y = (uint32_t)(pi[1] + dy), z = (uint32_t)(pi[2] + dz);
             int64_t e;
             if (dense) {
-                const int64_t r = res;
-                e = (((int64_t)(int32_t)x % r + r) % r) + (((int64_t)(int32_t)y % r + r) % r) * r +
-                    (((int64_t)(int32_t)z % r + r) % r) * r * r;
+                // ((v mod r) + r) mod r of the signed corner coordinate: every level's
+                // resolution is a power of two, where that is v & (r - 1)
+                const uint32_t m = (uint32_t)res - 1u;
+                e = (int64_t)((x & m) + (y & m) * (uint32_t)res + (z & m) * (uint32_t)(res * res));
             } else {
                 e = (int64_t)((x * 1u ^ y * 2654435761u ^ z * 805459861u) & ((1u << kNrLog2T) - 1u));
             }
@@ -302,14 +301,23 @@ __global__ void __launch_bounds__(256) k_nr_encode(const float* __restrict__ inp
         q8.w = pack2_bf16(acc[6], acc[7]);
         *reinterpret_cast<uint4*>(out + nr_enc_off(q, l * kNrFeat)) = q8;
         if (l == 0) {
-            float sd[9], sn[9];
-            sh3(in[3] * 2.0f - 1.0f, in[4] * 2.0f - 1.0f, in[5] * 2.0f - 1.0f, sd);
-            sh3(in[6] * 2.0f - 1.0f, in[7] * 2.0f - 1.0f, in[8] * 2.0f - 1.0f, sn);
-            const int b0 = kNrLevels * kNrFeat;
-            for (int k = 0; k < 9; ++k) put(b0 + k, sd[k]);
-            for (int k = 0; k < 9; ++k) put(b0 + 9 + k, sn[k]);
-            for (int k = 0; k < 3; ++k) put(b0 + 18 + k, in[9 + k]);
-            for (int k = kNrEncUsed; k < kNrEnc; ++k) put(k, 1.0f);
+            // columns 64..95: direction and normal SH, colour, then ones; four
+            // 16-byte core-matrix rows, one vector store each
+            static_assert(kNrLevels * kNrFeat == 64 && kNrEnc == 96, "encoding layout");
+            float v[32];
+            sh3(in[3] * 2.0f - 1.0f, in[4] * 2.0f - 1.0f, in[5] * 2.0f - 1.0f, v);
+            sh3(in[6] * 2.0f - 1.0f, in[7] * 2.0f - 1.0f, in[8] * 2.0f - 1.0f, v + 9);
+            for (int k = 0; k < 3; ++k) v[18 + k] = in[9 + k];
+            for (int k = kNrEncUsed - 64; k < 32; ++k) v[k] = 1.0f;
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                uint4 w;
+                w.x = pack2_bf16(v[8 * g], v[8 * g + 1]);
+                w.y = pack2_bf16(v[8 * g + 2], v[8 * g + 3]);
+                w.z = pack2_bf16(v[8 * g + 4], v[8 * g + 5]);
+                w.w = pack2_bf16(v[8 * g + 6], v[8 * g + 7]);
+                *reinterpret_cast<uint4*>(out + nr_enc_off(q, 64 + 8 * g)) = w;
+            }
         }
     }
 }
