@@ -378,9 +378,9 @@ srt_status srt_pt_set_launch_mode(srt_pt* pt, int32_t mode);
  * takes them over and carries each, with its pixel's remaining samples, to
  * the end, through the same device code (the image is the same bit for
  * bit; iteration counts past that point are not recorded).  0 disables it;
- * the default is SRT_PT_TAIL_DEFAULT paths.  Renders with a radiance cache
- * always run their iterations to the end. */
-enum { SRT_PT_TAIL_DEFAULT = 32768 };
+ * the default is min(SRT_PT_TAIL_DEFAULT, width * height / 8) paths.
+ * Renders with a radiance cache always run their iterations to the end. */
+enum { SRT_PT_TAIL_DEFAULT = 65536 };
 srt_status srt_pt_set_tail(srt_pt* pt, int64_t max_paths);
 
 /* Queue counts of the last render's wavefront iterations (no counterpart in

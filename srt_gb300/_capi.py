@@ -25,7 +25,7 @@ RNG_CURAND, RNG_HASH = 0, 1
 PT_FIXED_CDF_REMAP = 1
 PT_NEE_FIRST_VERTEX_ONLY = 2
 LAUNCH_GRAPH, LAUNCH_DIRECT = 0, 1
-PT_TAIL_DEFAULT = 32768
+PT_TAIL_DEFAULT = 65536
 TONE_NONE, TONE_CLAMP, TONE_REINHARD, TONE_UNCHARTED2, TONE_ACES = 0, 1, 2, 3, 4
 METRIC_MSE, METRIC_MAPE, METRIC_SMAPE, METRIC_RELMSE = 0, 1, 2, 3
 MEASURE_NONE, MEASURE_REFERENCE, MEASURE_ERROR = 0, 1, 2

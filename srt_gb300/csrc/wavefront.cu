@@ -1290,7 +1290,8 @@ extern "C" srt_status srt_pt_create(srt_scene* scene, int32_t width, int32_t hei
     p->height = height;
     const size_t npix = (size_t)width * height;
     srt_status st = p->engine.init((int64_t)npix, 1);
-    p->engine.set_tail(SRT_PT_TAIL_DEFAULT);
+    // the end of the frame from at most min(SRT_PT_TAIL_DEFAULT, pixels / 8) paths in flight
+    p->engine.set_tail((int32_t)std::min<int64_t>(SRT_PT_TAIL_DEFAULT, (int64_t)npix / 8));
     if (st == SRT_OK) st = p->job_buf.alloc(npix * 16 + 1024, "per-pixel path state");
     if (st != SRT_OK) {
         delete p;
