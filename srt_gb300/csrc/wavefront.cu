@@ -89,6 +89,13 @@ __device__ __forceinline__ int region_cell(const CacheRec& c, float3 p)
     return (z * r + y) * r + x;
 }
 
+// Slot of entry i of a path queue whose first nf entries fill it from the
+// front and the rest from the back (Counters::nf_cur).
+__device__ __forceinline__ int64_t qslot(int64_t i, int32_t nf, int64_t capacity)
+{
+    return i < nf ? i : capacity - 1 - (i - nf);
+}
+
 __device__ __forceinline__ uint32_t pack_flags(int depth, bool specular, int job)
 {
     return (uint32_t)depth | (specular ? 0x100u : 0u) | ((uint32_t)job << 16);
@@ -119,7 +126,7 @@ __device__ __forceinline__ void end_sample(const JobRec& J, int pix, float4 l, i
 // Seeds job `job`: RandomGenerator(seed + idx, 0), film = (0, 0, 0, 1),
 // sample-0 camera ray (two jitter draws) appended to queue q at *n.
 __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ jobs, int job, PathQueue q,
-                                                    int32_t* n, int64_t capacity, int32_t* overflow)
+                                                    int32_t* n, int32_t* front, int64_t capacity, int32_t* overflow)
 {
     const JobRec& J = jobs[job];
     const int npix = J.npix;
@@ -143,7 +150,9 @@ __global__ void __launch_bounds__(kThreads) k_start(const JobRec* __restrict__ j
             if (J.cache.w && (pix % J.cache.train_stride) == J.cache.train_phase)
                 J.cache.t_len[pix / J.cache.train_stride] = 0;
         }
-        int32_t slot = warp_append(n, valid);
+        // at the front of the current queue (its back may hold other jobs' camera rays)
+        int32_t slot = warp_append(front, valid);
+        warp_append(n, valid);
         if (valid) {
             if (slot < capacity) {
                 q.o[slot] = make_float4(o.x, o.y, o.z, __int_as_float(pix));
@@ -177,6 +186,7 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace(c
     // a counter past the capacity (overflow, reported by the host) never indexes past a queue
     const int64_t ns = min((int64_t)ctr->n_sp, capacity);
     const int64_t nc = shadows_only ? 0 : min((int64_t)ctr->n_cur, capacity);
+    const int32_t nf = ctr->nf_cur;
     int overflow = 0;
     TraceCount cnt, scnt;
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
@@ -191,7 +201,7 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace(c
                 trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, d.w, stk, SRT_SHADOW_FAR_FIRST != 0);
                 mark_any_hit(s);
             } else {
-                const int64_t j = i - ns;
+                const int64_t j = qslot(i - ns, nf, capacity);
                 const float4 o = q.o[j], d = q.d[j];
                 const SceneView& S = jobs[__float_as_uint(q.beta[j].w) >> 16].scene;
                 trav_init(s, S.nodes, S.tris, f3(o), f3(d), 1e-3f, 1e16f, stk);
@@ -445,13 +455,15 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                                                     DoneQueue done, Counters* ctr, int64_t capacity)
 {
     const int n = (int)min((int64_t)ctr->n_cur, capacity);
+    const int32_t nf = ctr->nf_cur;
     const int stride = gridDim.x * blockDim.x;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
         // queue entries in k_order's shading order: hits first, then misses
         const int j = base + (threadIdx.x & 31);
         const bool valid = j < n;
         const int i = valid ? __ldg(order + j) : 0;
-        bool push_next = false, push_shadow = false, terminate = false, push_query = false;
+        const int64_t si = qslot(i, nf, capacity);
+        bool push_next = false, push_shadow = false, terminate = false, push_query = false, push_cam = false;
         float4 qrec[4];
         float3 ro = f3(0.0f), rd = f3(0.0f), beta = f3(0.0f), L_add = f3(0.0f);
         float3 sh_o = f3(0.0f), sh_d = f3(0.0f), sh_c = f3(0.0f);
@@ -461,10 +473,10 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
         uint4 ra = make_uint4(0, 0, 0, 0);
         uint2 rb = make_uint2(0, 0);
         if (valid) {
-            float4 o4 = q.o[i], d4 = q.d[i], b4 = q.beta[i];
+            float4 o4 = q.o[si], d4 = q.d[si], b4 = q.beta[si];
             float4 h = hits[i];
-            ra = q.ra[i];
-            rb = q.rb[i];
+            ra = q.ra[si];
+            rb = q.rb[si];
             shade_vertex<kCache>(jobs, o4, d4, b4, h, push_next, push_shadow, terminate, push_query, qrec, ro, rd,
                                  beta, L_add, sh_o, sh_d, sh_c, sh_t, pdf_next, flags, pix, job, ra, rb);
         }
@@ -501,10 +513,18 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                 beta = f3(1.0f);
                 pdf_next = 1.0f;
                 flags = pack_flags(0, true, job);
-                push_next = true;
+                push_cam = true;
             }
         }
+        // the next queue: continuing paths from the front, camera rays from the
+        // back (a lane does at most one of the two; every lane takes part in
+        // both warp-wide appends)
         int32_t slot = warp_append(&ctr->n_next, push_next);
+        {
+            const int32_t cs = warp_append(&ctr->n_cam, push_cam);
+            if (push_cam) slot = cs < capacity ? (int32_t)(capacity - 1 - cs) : (int32_t)capacity;
+            push_next = push_next || push_cam;
+        }
         if (push_next) {
             if (slot < capacity) {
                 qn.o[slot] = make_float4(ro.x, ro.y, ro.z, __int_as_float(pix));
@@ -629,11 +649,12 @@ __global__ void __launch_bounds__(kFinishThreads) k_finish(const JobRec* __restr
         if (owner && !has_path && !drained) {
             const unsigned long long i = atomicAdd(&ctr->fetch_tail, 1ull);
             if (i < (unsigned long long)n) {
-                o4 = q.o[i];
-                d4 = q.d[i];
-                b4 = q.beta[i];
-                ra = q.ra[i];
-                rb = q.rb[i];
+                const int64_t si = qslot((int64_t)i, ctr->nf_cur, capacity);
+                o4 = q.o[si];
+                d4 = q.d[si];
+                b4 = q.beta[si];
+                ra = q.ra[si];
+                rb = q.rb[si];
                 has_path = true;
                 ++taken;
             } else {
@@ -773,6 +794,7 @@ __global__ void k_end_tail(Counters* c)
 {
     if (!c->tail_go) return;
     c->n_cur = 0;
+    c->nf_cur = 0;
     c->fetch_tail = 0;
     c->tail_go = 0;
 }
@@ -805,8 +827,10 @@ __global__ void k_advance(Counters* c, IterCount* history, const JobRec* __restr
     c->started += c->n_done;
     c->n_sp = c->n_shadow;  // traced by the next k_trace
     c->n_dp = c->n_done;    // added to the film by the next k_regen
-    c->n_cur = c->n_next;
+    c->n_cur = c->n_next + c->n_cam;
+    c->nf_cur = c->n_next;
     c->n_next = 0;
+    c->n_cam = 0;
     c->n_shadow = 0;
     c->n_done = 0;
     c->fetch_closest = 0;
@@ -942,7 +966,7 @@ srt_status Engine::start_job(int job, const JobRec& rec, cudaStream_t st)
 {
     int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((rec.npix + kThreads - 1) / kThreads,
                                                              (int64_t)device_sm_count() * 16));
-    k_start<<<blocks, kThreads, 0, st>>>(jobs_, job, q_[0], &counters_->n_cur, capacity_,
+    k_start<<<blocks, kThreads, 0, st>>>(jobs_, job, q_[0], &counters_->n_cur, &counters_->nf_cur, capacity_,
                                          &counters_->overflow_queue);
     times_.launches += 1;
     SRT_CUDA_TRY(cudaGetLastError());
