@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -53,6 +54,28 @@ __device__ __forceinline__ int32_t warp_append(int32_t* counter, bool pred)
     if (lane == leader) base = atomicAdd(counter, __popc(m));
     base = __shfl_sync(kFull, base, leader);
     return pred ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+static_assert(offsetof(Counters, n_next) % 8 == 0 && offsetof(Counters, n_cam) == offsetof(Counters, n_next) + 4,
+              "n_next and n_cam share one 64-bit word");
+
+// Two appends with one atomic on a 64-bit word holding both counters (low
+// word: a's, high word: b's); a lane takes part in at most one of them.
+__device__ __forceinline__ void warp_append_pair(int32_t* counters, bool a, bool b, int32_t& sa, int32_t& sb)
+{
+    const uint32_t ma = __ballot_sync(kFull, a), mb = __ballot_sync(kFull, b);
+    sa = sb = -1;
+    if ((ma | mb) == 0u) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ma | mb) - 1;
+    unsigned long long base = 0;
+    if (lane == leader)
+        base = atomicAdd(reinterpret_cast<unsigned long long*>(counters),
+                         (unsigned long long)__popc(ma) | ((unsigned long long)__popc(mb) << 32));
+    base = __shfl_sync(kFull, base, leader);
+    const uint32_t below = (1u << lane) - 1u;
+    if (a) sa = (int32_t)(uint32_t)base + __popc(ma & below);
+    if (b) sb = (int32_t)(uint32_t)(base >> 32) + __popc(mb & below);
 }
 
 // Append where lanes may target different counters (one per job): lanes
@@ -519,12 +542,10 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
         // the next queue: continuing paths from the front, camera rays from the
         // back (a lane does at most one of the two; every lane takes part in
         // both warp-wide appends)
-        int32_t slot = warp_append(&ctr->n_next, push_next);
-        {
-            const int32_t cs = warp_append(&ctr->n_cam, push_cam);
-            if (push_cam) slot = cs < capacity ? (int32_t)(capacity - 1 - cs) : (int32_t)capacity;
-            push_next = push_next || push_cam;
-        }
+        int32_t slot, cs;
+        warp_append_pair(&ctr->n_next, push_next, push_cam, slot, cs);
+        if (push_cam) slot = cs < capacity ? (int32_t)(capacity - 1 - cs) : (int32_t)capacity;
+        push_next = push_next || push_cam;
         if (push_next) {
             if (slot < capacity) {
                 qn.o[slot] = make_float4(ro.x, ro.y, ro.z, __int_as_float(pix));

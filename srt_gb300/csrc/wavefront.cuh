@@ -73,12 +73,14 @@ struct ShadowQueue {
 };
 
 struct Counters {
-    int32_t n_cur, n_next, n_shadow, n_done;
     // the path queue fills from both ends: paths that continue from the front
     // (n_next), next samples' camera rays from the back (n_cam), so that
-    // camera rays, which traverse coherently, share warps; the current
-    // queue's entries [0, nf_cur) sit at slots 0.., the rest at capacity-1..
-    int32_t n_cam, nf_cur;
+    // camera rays, which traverse coherently, share warps; one 64-bit atomic
+    // counts both (n_next the low word); the current queue's entries
+    // [0, nf_cur) sit at slots 0.., the rest at capacity-1..
+    alignas(8) int32_t n_next;
+    int32_t n_cam;
+    int32_t n_cur, nf_cur, n_shadow, n_done;
     // the previous iteration's shadow rays and ended samples, which this
     // iteration's k_trace and k_regen take
     int32_t n_sp, n_dp;
