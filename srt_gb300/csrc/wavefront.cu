@@ -58,9 +58,11 @@ __device__ __forceinline__ int32_t warp_append(int32_t* counter, bool pred)
 
 static_assert(offsetof(Counters, n_next) % 8 == 0 && offsetof(Counters, n_cam) == offsetof(Counters, n_next) + 4,
               "n_next and n_cam share one 64-bit word");
+static_assert(offsetof(Counters, n_shadow) % 8 == 0 && offsetof(Counters, n_done) == offsetof(Counters, n_shadow) + 4,
+              "n_shadow and n_done share one 64-bit word");
 
 // Two appends with one atomic on a 64-bit word holding both counters (low
-// word: a's, high word: b's); a lane takes part in at most one of them.
+// word: a's, high word: b's); a lane may take part in either or both.
 __device__ __forceinline__ void warp_append_pair(int32_t* counters, bool a, bool b, int32_t& sa, int32_t& sb)
 {
     const uint32_t ma = __ballot_sync(kFull, a), mb = __ballot_sync(kFull, b);
@@ -557,7 +559,8 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                 atomicAdd(&ctr->overflow_queue, 1);
             }
         }
-        slot = warp_append(&ctr->n_shadow, push_shadow);
+        int32_t dslot;
+        warp_append_pair(&ctr->n_shadow, push_shadow, fin, slot, dslot);
         if (push_shadow) {
             if (slot < capacity) {
                 sq.o[slot] = make_float4(sh_o.x, sh_o.y, sh_o.z, __int_as_float(pix));
@@ -567,10 +570,9 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
                 atomicAdd(&ctr->overflow_queue, 1);
             }
         }
-        slot = warp_append(&ctr->n_done, fin);
         if (fin) {
-            if (slot < capacity) {
-                done.rec[slot] = make_uint2((uint32_t)job, (uint32_t)pix);
+            if (dslot < capacity) {
+                done.rec[dslot] = make_uint2((uint32_t)job, (uint32_t)pix);
             } else {
                 atomicAdd(&ctr->overflow_queue, 1);
             }

@@ -80,7 +80,9 @@ struct Counters {
     // [0, nf_cur) sit at slots 0.., the rest at capacity-1..
     alignas(8) int32_t n_next;
     int32_t n_cam;
-    int32_t n_cur, nf_cur, n_shadow, n_done;
+    int32_t n_cur, nf_cur;
+    alignas(8) int32_t n_shadow;  // with n_done: one 64-bit word, one atomic per warp
+    int32_t n_done;
     // the previous iteration's shadow rays and ended samples, which this
     // iteration's k_trace and k_regen take
     int32_t n_sp, n_dp;
