@@ -60,6 +60,8 @@ static_assert(offsetof(Counters, n_next) % 8 == 0 && offsetof(Counters, n_cam) =
               "n_next and n_cam share one 64-bit word");
 static_assert(offsetof(Counters, n_shadow) % 8 == 0 && offsetof(Counters, n_done) == offsetof(Counters, n_shadow) + 4,
               "n_shadow and n_done share one 64-bit word");
+static_assert(offsetof(Counters, n_hit) % 8 == 0 && offsetof(Counters, n_miss) == offsetof(Counters, n_hit) + 4,
+              "n_hit and n_miss share one 64-bit word");
 
 // Two appends with one atomic on a 64-bit word holding both counters (low
 // word: a's, high word: b's); a lane may take part in either or both.
@@ -283,8 +285,12 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(const float4* __restric
         }
         if (t == 0) {
             const int tile_valid = min(kOrderThreads, n - tile);
-            base_hit = atomicAdd(&ctr->n_hit, total);
-            base_miss = atomicAdd(&ctr->n_miss, tile_valid - total);
+            // both counts with one atomic on their shared 64-bit word (n_hit the low word)
+            const unsigned long long b = atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->n_hit),
+                                                   (unsigned long long)(uint32_t)total |
+                                                       ((unsigned long long)(uint32_t)(tile_valid - total) << 32));
+            base_hit = (int)(uint32_t)b;
+            base_miss = (int)(uint32_t)(b >> 32);
         }
         __syncthreads();
         const uint32_t below = (1u << lane) - 1u;

@@ -86,7 +86,8 @@ struct Counters {
     // the previous iteration's shadow rays and ended samples, which this
     // iteration's k_trace and k_regen take
     int32_t n_sp, n_dp;
-    int32_t n_hit, n_miss;  // closest-hit results of the iteration, by kind
+    alignas(8) int32_t n_hit;  // closest-hit results of the iteration, by kind (one 64-bit word)
+    int32_t n_miss;
     unsigned long long fetch_closest, fetch_shadow;
     long long closest_total, shadow_total, iterations, started;
     long long c_nodes, c_tris, s_nodes, s_tris;  // traversal work (profiling kernels)
