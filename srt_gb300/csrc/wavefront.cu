@@ -548,8 +548,8 @@ __global__ void __launch_bounds__(kShadeThreads, SRT_SHADE_MIN_BLOCKS) k_shade(c
             }
         }
         // the next queue: continuing paths from the front, camera rays from the
-        // back (a lane does at most one of the two; every lane takes part in
-        // both warp-wide appends)
+        // back (a lane does at most one of the two; one warp-wide append counts
+        // both, as the next one counts the shadow rays and the ended samples)
         int32_t slot, cs;
         warp_append_pair(&ctr->n_next, push_next, push_cam, slot, cs);
         if (push_cam) slot = cs < capacity ? (int32_t)(capacity - 1 - cs) : (int32_t)capacity;
