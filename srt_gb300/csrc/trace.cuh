@@ -510,43 +510,58 @@ __device__ __forceinline__ bool trav_advance_mixed(TravState& s, Stack& st, int&
     return trav_advance_impl<kCount>(s, st, overflow, any ? scnt : cnt, any);
 }
 
+// A lane's ray index in the persistent loop: 64-bit, or 32-bit where the
+// caller's n is below 2^32 - 1 (a register fewer beside the traversal state).
+template <bool kNarrow>
+struct RayIndex {
+    using T = int64_t;
+    static constexpr T kNone = -1;
+};
+template <>
+struct RayIndex<true> {
+    using T = uint32_t;
+    static constexpr T kNone = 0xffffffffu;
+};
+
 // Drives a warp over rays [0, n) taken from *fetch.  load(i, state, stack)
 // starts ray i (calls trav_init); store(i, state, fin) is called by all 32
 // lanes after every round (so it may use warp-wide votes and appends), with
-// fin set in the lanes whose ray i just finished.
-template <class Advance, class Load, class Store>
+// fin set in the lanes whose ray i just finished.  kNarrow: n < 2^32 - 1.
+template <bool kNarrow = false, class Advance, class Load, class Store>
 __device__ __forceinline__ void trace_persistent_with(int64_t n, unsigned long long* fetch, Stack& st, Advance advance,
                                                       Load load, Store store)
 {
+    using Index = typename RayIndex<kNarrow>::T;
+    constexpr Index kNone = RayIndex<kNarrow>::kNone;
     const uint32_t full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     // Warps past the first n / 32 leave before touching the fetch counter:
     // the ones below take every ray, and a short queue (the end of a frame)
     // does not cost one contended atomic per resident warp of the grid.
     if ((int64_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 >= n) return;
-    int64_t ray = -1;
+    Index ray = kNone;
     TravState s;
     bool drained = false;
     for (;;) {
-        uint32_t idle = __ballot_sync(full, ray < 0);
+        uint32_t idle = __ballot_sync(full, ray == kNone);
         if (!drained && (int)__popc(idle) >= kRefill) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(fetch, (unsigned long long)__popc(idle));
             base = __shfl_sync(full, base, 0);
             if (base + __popc(idle) >= (unsigned long long)n) drained = true;
-            if (ray < 0) {
+            if (ray == kNone) {
                 int64_t idx = (int64_t)base + __popc(idle & ((1u << lane) - 1u));
                 if (idx < n) {
-                    ray = idx;
+                    ray = (Index)idx;
                     load(idx, s, st);
                 }
             }
-            idle = __ballot_sync(full, ray < 0);
+            idle = __ballot_sync(full, ray == kNone);
         }
         if (idle == full && drained) break;
-        const bool fin = ray >= 0 && advance(s, st);
-        store(ray, s, fin);
-        if (fin) ray = -1;
+        const bool fin = ray != kNone && advance(s, st);
+        store((int64_t)ray, s, fin);
+        if (fin) ray = kNone;
     }
 }
 template <bool kAny, bool kCount, class Load, class Store>

@@ -218,7 +218,8 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace(c
     TraceCount cnt, scnt;
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
     Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
-    trace_persistent_with(
+    // ns + nc <= 2 * capacity < 2^32 - 1 (Engine::init): 32-bit ray indices
+    trace_persistent_with<true>(
         ns + nc, &ctr->fetch_closest, st,
         [&](TravState& s, Stack& stk) { return trav_advance_mixed<kCount>(s, stk, overflow, cnt, scnt); },
         [&](int64_t i, TravState& s, Stack& stk) {
