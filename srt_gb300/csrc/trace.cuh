@@ -22,8 +22,6 @@ namespace srt {
 #endif
 constexpr int kStackEntries = SRT_STACK_ENTRIES;  // node groups; at most one per tree level
 
-
-// resident 128-thread traversal blocks per SM the compiler budgets registers for
 #ifndef SRT_SLAB_MARGIN
 #define SRT_SLAB_MARGIN 1.0f  // quantisation steps added to each slab side
 #endif
@@ -35,6 +33,8 @@ constexpr int kStackEntries = SRT_STACK_ENTRIES;  // node groups; at most one pe
 #define SRT_SHADOW_FAR_FIRST 1
 #endif
 
+// resident 128-thread traversal blocks per SM the compiler budgets registers
+// for: 7 (72 registers, no spills)
 #ifndef SRT_TRACE_MIN_BLOCKS
 #define SRT_TRACE_MIN_BLOCKS 7
 #endif

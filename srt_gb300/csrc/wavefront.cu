@@ -306,8 +306,8 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(const float4* __restric
 }
 
 // shading block size and the resident blocks per SM the compiler budgets
-// registers for: 256 x 2 (125 registers, no spills); with the shading order
-// it measured 1 % faster than 128 x 6 (80 registers, spills) and 128 x 4
+// registers for: 256 x 2 (128 registers, 8 bytes spilled); with the shading
+// order it measured 1 % faster than 128 x 6 (80 registers, spills) and 128 x 4
 #ifndef SRT_SHADE_THREADS
 #define SRT_SHADE_THREADS 256
 #endif
