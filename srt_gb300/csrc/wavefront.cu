@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kTraceThreads, SRT_TRACE_MIN_BLOCKS) k_trace(c
     TraceCount cnt, scnt;
     __shared__ uint2 stack_mem[kStackEntries * kTraceThreads];
     Stack st{stack_mem + threadIdx.x, kTraceThreads, 0};
-    // ns + nc <= 2 * capacity < 2^32 - 1 (Engine::init): 32-bit ray indices
+    // ns + nc <= 2 * capacity < 2^32 - 1 (kMaxCapacity): 32-bit ray indices
     trace_persistent_with<true>(
         ns + nc, &ctr->fetch_closest, st,
         [&](TravState& s, Stack& stk) { return trav_advance_mixed<kCount>(s, stk, overflow, cnt, scnt); },
@@ -921,9 +921,14 @@ Engine::~Engine()
     if (host_counters_) cudaFreeHost(host_counters_);
 }
 
+// Largest queue capacity: entry indices fit in int32, and k_trace's rays
+// (shadow plus path entries) in its 32-bit ray indices.
+constexpr int64_t kMaxCapacity = 0x7ffffff0;
+static_assert(2 * kMaxCapacity < (int64_t)RayIndex<true>::kNone, "k_trace ray indices must fit in 32 bits");
+
 srt_status Engine::init(int64_t capacity, int max_jobs)
 {
-    if (capacity <= 0 || capacity > (int64_t)0x7ffffff0 || max_jobs <= 0 || max_jobs > 65535)
+    if (capacity <= 0 || capacity > kMaxCapacity || max_jobs <= 0 || max_jobs > 65535)
         return set_error(SRT_ERR_ARG, "engine capacity out of range");
     capacity_ = capacity;
     max_jobs_ = max_jobs;
