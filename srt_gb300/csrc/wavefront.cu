@@ -983,6 +983,7 @@ srt_status Engine::init(int64_t capacity, int max_jobs)
     grid_trace_ = resident(reinterpret_cast<const void*>(k_trace<false>));
     grid_finish_ = resident(reinterpret_cast<const void*>(k_finish<false>));
     grid_stride_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kThreads - 1) / kThreads, sms * 8));
+    grid_regen_ = std::max(1, grid_stride_ / 2);
     grid_order_ = (int)std::max<int64_t>(1, std::min<int64_t>((capacity + kOrderThreads - 1) / kOrderThreads, sms * 8));
     grid_shade_ = (int)std::max<int64_t>(
         1, std::min<int64_t>((capacity + kShadeThreads - 1) / kShadeThreads, (int64_t)sms * 8 * (256 / kShadeThreads)));
@@ -1033,11 +1034,12 @@ void Engine::launch_iteration(int parity, cudaStream_t st, bool prof, const cuda
     // k_regen (the previous iteration's ended samples) and k_order (this
     // iteration's hits) touch disjoint data: k_regen runs on a forked stream
     // beside k_order, and k_shade, which reads the sample counts k_regen
-    // writes, waits for both
+    // writes, waits for both; k_regen takes half the grid of a lone launch
+    // (grid_regen_), which balances the two branches
     cudaEventRecord(fork_ev_, st);
     cudaStreamWaitEvent(side_stream_, fork_ev_, 0);
     mark_on(side_stream_, 3, 0);
-    k_regen<<<grid_stride_, kThreads, 0, side_stream_>>>(jobs_, done_, counters_, capacity_);
+    k_regen<<<grid_regen_, kThreads, 0, side_stream_>>>(jobs_, done_, counters_, capacity_);
     mark_on(side_stream_, 3, 1);
     cudaEventRecord(join_ev_, side_stream_);
     mark(2, 0);

@@ -215,7 +215,7 @@ private:
     bool cache_ = false;
     bool direct_ = false;
     KernelTimes times_;
-    int grid_trace_ = 0, grid_stride_ = 0, grid_shade_ = 0, grid_order_ = 0, grid_finish_ = 0;
+    int grid_trace_ = 0, grid_stride_ = 0, grid_regen_ = 0, grid_shade_ = 0, grid_order_ = 0, grid_finish_ = 0;
     int32_t tail_below_ = 0;
 };
 
