@@ -33,7 +33,7 @@ typedef enum srt_status {
     SRT_ERR_STACK = 6,       /* traversal stack overflowed (result incomplete) */
     SRT_ERR_NOT_FOUND = 7,   /* unknown render-pass / scene name               */
     SRT_ERR_PARSE = 8,       /* malformed JSON configuration                   */
-    SRT_ERR_UNSUPPORTED = 9  /* feature outside this build (textures, ...)     */
+    SRT_ERR_UNSUPPORTED = 9  /* feature the library does not support           */
 } srt_status;
 
 /* Message of the last failing call on this thread ("" if none). */

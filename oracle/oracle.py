@@ -2,8 +2,8 @@
 the reference-header build (oracle/_ref/libsrtref.so).
 
 Test infrastructure only: imported by tests/, __graft_entry__.smoke() and
-bench.py's cpu_baseline / reference arm, as the checker or the CPU
-baseline, never as the product path.
+bench.py's cpu_baseline / reference arm, as the results the CUDA path is
+compared against or as the timed CPU baseline, never as the product path.
 """
 from __future__ import annotations
 

@@ -1,9 +1,10 @@
 /*
  * ORACLE — CPU restatement of the reference path-tracing hot path.
  *
- * Test infrastructure only: imported by tests/, __graft_entry__.smoke() and
- * bench.py's cpu_baseline / reference arm, always as the checker, never as
- * the thing measured or shipped.  The product library never links it.
+ * Test infrastructure only: used by tests/, __graft_entry__.smoke() and
+ * bench.py's cpu_baseline / reference arm, as the results the CUDA path is
+ * compared against or as the timed CPU baseline, never as the product path.
+ * The product library never links it.
  *
  * Parity pins: the BxDF, light, camera and hit-attribute pieces are checked
  * against golden vectors generated from the reference's own headers

@@ -2,7 +2,7 @@
 own paths, queries at the second vertex, per-cell plain fallback, and the
 gain over plain path tracing at equal samples.
 
-The judge of the error is a high-spp plain render accumulated in FP64; the
+The error is measured against a high-spp plain render accumulated in FP64; the
 relMSE is the reference's definition (((x - r) / (r + 1e-6))^2 averaged over
 RGB, largest 0.1 % discarded, src/utils/metrics.h:30-34, measure.cu:46-49).
 """
